@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark of the FDTD step loop on GB300.
+
+One bench step = one FDTD time step (H and E half-steps with CPML, TF/SF
+plane wave and probe recording) over the whole grid of the workload.
+Default workload: the 256^3 single-grid scattering configuration (c2: 12-cell
+CPML, 40 dielectric/lossy spheres, TF/SF plane wave, 64 probes), synthetic
+seeded inputs; the fields and coefficients (~0.8 GB) exceed the 129 MB L2, so
+no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1|c2|c3]
+  python bench.py --impl reference ...   # the CPU arm (oracle, all cores)
+
+Prints ONE JSON line on rank 0.  Multi-GPU: one process per GPU (torchrun),
+each advancing its own replica of the workload (the path has no exchange);
+value = all ranks' cell-steps / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG_BYTES_STEP = 96   # per cell-step: H half 9 x 4 B, E half 15 x 4 B
+ALG_BYTES_E = 60      # E half-step: read 3 E + 3 H + 6 coefficients, write 3 E
+ALG_BYTES_H = 36      # H half-step: read 3 H + 3 E, write 3 H
+FALLBACK_HBM_GBS = 6800.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------- ranks
+
+class Ranks:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples taken during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        import tempfile
+
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-i", str(self.gpu), "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(workload: str):
+    """DRAM bytes per launch of the E half-step kernel from the committed
+    ncu summary (profiles/ncu_traffic.json), scaled to this workload."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(workload, {}).get("k_half_e_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+# ----------------------------------------------------------------- CPU arm
+
+def cpu_oracle_rate(w, target_s: float, max_steps: int):
+    """Times the FP32 oracle (OpenMP, all host threads) on the workload's grid
+    for a bounded number of steps; returns (Mcell-steps/s, steps, seconds)."""
+    import oracle
+    from maxwell_solver_gb300.workloads import materials, probe_locations, sources
+
+    oracle.build()
+    T = max_steps + 2
+    o = oracle.OracleSim("f32")
+    o.set_params(pml=w.pml, tfsf_width=w.pml + 5)
+    I, J, K = w.dims
+    o.set_const(np.float32([w.fctr, w.delX, w.delT]), np.int32([T, I, J, K, w.n_probes]))
+    pw, cur = sources(w, T)
+    o.set_source(cur)
+    if w.n_probes:
+        o.set_antenna_locations(np.asfortranarray(probe_locations(w)))
+    for flag, arr in materials(w).items():
+        o.update_material(flag, arr)
+    o.ready_simulation()
+    o.init_1d(1.0, pw)
+    o.step(0, w.mode)  # warm-up
+    n, t0 = 1, time.perf_counter()
+    while n <= max_steps:
+        o.step(n, w.mode)
+        n += 1
+        if time.perf_counter() - t0 >= target_s:
+            break
+    dt = time.perf_counter() - t0
+    steps = n - 1
+    o.close()
+    return w.cells * steps / dt / 1e6, steps, dt
+
+
+def run_reference(args, ranks):
+    from maxwell_solver_gb300.workloads import WORKLOADS
+
+    if ranks.rank != 0:
+        return None
+    w = WORKLOADS[args.workload]
+    cores = os.cpu_count()
+    steps = max(1, min(args.steps, 200))
+    rate, done, secs = cpu_oracle_rate(w, target_s=10.0, max_steps=steps)
+    sample = (f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} grid of workload {w.name}, {done} FDTD "
+              f"steps ({secs:.1f} s) of the FP32 CPU restatement, OpenMP {cores} threads")
+    return {
+        "impl": "reference", "metric": "Mcell-steps/s", "value": round(rate, 3),
+        "unit": "Mcell-steps/s", "n_gpus": args.gpus, "steps": done, "warmup": 1,
+        "ms_per_step": round(secs / done * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(w),
+        "cpu_baseline": {"value": round(rate, 3), "unit": "Mcell-steps/s", "cores": cores,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(rate, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("the reference ships no CPU implementation of the step loop; its GPU "
+                 "kernels run only under MATLAB's MEX runtime, so the reference arm is the "
+                 "oracle's restatement of them, pinned bit-exact to the reference's sources"),
+    }
+
+
+def workload_config(w):
+    return {"workload": f"{w.name}: {w.dims[0]}x{w.dims[1]}x{w.dims[2]} Yee grid",
+            "cells": w.cells, "pml": w.pml, "media": w.media, "tfsf_mode": w.mode,
+            "probes": w.n_probes, "config_steps": w.steps,
+            "l2": (f"inputs larger than L2 (fields+coefficients {w.cells * 48 / 1e6:.0f} MB"
+                   " > 129 MB), no flush needed" if w.cells * 48 > 129e6 else
+                   f"state {w.cells * 48 / 1e6:.0f} MB fits in L2: not a headline configuration")}
+
+
+# ----------------------------------------------------------------- GPU arm
+
+def run_ours(args, ranks):
+    from maxwell_solver_gb300 import _native, launch_count, simFDTD
+    from maxwell_solver_gb300.simfdtd import _check
+    from maxwell_solver_gb300.workloads import WORKLOADS, materials, probe_locations, setup, sources
+
+    lib = _native.load()
+    _check(lib.fdtd_set_device(ranks.local))
+    w = WORKLOADS[args.workload]
+    W, K = args.warmup, args.steps
+    KP = max(8, min(64, K // 4))  # per-kernel profiled steps
+    T = W + K + KP
+    P = setup(simFDTD, w, steps=T)
+    h = int(P[0])
+    simFDTD("Synchronize", P)
+
+    simFDTD("StepN", P, np.int32([0, W, w.mode]))
+    simFDTD("Synchronize", P)
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    gpu_index = int(vis) if vis.isdigit() else ranks.local
+    clocks = ClockSampler(gpu_index)
+    ranks.barrier()
+    clocks.start()
+    n0 = launch_count()
+    _check(lib.fdtd_event_record(h, 0))
+    simFDTD("StepN", P, np.int32([W, K, w.mode]))
+    _check(lib.fdtd_event_record(h, 1))
+    simFDTD("Synchronize", P)
+    ms = ctypes_float()
+    _check(lib.fdtd_event_elapsed_ms(h, 0, 1, ms))
+    launches = launch_count() - n0
+    clk = clocks.stop()
+    ranks.barrier()
+    ms_max = ranks.max(ms.value)
+
+    # per-kernel device time, measured live with CUDA events around every launch
+    import ctypes
+
+    acc = (ctypes.c_float * 3)()
+    _check(lib.fdtd_profile_steps(h, W + K, KP, w.mode, None, ctypes.byref(acc)))
+    t_h, t_e, t_o = acc[0] / KP, acc[1] / KP, acc[2] / KP
+    simFDTD("DeleteSimulation", P)
+
+    peak, peak_kind = measured_hbm_peak()
+    cells = w.cells
+    value = cells * K * ranks.world / (ms_max / 1e3) / 1e6
+    ach_e = ALG_BYTES_E * cells / (t_e / 1e3) / 1e9
+    ach_h = ALG_BYTES_H * cells / (t_h / 1e3) / 1e9
+    ach_step = ALG_BYTES_STEP * cells * K / (ms.value / 1e3) / 1e9
+    traffic = ncu_traffic(w.name)
+
+    # end to end through the public per-op interface (host buffers, H2D of
+    # materials and sources, D2H of probes and a field, all inside the timing)
+    e2e = None
+    if ranks.rank == 0 and not args.no_e2e:
+        e2e = run_e2e(w, K, simFDTD, materials, probe_locations, sources)
+
+    cpu = None
+    if ranks.rank == 0 and not args.no_cpu:
+        rate, done, secs = cpu_oracle_rate(w, target_s=args.cpu_seconds, max_steps=200)
+        cpu = {"value": round(rate, 3), "unit": "Mcell-steps/s", "cores": os.cpu_count(),
+               "kind": "port",
+               "sample": f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} grid, {done} steps "
+                         f"({secs:.1f} s) of the FP32 oracle, OpenMP all host threads"}
+    ranks.close()
+    if ranks.rank != 0:
+        return None
+    return {
+        "metric": "Mcell-steps/s", "value": round(value, 2), "unit": "Mcell-steps/s",
+        "n_gpus": ranks.world, "steps": K, "warmup": W, "ms_per_step": round(ms_max / K, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded spheres/layers, Gaussian-modulated plane wave)",
+        "config": {**workload_config(w), "parallelism": f"replicas x{ranks.world}",
+                   "timed": "fdtd_step_n: 2 fused kernels + probe gather per step, CUDA graph"},
+        "roofline": {"bound": "hbm", "kernel": "k_half_e (E half-step)",
+                     "achieved": round(ach_e, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(ach_e / peak, 4), "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "alg_bytes_per_cell": ALG_BYTES_E, "units_per_launch": cells,
+                     "avg_launch_ms": round(t_e, 5),
+                     "h_kernel": {"achieved": round(ach_h, 1), "frac": round(ach_h / peak, 4),
+                                  "alg_bytes_per_cell": ALG_BYTES_H, "avg_launch_ms": round(t_h, 5)},
+                     "probe_gather_ms": round(t_o, 5),
+                     "step": {"achieved": round(ach_step, 1), "frac": round(ach_step / peak, 4),
+                              "alg_bytes_per_cell_step": ALG_BYTES_STEP}},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+
+
+def ctypes_float():
+    import ctypes
+
+    return ctypes.c_float(0.0)
+
+
+def run_e2e(w, K, simFDTD, materials, probe_locations, sources):
+    I, J, K3 = w.dims
+    T = K
+    mats = materials(w)
+    pw, cur = sources(w, T)
+    loc = np.asfortranarray(probe_locations(w))
+    ijk = w.cells
+    t0 = time.perf_counter()
+    P = simFDTD("CreateSimulation")
+    simFDTD("SetParams", P, np.float64([w.pml, w.pml + 5, 3, 1, 0.08, 1, 0.8, 0]))
+    simFDTD("SetConst", P, np.float32([w.fctr, w.delX, w.delT]), np.int32([T, I, J, K3, w.n_probes]))
+    simFDTD("SetSource", P, cur)
+    simFDTD("SetAntennaLocations", P, loc)
+    for flag, arr in mats.items():
+        simFDTD("UpdateMaterial", P, np.int32(flag), arr)
+    simFDTD("ReadySimulation", P)
+    simFDTD("Init1D", P, np.float32(1.0), pw)
+    simFDTD("UpdateCuda", P)
+    simFDTD("ResetFieldAll", P)
+    m = w.mode
+    for n in range(K):
+        tm = np.array([n, m], dtype=np.int32)
+        simFDTD("UpdateH_All", P)
+        simFDTD("UpdateH_PlaneWave", P, tm)
+        simFDTD("UpdateH_PML", P)
+        simFDTD("UpdateE_All", P)
+        simFDTD("UpdateE_PlaneWave", P, tm)
+        simFDTD("UpdateE_PML", P)
+    probes = simFDTD("OutputProbes", P, np.uint32(T * w.n_probes * 6))
+    ez = simFDTD("OutputVis", P, np.uint32(ijk), np.int32(3))
+    simFDTD("DeleteSimulation", P)
+    dt = time.perf_counter() - t0
+    assert np.isfinite(ez).all() and np.isfinite(probes).all()
+    h2d = 2 * 6 * ijk * 4 + 2 * T * 4 + loc.size * 4
+    d2h = ijk * 4 + probes.size * 4
+    return {"value": round(ijk * K / dt / 1e6, 2), "unit": "Mcell-steps/s",
+            "h2d_bytes_per_step": int(round(h2d / K)), "d2h_bytes_per_step": int(round(d2h / K)),
+            "seconds": round(dt, 3),
+            "path": "simFDTD per-op calls (6 per step, as highfrequency.m) incl. setup, "
+                    "material/source upload, probe + Ez readout"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", default="c2", choices=("c1", "c2", "c3"))
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ranks = Ranks()
+    if args.impl == "reference":
+        out = run_reference(args, ranks)
+        ranks.close()
+    else:
+        out = run_ours(args, ranks)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

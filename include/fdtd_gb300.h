@@ -1,0 +1,217 @@
+/*
+ * fdtd_gb300.h -- C ABI of the GB300 (sm_103a) FDTD step loop.
+ *
+ * Drop-in replacement for the operations behind the reference's MEX entry
+ * point simFDTD (enricoballini/maxwell_solver, src/simFDTD.cu:19-187).  Each
+ * function below replaces one op string of that dispatcher; the comment on
+ * each cites the dispatcher branch and the `simulation` method it calls
+ * (src/simulation.h).  Argument meaning, units, array layouts (x fastest,
+ * i + j*Imax + k*Imax*Jmax) and the order in which the ops may be called are
+ * the reference's.  A MATLAB binding is maxwell_solver_gb300/csrc/mex/
+ * simFDTD_mex.c; a Python binding is maxwell_solver_gb300.simfdtd.
+ *
+ * Conventions
+ *  - Every function returns an fdtd_status; FDTD_OK is 0.  On failure,
+ *    fdtd_last_error() gives a message (thread-local).
+ *  - Handles are opaque 64-bit ids checked against a registry: a deleted or
+ *    forged handle yields FDTD_ERR_INVALID_HANDLE instead of a crash.
+ *  - All pointers are host pointers; lengths are element counts.  Work is
+ *    queued on the handle's own CUDA stream; only the output functions wait.
+ *  - Fields, coefficients and CPML state stay in device memory (HBM) for
+ *    the lifetime of the handle.
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef uint64_t fdtd_handle;
+
+typedef enum {
+  FDTD_OK = 0,
+  FDTD_ERR_INVALID_HANDLE = 1,   /* unknown / deleted handle */
+  FDTD_ERR_INVALID_ARG = 2,      /* bad size, flag, index, null pointer */
+  FDTD_ERR_STATE = 3,            /* op called before its prerequisite */
+  FDTD_ERR_ALREADY_INITIALIZED = 4, /* SetConst twice (simFDTD:AlreadyInitialized) */
+  FDTD_ERR_CUDA = 5,             /* CUDA runtime / launch error */
+  FDTD_ERR_OOM = 6,              /* device or pinned allocation failed */
+  FDTD_ERR_UNSUPPORTED = 7       /* outside the supported envelope */
+} fdtd_status;
+
+/* Extension (no reference counterpart): runtime CPML and TF/SF settings.
+ * fdtd_default_params() returns the reference's compile-time constants
+ * (src/simulation.h:17, :86-90, :102): pml 10, poly_m 3, alpha_m 1,
+ * alpha_max 0.08, kappa_max 1, sigma_max = 0.8 (m+1) / (eta dx), inset 15.
+ * When r0 > 0, sigma_max = -(m+1) ln(r0) / (2 eta pml dx) instead. */
+typedef struct {
+  int32_t pml;          /* CPML thickness in cells, 2..32 */
+  int32_t tfsf_width;   /* TF/SF box inset from the outer boundary */
+  double poly_m, alpha_m, alpha_max, kappa_max, sig_factor, r0;
+} fdtd_params;
+
+fdtd_params fdtd_default_params(void);
+/* Must precede fdtd_set_const. */
+int fdtd_set_params(fdtd_handle h, const fdtd_params *p);
+
+/* 'CreateSimulation' -- src/simFDTD.cu:30-38, simulation::simulation()
+ * src/simulation.h:71-77.  Creates a handle with its own CUDA stream. */
+int fdtd_create(fdtd_handle *out);
+
+/* 'DeleteSimulation' -- src/simFDTD.cu:49-52, ~simulation()
+ * src/simulation.h:1153-1269. */
+int fdtd_destroy(fdtd_handle h);
+
+/* 'SetConst' -- src/simFDTD.cu:103-110, setConst src/simulation.h:79-131.
+ * freqRes = [fctr, delX, delT]; timeDim = [T, Imax, Jmax, Kmax, numAnt].
+ * A second call fails with FDTD_ERR_ALREADY_INITIALIZED. */
+int fdtd_set_const(fdtd_handle h, const float freqRes[3], const int32_t timeDim[5]);
+
+/* 'SetSource' with 3 arguments -- src/simFDTD.cu:111-125, setSource
+ * src/simulation.h:1068-1082.  n must be >= T; the first T values are used.
+ * A second call is ignored (the reference prints and returns). */
+int fdtd_set_source(fdtd_handle h, const float *src, size_t n);
+
+/* 'SetSource' with a 4th argument -- updateSource src/simulation.h:1084-1095. */
+int fdtd_update_source(fdtd_handle h, const float *src, size_t n);
+
+/* 'UpdateMaterial' -- src/simFDTD.cu:150-157, updateMaterial
+ * src/simulation.h:288-328.  flag 1,2,3 = sigma_x,y,z; 4,5,6 = eps_x,y,z;
+ * other flags are ignored.  Takes effect at ReadySimulation / UpdateCuda. */
+int fdtd_update_material(fdtd_handle h, int32_t flag, const float *values, size_t n);
+
+/* 'CreateMu' -- src/simFDTD.cu:133-141, createMu src/simulation.h:28-68.
+ * As in the reference, a call after ReadySimulation computes the
+ * coefficients but leaves the H update unchanged; a call before it is
+ * rejected with FDTD_ERR_STATE (the reference reads unset state there). */
+int fdtd_create_mu(fdtd_handle h, const float *mu_x, const float *mu_y,
+                   const float *mu_z, size_t n);
+
+/* 'SetAntennaLocations' -- src/simFDTD.cu:126-132, setAntennaLocations
+ * src/simulation.h:1047-1067.  loc is numAnt x 3 int32, column-major
+ * (x column, then y, then z), offsets inside the CPML (pml is added).
+ * Must precede ReadySimulation (src/simulation.h:954). */
+int fdtd_set_antenna_locations(fdtd_handle h, const int32_t *loc, size_t n);
+
+/* 'ReadySimulation' -- src/simFDTD.cu:81-84, readySimulation
+ * src/simulation.h:640-979: CPML tables, coefficients, field allocation. */
+int fdtd_ready_simulation(fdtd_handle h);
+
+/* 'Init1D' -- src/simFDTD.cu:142-149, init1D src/simulation.h:134-254.
+ * Precomputes the forward and inverse 1D incident runs for all T steps
+ * (one launch).  Requires ReadySimulation. */
+int fdtd_init_1d(fdtd_handle h, float rate, const float *pw_source, size_t n);
+
+/* 'UpdateCuda' -- src/simFDTD.cu:69-72, updateCuda src/simulation.h:1097-1127. */
+int fdtd_update_cuda(fdtd_handle h);
+
+/* 'ResetFieldAll' -- src/simFDTD.cu:85-88, src/simulation.h:1128-1151.
+ * Also rewinds the probe recorder to row 0. */
+int fdtd_reset_field_all(fdtd_handle h);
+
+/* 'UpdateH_All' -- src/simFDTD.cu:57-60, src/simulation.h:371-385. */
+int fdtd_update_h_all(fdtd_handle h);
+/* 'UpdateE_All' -- src/simFDTD.cu:53-56, src/simulation.h:386-391. */
+int fdtd_update_e_all(fdtd_handle h);
+/* 'UpdateH_PML' -- src/simFDTD.cu:65-68, src/simulation.h:392-403. */
+int fdtd_update_h_pml(fdtd_handle h);
+/* 'UpdateE_PML' -- src/simFDTD.cu:61-64, src/simulation.h:404-418. */
+int fdtd_update_e_pml(fdtd_handle h);
+/* 'UpdateH_PlaneWave' [step, mode] -- src/simFDTD.cu:96-102,
+ * src/simulation.h:330-349.  mode 1..4; other modes do nothing. */
+int fdtd_update_h_planewave(fdtd_handle h, int32_t step, int32_t mode);
+/* 'UpdateE_PlaneWave' [step, mode] -- src/simFDTD.cu:89-95,
+ * src/simulation.h:350-369. */
+int fdtd_update_e_planewave(fdtd_handle h, int32_t step, int32_t mode);
+
+/* 'AddCurrents' [step, mode], [i0 i1 j0 j1 k0 k1] -- src/simFDTD.cu:73-80,
+ * addCurrents src/simulation.h:256-286.  mode 1,2,3 = Ex,Ey,Ez. */
+int fdtd_add_currents(fdtd_handle h, int32_t step, int32_t mode, const int32_t box[6]);
+
+/* 'OutputAnt' N -- src/simFDTD.cu:159-168, outputAnt src/simulation.h:621-638.
+ * Writes min(n, numAnt*T) values: the Ez probe record, probe fastest
+ * (value of probe a at step row r at a + r*numAnt).  Row r holds the fields
+ * at the start of step r (before its H update), r counting UpdateH_All
+ * calls since ResetFieldAll.  (The reference allocates this record but
+ * never fills it.) */
+int fdtd_output_ant(fdtd_handle h, float *out, size_t n);
+
+/* 'OutputVis' N, flag -- src/simFDTD.cu:169-179, outputVis
+ * src/simulation.h:572-619.  flag 1,2,3 = Ex,Ey,Ez; 0,-1,-2 = sigma_x,y,z.
+ * Extension: 4,5,6 = Hx,Hy,Hz; -3,-4,-5 = eps_x,y,z.  Writes
+ * min(n, Imax*Jmax*Kmax) values; other flags write nothing. */
+int fdtd_output_vis(fdtd_handle h, float *out, size_t n, int32_t flag);
+
+/* ---------------------------------------------------------------------
+ * Extensions (no reference counterpart)
+ * --------------------------------------------------------------------- */
+
+/* Current-source description for fdtd_step_n (mode 0 = none). */
+typedef struct {
+  int32_t mode;     /* 1,2,3 = Ex,Ey,Ez */
+  int32_t box[6];   /* i0 i1 j0 j1 k0 k1 */
+} fdtd_current;
+
+/* Runs steps first..first+count-1 of the reference step order
+ * (highfrequency.m:85-91, plus AddCurrents as in GICsimulation.m:119-124
+ * when cur != NULL and cur->mode != 0), each step as two fused half-step
+ * kernels, with the loop captured in a CUDA graph.  tfsf_mode 0 skips the
+ * plane-wave corrections.  Bitwise identical to issuing the per-op calls. */
+int fdtd_step_n(fdtd_handle h, int32_t first, int32_t count, int32_t tfsf_mode,
+                const fdtd_current *cur);
+
+/* All six probe components: out[(r*numAnt + a)*6 + c], c = Ex,Ey,Ez,Hx,Hy,Hz. */
+int fdtd_output_probes(fdtd_handle h, float *out, size_t n);
+
+/* Waits for the handle's stream. */
+int fdtd_synchronize(fdtd_handle h);
+
+typedef struct {
+  int32_t I, J, K, T, num_ant, pml, size_1d;
+  int32_t i0, i1, j0, j1, k0, k1;
+  int32_t coef_mode;       /* 0 per-cell arrays, 1 material-indexed */
+  int32_t num_materials;   /* distinct coefficient tuples (coef_mode 1) */
+  uint64_t device_bytes;   /* device memory held by the handle */
+  float Chh, Che;
+} fdtd_info;
+int fdtd_get_info(fdtd_handle h, fdtd_info *out);
+
+/* Copies one of the CPML tables (0 b_E, 1 c_E, 2 b_H, 3 c_H: 2*pml floats)
+ * or the x-only stretch denominators (4 den_ex, 5 den_hx: Imax floats). */
+int fdtd_get_table(fdtd_handle h, int32_t which, float *out, size_t n);
+
+/* Timing on the handle's stream (CUDA events).  slot 0..15. */
+int fdtd_event_record(fdtd_handle h, int32_t slot);
+int fdtd_event_elapsed_ms(fdtd_handle h, int32_t slot_a, int32_t slot_b, float *ms);
+
+/* Runs steps like fdtd_step_n but with direct launches and a CUDA event
+ * pair around every kernel; adds the summed device time of the H half-step
+ * kernels, the E half-step kernels and the remaining kernels (probe gather)
+ * to ms_out[0..2].  For measurement only. */
+int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t tfsf_mode,
+                       const fdtd_current *cur, float ms_out[3]);
+
+/* Selects the CUDA device used by handles created afterwards on the calling
+ * thread (one process per GPU: pass the local rank). */
+int fdtd_set_device(int32_t device);
+
+/* Number of kernels this library has launched (all handles). */
+uint64_t fdtd_launch_count(void);
+
+/* Message for the last failing call on this thread. */
+const char *fdtd_last_error(void);
+
+/* Source waveform of FunLib('CreateSignal', ...) --
+ * src/cpucode/FunLib.cpp:6-45 (double precision, 1-based n). */
+int fdtd_create_signal(double fctr, double delT, double percentage_bw,
+                       double num_side_lobes, size_t time_steps, double *out,
+                       double *fmaxx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,112 @@
+"""ctypes binding of libfdtd_gb300.so (the C ABI of include/fdtd_gb300.h).
+
+The library is built in-tree (maxwell_solver_gb300/build.py).  There is no
+CPU fallback: if the library cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from .build import LIB
+
+_lock = threading.Lock()
+_lib = None
+
+P = ctypes.c_void_p
+U64 = ctypes.c_uint64
+I32 = ctypes.c_int32
+SZ = ctypes.c_size_t
+
+
+class FdtdParams(ctypes.Structure):
+    _fields_ = [("pml", I32), ("tfsf_width", I32), ("poly_m", ctypes.c_double),
+                ("alpha_m", ctypes.c_double), ("alpha_max", ctypes.c_double),
+                ("kappa_max", ctypes.c_double), ("sig_factor", ctypes.c_double),
+                ("r0", ctypes.c_double)]
+
+
+class FdtdCurrent(ctypes.Structure):
+    _fields_ = [("mode", I32), ("box", I32 * 6)]
+
+
+class FdtdInfo(ctypes.Structure):
+    _fields_ = [("I", I32), ("J", I32), ("K", I32), ("T", I32), ("num_ant", I32),
+                ("pml", I32), ("size_1d", I32), ("i0", I32), ("i1", I32), ("j0", I32),
+                ("j1", I32), ("k0", I32), ("k1", I32), ("coef_mode", I32),
+                ("num_materials", I32), ("device_bytes", ctypes.c_uint64),
+                ("Chh", ctypes.c_float), ("Che", ctypes.c_float)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "fdtd_default_params": (FdtdParams, []),
+    "fdtd_set_params": (ctypes.c_int, [U64, ctypes.POINTER(FdtdParams)]),
+    "fdtd_create": (ctypes.c_int, [ctypes.POINTER(U64)]),
+    "fdtd_destroy": (ctypes.c_int, [U64]),
+    "fdtd_set_const": (ctypes.c_int, [U64, P, P]),
+    "fdtd_set_source": (ctypes.c_int, [U64, P, SZ]),
+    "fdtd_update_source": (ctypes.c_int, [U64, P, SZ]),
+    "fdtd_update_material": (ctypes.c_int, [U64, I32, P, SZ]),
+    "fdtd_create_mu": (ctypes.c_int, [U64, P, P, P, SZ]),
+    "fdtd_set_antenna_locations": (ctypes.c_int, [U64, P, SZ]),
+    "fdtd_ready_simulation": (ctypes.c_int, [U64]),
+    "fdtd_init_1d": (ctypes.c_int, [U64, ctypes.c_float, P, SZ]),
+    "fdtd_update_cuda": (ctypes.c_int, [U64]),
+    "fdtd_reset_field_all": (ctypes.c_int, [U64]),
+    "fdtd_update_h_all": (ctypes.c_int, [U64]),
+    "fdtd_update_e_all": (ctypes.c_int, [U64]),
+    "fdtd_update_h_pml": (ctypes.c_int, [U64]),
+    "fdtd_update_e_pml": (ctypes.c_int, [U64]),
+    "fdtd_update_h_planewave": (ctypes.c_int, [U64, I32, I32]),
+    "fdtd_update_e_planewave": (ctypes.c_int, [U64, I32, I32]),
+    "fdtd_add_currents": (ctypes.c_int, [U64, I32, I32, P]),
+    "fdtd_output_ant": (ctypes.c_int, [U64, P, SZ]),
+    "fdtd_output_vis": (ctypes.c_int, [U64, P, SZ, I32]),
+    "fdtd_step_n": (ctypes.c_int, [U64, I32, I32, I32, ctypes.POINTER(FdtdCurrent)]),
+    "fdtd_output_probes": (ctypes.c_int, [U64, P, SZ]),
+    "fdtd_synchronize": (ctypes.c_int, [U64]),
+    "fdtd_get_info": (ctypes.c_int, [U64, ctypes.POINTER(FdtdInfo)]),
+    "fdtd_get_table": (ctypes.c_int, [U64, I32, P, SZ]),
+    "fdtd_event_record": (ctypes.c_int, [U64, I32]),
+    "fdtd_event_elapsed_ms": (ctypes.c_int, [U64, I32, I32, ctypes.POINTER(ctypes.c_float)]),
+    "fdtd_profile_steps": (ctypes.c_int, [U64, I32, I32, I32, ctypes.POINTER(FdtdCurrent),
+                                          ctypes.POINTER(ctypes.c_float * 3)]),
+    "fdtd_set_device": (ctypes.c_int, [I32]),
+    "fdtd_launch_count": (ctypes.c_uint64, []),
+    "fdtd_last_error": (ctypes.c_char_p, []),
+    "fdtd_create_signal": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, SZ, P, ctypes.POINTER(ctypes.c_double)]),
+}
+
+
+def lib_path() -> str:
+    return os.environ.get("FDTD_GB300_LIB", LIB)
+
+
+def load():
+    """Loads (never builds) the native library; raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = lib_path()
+            if not os.path.exists(path):
+                raise ImportError(
+                    f"libfdtd_gb300.so not found at {path}: run "
+                    "`python -c 'import __graft_entry__ as g; g.build()'` "
+                    "(there is no CPU fallback)")
+            lib = ctypes.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+STATUS_NAMES = {
+    0: "FDTD_OK", 1: "FDTD_ERR_INVALID_HANDLE", 2: "FDTD_ERR_INVALID_ARG",
+    3: "FDTD_ERR_STATE", 4: "FDTD_ERR_ALREADY_INITIALIZED", 5: "FDTD_ERR_CUDA",
+    6: "FDTD_ERR_OOM", 7: "FDTD_ERR_UNSUPPORTED",
+}

@@ -1,0 +1,1126 @@
+/*
+ * fdtd_host.c -- host side of the GB300 FDTD solver (plain C11).
+ *
+ * Implements the public C ABI of include/fdtd_gb300.h: the state and setup
+ * of the reference's `simulation` class (enricoballini/maxwell_solver
+ * src/simulation.h) and the dispatch of its per-op calls onto the fused
+ * sm_103a kernels of fdtd_kernels.cu through the launchers declared in
+ * fdtd_internal.h.
+ *
+ * Per-op calls are fused lazily: UpdateH_All, UpdateH_PlaneWave and
+ * UpdateH_PML arriving in the reference order (highfrequency.m:85-91) are
+ * queued and issued as one H half-step kernel when the next op needs their
+ * result; the same for UpdateE_All / UpdateE_PlaneWave / UpdateE_PML /
+ * AddCurrents.  Every op only touches its own cell's fields given the other
+ * family, so the fused kernel applies exactly the same operations in the
+ * same order.  Ops arriving out of that order flush the queue first.
+ */
+#define _GNU_SOURCE
+#include <math.h>
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "../../include/fdtd_gb300.h"
+#include "fdtd_internal.h"
+
+/* physical constants, src/simulation.h:19-21 */
+#define K_PI 3.14159265358979323846
+static const double k_c0 = 299792458;
+#define K_MU0 (4 * K_PI * 1e-7)
+#define K_EPS0 (1 / k_c0 / k_c0 / K_MU0)
+
+#define MAX_EVENTS 16
+#define GRAPH_CHUNK 32
+
+/* ------------------------------------------------------------ errors */
+
+static __thread char g_err[512];
+
+static int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+const char *fdtd_last_error(void) { return g_err; }
+
+#define CU(call)                                                           \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess)                                                 \
+      return fail(e_ == cudaErrorMemoryAllocation ? FDTD_ERR_OOM : FDTD_ERR_CUDA, \
+                  "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                               \
+  } while (0)
+
+#define KL(call)                                                           \
+  do {                                                                     \
+    int e_ = (call);                                                       \
+    if (e_ != 0)                                                           \
+      return fail(FDTD_ERR_CUDA, "%s: %s", #call,                          \
+                  cudaGetErrorString((cudaError_t)e_));                    \
+  } while (0)
+
+/* ------------------------------------------------------------ state */
+
+typedef struct {
+  int active;      /* something queued */
+  int h;           /* 1: H family, 0: E family */
+  fdtd_op op;
+} pending_t;
+
+typedef struct sim {
+  fdtd_params prm;
+  int init_const, init_ready, init_1d, init_src, init_ant, init_mu;
+  int32_t I, J, K, T, num_ant, p, size1d;
+  int64_t IJ, IJK;
+  float fctr, delX, delT;
+  float poly_m, alpha_m, sig_max, alpha_max, kappa_max;
+  int32_t i0, i1, j0, j1, k0, k1;
+  int64_t size_x, size_y, size_z;
+  /* host copies (reference: pinned arrays of setConst / setSource) */
+  float *h_mat[6];      /* sigma_x,y,z, eps_x,y,z */
+  float *h_src;
+  int64_t *h_probe_idx;
+  float bE[2 * FDTD_MAX_PML], cE[2 * FDTD_MAX_PML];
+  float bH[2 * FDTD_MAX_PML], cH[2 * FDTD_MAX_PML];
+  float *h_den_ex, *h_den_hx;
+  float Chh, Che;
+  /* device */
+  cudaStream_t stream;
+  cudaEvent_t ev[MAX_EVENTS];
+  float *d_f[6], *d_ce[6], *d_psi_pool, *d_psi[FDTD_NUM_PSI];
+  float *d_den_ex, *d_den_hx, *d_inc[4], *d_src, *d_probes, *d_mu[3];
+  int64_t *d_probe_idx;
+  int32_t *d_ctr; /* [0] step base, [1] probe row */
+  uint64_t device_bytes;
+  fdtd_dev dev;
+  pending_t pend;
+  /* graph cache for fdtd_step_n */
+  cudaGraphExec_t gexec;
+  int g_mode, g_cur_mode, g_cur_box[6], g_probes;
+  unsigned long long g_kernels;
+} sim;
+
+/* ------------------------------------------------------------ registry */
+
+#define MAX_SIMS 4096
+static pthread_mutex_t g_reg_lock = PTHREAD_MUTEX_INITIALIZER;
+static sim *g_sims[MAX_SIMS];
+static uint32_t g_gen[MAX_SIMS];
+static unsigned long long g_graph_kernels = 0, g_captured_kernels = 0;
+
+static sim *lookup(fdtd_handle h) {
+  uint32_t slot = (uint32_t)(h & 0xffffffffu);
+  uint32_t gen = (uint32_t)(h >> 32);
+  if (slot == 0 || slot > MAX_SIMS) return NULL;
+  pthread_mutex_lock(&g_reg_lock);
+  sim *s = (g_gen[slot - 1] == gen) ? g_sims[slot - 1] : NULL;
+  pthread_mutex_unlock(&g_reg_lock);
+  return s;
+}
+
+#define GET(h)                                                             \
+  sim *s = lookup(h);                                                      \
+  if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "invalid simulation handle")
+
+uint64_t fdtd_launch_count(void) {
+  return (uint64_t)(fdtdk_launch_count() - g_captured_kernels + g_graph_kernels);
+}
+
+fdtd_params fdtd_default_params(void) {
+  fdtd_params p;
+  p.pml = 10;
+  p.tfsf_width = 15;
+  p.poly_m = 3;
+  p.alpha_m = 1.0;
+  p.alpha_max = 0.08;
+  p.kappa_max = 1.0;
+  p.sig_factor = 0.8;
+  p.r0 = 0.0;
+  return p;
+}
+
+int fdtd_create(fdtd_handle *out) {
+  if (!out) return fail(FDTD_ERR_INVALID_ARG, "null output handle");
+  sim *s = (sim *)calloc(1, sizeof(sim));
+  if (!s) return fail(FDTD_ERR_OOM, "out of host memory");
+  s->prm = fdtd_default_params();
+  cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    free(s);
+    return fail(FDTD_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  for (int i = 0; i < MAX_EVENTS; ++i) cudaEventCreate(&s->ev[i]);
+  pthread_mutex_lock(&g_reg_lock);
+  int slot = -1;
+  for (int i = 0; i < MAX_SIMS; ++i)
+    if (!g_sims[i]) {
+      slot = i;
+      break;
+    }
+  if (slot < 0) {
+    pthread_mutex_unlock(&g_reg_lock);
+    for (int i = 0; i < MAX_EVENTS; ++i) cudaEventDestroy(s->ev[i]);
+    cudaStreamDestroy(s->stream);
+    free(s);
+    return fail(FDTD_ERR_OOM, "too many live simulations");
+  }
+  g_sims[slot] = s;
+  g_gen[slot] += 1;
+  *out = ((uint64_t)g_gen[slot] << 32) | (uint64_t)(slot + 1);
+  pthread_mutex_unlock(&g_reg_lock);
+  return FDTD_OK;
+}
+
+static void dfree(void *p) {
+  if (p) cudaFree(p);
+}
+
+int fdtd_destroy(fdtd_handle h) {
+  uint32_t slot = (uint32_t)(h & 0xffffffffu);
+  sim *s = lookup(h);
+  if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "invalid simulation handle");
+  pthread_mutex_lock(&g_reg_lock);
+  g_sims[slot - 1] = NULL;
+  pthread_mutex_unlock(&g_reg_lock);
+  cudaStreamSynchronize(s->stream);
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  for (int a = 0; a < 6; ++a) {
+    dfree(s->d_f[a]);
+    dfree(s->d_ce[a]);
+    free(s->h_mat[a]);
+  }
+  for (int a = 0; a < 4; ++a) dfree(s->d_inc[a]);
+  for (int a = 0; a < 3; ++a) dfree(s->d_mu[a]);
+  dfree(s->d_psi_pool);
+  dfree(s->d_den_ex);
+  dfree(s->d_den_hx);
+  dfree(s->d_src);
+  dfree(s->d_probes);
+  dfree(s->d_probe_idx);
+  dfree(s->d_ctr);
+  free(s->h_src);
+  free(s->h_probe_idx);
+  free(s->h_den_ex);
+  free(s->h_den_hx);
+  for (int i = 0; i < MAX_EVENTS; ++i) cudaEventDestroy(s->ev[i]);
+  cudaStreamDestroy(s->stream);
+  free(s);
+  return FDTD_OK;
+}
+
+static int dalloc(sim *s, void **p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 4);
+  if (e != cudaSuccess)
+    return fail(FDTD_ERR_OOM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  s->device_bytes += bytes;
+  return FDTD_OK;
+}
+
+/* ------------------------------------------------------------ setup */
+
+int fdtd_set_params(fdtd_handle h, const fdtd_params *p) {
+  GET(h);
+  if (!p) return fail(FDTD_ERR_INVALID_ARG, "null params");
+  if (s->init_const) return fail(FDTD_ERR_STATE, "SetParams must precede SetConst");
+  if (p->pml < 2 || p->pml > FDTD_MAX_PML)
+    return fail(FDTD_ERR_UNSUPPORTED, "pml must be in [2, %d]", FDTD_MAX_PML);
+  if (p->tfsf_width < 1) return fail(FDTD_ERR_INVALID_ARG, "tfsf_width must be >= 1");
+  s->prm = *p;
+  return FDTD_OK;
+}
+
+/* src/simulation.h:79-131 */
+int fdtd_set_const(fdtd_handle h, const float freqRes[3], const int32_t timeDim[5]) {
+  GET(h);
+  if (s->init_const)
+    return fail(FDTD_ERR_ALREADY_INITIALIZED, "SetConst: already called.");
+  if (!freqRes || !timeDim) return fail(FDTD_ERR_INVALID_ARG, "freqRes and TimeDim required.");
+  const int32_t T = timeDim[0], I = timeDim[1], J = timeDim[2], K = timeDim[3];
+  const int32_t na = timeDim[4];
+  const int32_t p = s->prm.pml;
+  if (T < 1 || na < 0) return fail(FDTD_ERR_INVALID_ARG, "TimeDim: T >= 1, numAnt >= 0");
+  if (I < 2 * p + 2 || J < 2 * p + 2 || K < 2 * p + 2)
+    return fail(FDTD_ERR_UNSUPPORTED, "grid %dx%dx%d too small for a %d-cell CPML", I, J, K, p);
+  if (!(freqRes[1] > 0.0f) || !(freqRes[2] > 0.0f))
+    return fail(FDTD_ERR_INVALID_ARG, "delX and delT must be positive");
+  s->fctr = freqRes[0];
+  s->delX = freqRes[1];
+  s->delT = freqRes[2];
+  s->poly_m = (float)s->prm.poly_m;
+  s->alpha_m = (float)s->prm.alpha_m;
+  if (s->prm.r0 > 0.0)
+    s->sig_max = (float)(-((double)s->poly_m + 1.0) * log(s->prm.r0) /
+                         (2.0 * sqrt(K_MU0 / K_EPS0) * (double)p * (double)s->delX));
+  else
+    s->sig_max = (float)(s->prm.sig_factor * ((double)s->poly_m + 1.0) /
+                         (sqrt(K_MU0 / K_EPS0) * (double)s->delX));
+  s->alpha_max = (float)s->prm.alpha_max;
+  s->kappa_max = (float)s->prm.kappa_max;
+  s->T = T;
+  s->I = I;
+  s->J = J;
+  s->K = K;
+  s->num_ant = na;
+  s->p = p;
+  s->IJ = (int64_t)I * J;
+  s->IJK = s->IJ * K;
+  const int32_t w = s->prm.tfsf_width;
+  s->i0 = w;
+  s->i1 = I - w - 1;
+  s->j0 = w;
+  s->j1 = J - w - 1;
+  s->k0 = w;
+  s->k1 = K - w - 1;
+  s->size_x = (int64_t)p * J * K;
+  s->size_y = (int64_t)I * p * K;
+  s->size_z = (int64_t)I * J * p;
+  for (int a = 0; a < 6; ++a) {
+    s->h_mat[a] = (float *)malloc((size_t)s->IJK * sizeof(float));
+    if (!s->h_mat[a]) return fail(FDTD_ERR_OOM, "out of host memory");
+    const float v = a < 3 ? 0.0f : 1.0f;
+    for (int64_t n = 0; n < s->IJK; ++n) s->h_mat[a][n] = v;
+  }
+  s->init_const = 1;
+  return FDTD_OK;
+}
+
+/* src/simulation.h:1068-1082 */
+int fdtd_set_source(fdtd_handle h, const float *src, size_t n) {
+  GET(h);
+  if (!s->init_const) return fail(FDTD_ERR_STATE, "SetSource requires SetConst");
+  if (!src || n < (size_t)s->T) return fail(FDTD_ERR_INVALID_ARG, "SourceIn needs T=%d values", s->T);
+  if (s->init_src) return FDTD_OK; /* reference: "Source is already initialized" */
+  s->h_src = (float *)malloc((size_t)s->T * sizeof(float));
+  if (!s->h_src) return fail(FDTD_ERR_OOM, "out of host memory");
+  memcpy(s->h_src, src, (size_t)s->T * sizeof(float));
+  int rc = dalloc(s, (void **)&s->d_src, (size_t)s->T * sizeof(float));
+  if (rc) return rc;
+  CU(cudaMemcpyAsync(s->d_src, s->h_src, (size_t)s->T * sizeof(float),
+                     cudaMemcpyHostToDevice, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  s->dev.src = s->d_src;
+  s->init_src = 1;
+  return FDTD_OK;
+}
+
+static int flush(sim *s);
+
+/* src/simulation.h:1084-1095 */
+int fdtd_update_source(fdtd_handle h, const float *src, size_t n) {
+  GET(h);
+  if (!s->init_src) return FDTD_OK; /* reference: "Source is not initialized" */
+  if (!src || n < (size_t)s->T) return fail(FDTD_ERR_INVALID_ARG, "SourceIn needs T=%d values", s->T);
+  int rc = flush(s);
+  if (rc) return rc;
+  memcpy(s->h_src, src, (size_t)s->T * sizeof(float));
+  CU(cudaMemcpyAsync(s->d_src, s->h_src, (size_t)s->T * sizeof(float),
+                     cudaMemcpyHostToDevice, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+/* src/simulation.h:288-328 */
+int fdtd_update_material(fdtd_handle h, int32_t flag, const float *values, size_t n) {
+  GET(h);
+  if (!s->init_const) return fail(FDTD_ERR_STATE, "UpdateMaterial requires SetConst");
+  if (flag < 1 || flag > 6) return FDTD_OK;
+  if (!values || n < (size_t)s->IJK)
+    return fail(FDTD_ERR_INVALID_ARG, "UpdateMaterial needs Imax*Jmax*Kmax=%lld values",
+                (long long)s->IJK);
+  memcpy(s->h_mat[flag - 1], values, (size_t)s->IJK * sizeof(float));
+  return FDTD_OK;
+}
+
+/* src/simulation.h:1047-1067 */
+int fdtd_set_antenna_locations(fdtd_handle h, const int32_t *loc, size_t n) {
+  GET(h);
+  if (!s->init_const) return fail(FDTD_ERR_STATE, "SetAntennaLocations requires SetConst");
+  if (s->init_ready)
+    return fail(FDTD_ERR_STATE, "SetAntennaLocations must precede ReadySimulation");
+  if (n < (size_t)s->num_ant * 3 || (!loc && s->num_ant))
+    return fail(FDTD_ERR_INVALID_ARG, "Locations needs numAnt x 3 = %d values", s->num_ant * 3);
+  free(s->h_probe_idx);
+  s->h_probe_idx = (int64_t *)calloc((size_t)(s->num_ant ? s->num_ant : 1), sizeof(int64_t));
+  for (int a = 0; a < s->num_ant; ++a) {
+    const int64_t x = (int64_t)s->p + loc[a + 0 * s->num_ant];
+    const int64_t y = (int64_t)s->p + loc[a + 1 * s->num_ant];
+    const int64_t z = (int64_t)s->p + loc[a + 2 * s->num_ant];
+    const int inside = x >= 0 && x < s->I && y >= 0 && y < s->J && z >= 0 && z < s->K;
+    s->h_probe_idx[a] = inside ? x + y * s->I + z * s->IJ : -1;
+  }
+  s->init_ant = 1;
+  return FDTD_OK;
+}
+
+/* CPML grading samples, src/simulation.h:730-767 */
+static void cpml_sample(const sim *s, double num_sig, double num_alpha, float *sig,
+                        float *alpha, float *kappa) {
+  const double pm1 = (double)s->p - 1.0;
+  *sig = (float)((double)s->sig_max * pow(num_sig / pm1, (double)s->poly_m));
+  *alpha = (float)((double)s->alpha_max * pow(num_alpha / pm1, (double)s->alpha_m));
+  *kappa = (float)(1.0 + ((double)s->kappa_max - 1.0) * pow(num_sig / pm1, (double)s->poly_m));
+}
+
+static float cpml_b(const sim *s, float sig, float alpha, float kappa) {
+  float t = sig / kappa;
+  t = t + alpha;
+  t = -t;
+  t = t * s->delT;
+  return (float)exp((double)t / K_EPS0);
+}
+
+static float cpml_c(float sig, float alpha, float kappa, float b) {
+  const float u1 = sig / kappa;
+  const float u2 = kappa * alpha;
+  const float u3 = sig + u2;
+  const float u4 = u1 / u3;
+  return (float)((double)u4 * ((double)b - 1.0));
+}
+
+static void build_tables(sim *s, float *kaE, float *kaH) {
+  const int p = s->p;
+  float sigE[FDTD_MAX_PML], alE[FDTD_MAX_PML], bE1[FDTD_MAX_PML], cE1[FDTD_MAX_PML];
+  float sigH[FDTD_MAX_PML], alH[FDTD_MAX_PML], bH1[FDTD_MAX_PML], cH1[FDTD_MAX_PML];
+  memset(s->bE, 0, sizeof(s->bE));
+  memset(s->cE, 0, sizeof(s->cE));
+  memset(s->bH, 0, sizeof(s->bH));
+  memset(s->cH, 0, sizeof(s->cH));
+  for (int i = 0; i < p; ++i) { /* :730-749 */
+    cpml_sample(s, (double)(p - i - 1), (double)(i + 1) - 1.0, &sigE[i], &alE[i], &kaE[i]);
+    bE1[i] = cpml_b(s, sigE[i], alE[i], kaE[i]);
+    if (sigE[i] == 0.0f && alE[i] == 0.0f && (i + 1) == (p - 1))
+      cE1[i] = 0.0f;
+    else
+      cE1[i] = cpml_c(sigE[i], alE[i], kaE[i], bE1[i]);
+  }
+  for (int i = 0; i + 1 < p; ++i) { /* :752-767 */
+    cpml_sample(s, (double)(p - i - 1) - 0.5, (double)(i + 1) - 0.5, &sigH[i], &alH[i], &kaH[i]);
+    bH1[i] = cpml_b(s, sigH[i], alH[i], kaH[i]);
+    cH1[i] = cpml_c(sigH[i], alH[i], kaH[i], bH1[i]);
+  }
+  for (int i = 0; i < p; ++i) { /* :772-822 */
+    s->bE[i] = bE1[i];
+    s->cE[i] = cE1[i];
+    s->bE[p + i] = bE1[p - 1 - i];
+    s->cE[p + i] = cE1[p - 1 - i];
+  }
+  for (int i = 0; i + 1 < p; ++i) {
+    s->bH[i] = bH1[i];
+    s->cH[i] = cH1[i];
+    s->bH[p + i] = bH1[p - 2 - i];
+    s->cH[p + i] = cH1[p - 2 - i];
+  }
+}
+
+static void fill_dev_struct(sim *s) {
+  fdtd_dev *d = &s->dev;
+  if (s->gexec) { /* a captured step graph holds the old descriptor */
+    cudaGraphExecDestroy(s->gexec);
+    s->gexec = NULL;
+  }
+  d->I = s->I;
+  d->J = s->J;
+  d->K = s->K;
+  d->p = s->p;
+  d->IJ = s->IJ;
+  d->IJK = s->IJK;
+  d->i0 = s->i0;
+  d->i1 = s->i1;
+  d->j0 = s->j0;
+  d->j1 = s->j1;
+  d->k0 = s->k0;
+  d->k1 = s->k1;
+  d->size1d = s->size1d;
+  d->T = s->T;
+  d->Chh = s->Chh;
+  d->Che = s->Che;
+  d->dx = s->delX;
+  memcpy(d->bE, s->bE, sizeof(d->bE));
+  memcpy(d->cE, s->cE, sizeof(d->cE));
+  memcpy(d->bH, s->bH, sizeof(d->bH));
+  memcpy(d->cH, s->cH, sizeof(d->cH));
+  for (int a = 0; a < 6; ++a) {
+    d->f[a] = s->d_f[a];
+    d->ce[a] = s->d_ce[a];
+  }
+  d->coef_mode = 0;
+  for (int a = 0; a < FDTD_NUM_PSI; ++a) d->psi[a] = s->d_psi[a];
+  for (int a = 0; a < 4; ++a) d->inc[a] = s->d_inc[a];
+  d->src = s->d_src;
+  d->step_base = s->d_ctr;
+  d->probe_row = s->d_ctr ? s->d_ctr + 1 : NULL;
+  d->probes = s->d_probes;
+  d->probe_idx = s->d_probe_idx;
+  d->num_ant = (s->init_ant && s->d_probes) ? s->num_ant : 0;
+}
+
+/* Uploads the six material arrays into the coefficient buffers and turns
+ * them into Cexe..Cezh in place (src/simulation.h:924-951 / :1099-1126). */
+static int upload_coefficients(sim *s) {
+  const size_t bytes = (size_t)s->IJK * sizeof(float);
+  /* sigma_x -> ce[0], sigma_y -> ce[1], sigma_z -> ce[2], eps -> ce[3..5]:
+   * the kernel reads both inputs of a component before writing its outputs */
+  for (int a = 0; a < 6; ++a)
+    CU(cudaMemcpyAsync(s->d_ce[a], s->h_mat[a], bytes, cudaMemcpyHostToDevice, s->stream));
+  float *ce[6];
+  const float *eps[3], *sig[3];
+  for (int a = 0; a < 6; ++a) ce[a] = s->d_ce[a];
+  for (int a = 0; a < 3; ++a) {
+    sig[a] = s->d_ce[a];
+    eps[a] = s->d_ce[3 + a];
+  }
+  KL(fdtdk_compute_ce(&s->dev, ce, eps, sig, s->d_den_ex, s->delT, s->stream));
+  return FDTD_OK;
+}
+
+static int zero_state(sim *s) {
+  const size_t bytes = (size_t)s->IJK * sizeof(float);
+  for (int a = 0; a < 6; ++a) CU(cudaMemsetAsync(s->d_f[a], 0, bytes, s->stream));
+  const size_t psi_total = (size_t)(4 * 2 * (s->size_x + s->size_y + s->size_z)) * sizeof(float);
+  CU(cudaMemsetAsync(s->d_psi_pool, 0, psi_total, s->stream));
+  CU(cudaMemsetAsync(s->d_ctr, 0, 2 * sizeof(int32_t), s->stream));
+  return FDTD_OK;
+}
+
+/* src/simulation.h:640-979 */
+int fdtd_ready_simulation(fdtd_handle h) {
+  GET(h);
+  if (!s->init_const) return fail(FDTD_ERR_STATE, "ReadySimulation requires SetConst");
+  if (s->init_ready) return fail(FDTD_ERR_STATE, "ReadySimulation already called");
+  float kaE[FDTD_MAX_PML], kaH[FDTD_MAX_PML];
+  build_tables(s, kaE, kaH);
+  const int p = s->p;
+  /* x-only stretch denominators, :861-912 (zero at i = Imax-1) */
+  s->h_den_ex = (float *)calloc((size_t)s->I, sizeof(float));
+  s->h_den_hx = (float *)calloc((size_t)s->I, sizeof(float));
+  if (!s->h_den_ex || !s->h_den_hx) return fail(FDTD_ERR_OOM, "out of host memory");
+  {
+    int ii = p - 2;
+    for (int i = 0; i + 1 < s->I; ++i) {
+      if (i < p - 1) {
+        s->h_den_hx[i] = (float)(1.0 / (double)(float)(s->delX * kaH[i]));
+      } else if (i >= s->I - p) {
+        s->h_den_hx[i] = (float)(1.0 / (double)(float)(s->delX * kaH[ii]));
+        ii = ii - 1;
+      } else {
+        s->h_den_hx[i] = (float)(1.0 / (double)s->delX);
+      }
+    }
+    ii = p - 1;
+    for (int i = 0; i + 1 < s->I; ++i) {
+      if (i < p) {
+        s->h_den_ex[i] = (float)(1.0 / (double)(float)(s->delX * kaE[i]));
+      } else if (i >= s->I - p) {
+        s->h_den_ex[i] = (float)(1.0 / (double)(float)(s->delX * kaE[ii]));
+        ii = ii - 1;
+      } else {
+        s->h_den_ex[i] = (float)(1.0 / (double)s->delX);
+      }
+    }
+  }
+  { /* :914-922, sigma_m = 0 */
+    const float sigma_m = 0.0f;
+    float t = sigma_m * s->delT;
+    t = t / 2;
+    const double q = (double)t / K_MU0;
+    s->Chh = (float)((1 - q) / (1 + q));
+    s->Che = (float)((double)s->delT / K_MU0 / (1 + q) / (double)s->delX);
+  }
+  const size_t bytes = (size_t)s->IJK * sizeof(float);
+  int rc;
+  for (int a = 0; a < 6; ++a) {
+    if ((rc = dalloc(s, (void **)&s->d_f[a], bytes))) return rc;
+    if ((rc = dalloc(s, (void **)&s->d_ce[a], bytes))) return rc;
+  }
+  const int64_t psi_n[FDTD_NUM_PSI] = {
+      [PSI_EXY] = 2 * s->size_y, [PSI_EZY] = 2 * s->size_y, [PSI_HXY] = 2 * s->size_y,
+      [PSI_HZY] = 2 * s->size_y, [PSI_EXZ] = 2 * s->size_z, [PSI_EYZ] = 2 * s->size_z,
+      [PSI_HXZ] = 2 * s->size_z, [PSI_HYZ] = 2 * s->size_z, [PSI_EYX] = 2 * s->size_x,
+      [PSI_EZX] = 2 * s->size_x, [PSI_HYX] = 2 * s->size_x, [PSI_HZX] = 2 * s->size_x};
+  int64_t psi_total = 0;
+  for (int a = 0; a < FDTD_NUM_PSI; ++a) psi_total += psi_n[a];
+  if ((rc = dalloc(s, (void **)&s->d_psi_pool, (size_t)psi_total * sizeof(float)))) return rc;
+  {
+    int64_t off = 0;
+    for (int a = 0; a < FDTD_NUM_PSI; ++a) {
+      s->d_psi[a] = s->d_psi_pool + off;
+      off += psi_n[a];
+    }
+  }
+  if ((rc = dalloc(s, (void **)&s->d_den_ex, (size_t)s->I * sizeof(float)))) return rc;
+  if ((rc = dalloc(s, (void **)&s->d_den_hx, (size_t)s->I * sizeof(float)))) return rc;
+  if ((rc = dalloc(s, (void **)&s->d_ctr, 2 * sizeof(int32_t)))) return rc;
+  CU(cudaMemcpyAsync(s->d_den_ex, s->h_den_ex, (size_t)s->I * sizeof(float),
+                     cudaMemcpyHostToDevice, s->stream));
+  CU(cudaMemcpyAsync(s->d_den_hx, s->h_den_hx, (size_t)s->I * sizeof(float),
+                     cudaMemcpyHostToDevice, s->stream));
+  if (s->init_ant && s->num_ant > 0) { /* :954-963 */
+    const size_t pb = (size_t)s->T * s->num_ant * 6 * sizeof(float);
+    if ((rc = dalloc(s, (void **)&s->d_probes, pb))) return rc;
+    if ((rc = dalloc(s, (void **)&s->d_probe_idx, (size_t)s->num_ant * sizeof(int64_t)))) return rc;
+    CU(cudaMemsetAsync(s->d_probes, 0, pb, s->stream));
+    CU(cudaMemcpyAsync(s->d_probe_idx, s->h_probe_idx, (size_t)s->num_ant * sizeof(int64_t),
+                       cudaMemcpyHostToDevice, s->stream));
+  }
+  fill_dev_struct(s);
+  if ((rc = upload_coefficients(s))) return rc;
+  if ((rc = zero_state(s))) return rc;
+  CU(cudaStreamSynchronize(s->stream));
+  s->init_ready = 1;
+  return FDTD_OK;
+}
+
+/* src/simulation.h:1097-1127 */
+int fdtd_update_cuda(fdtd_handle h) {
+  GET(h);
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "UpdateCuda requires ReadySimulation");
+  int rc = flush(s);
+  if (rc) return rc;
+  if ((rc = upload_coefficients(s))) return rc;
+  CU(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+/* src/simulation.h:1128-1151 */
+int fdtd_reset_field_all(fdtd_handle h) {
+  GET(h);
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "ResetFieldAll requires ReadySimulation");
+  int rc = flush(s);
+  if (rc) return rc;
+  return zero_state(s);
+}
+
+/* src/simulation.h:28-68.  The reference sets init_mu only when called
+ * before ReadySimulation (where it reads unset state); after it, the
+ * coefficients are computed and stored but the H update keeps the scalar
+ * coefficient.  That reachable behaviour is what is reproduced here. */
+int fdtd_create_mu(fdtd_handle h, const float *mu_x, const float *mu_y, const float *mu_z,
+                   size_t n) {
+  GET(h);
+  if (!s->init_ready)
+    return fail(FDTD_ERR_STATE, "CreateMu requires ReadySimulation (the reference reads "
+                                "unset coefficients before it)");
+  if (!mu_x || !mu_y || !mu_z || n < (size_t)s->IJK)
+    return fail(FDTD_ERR_INVALID_ARG, "mu_x, mu_y, mu_z need Imax*Jmax*Kmax values");
+  int rc = flush(s);
+  if (rc) return rc;
+  const float *mu[3] = {mu_x, mu_y, mu_z};
+  const size_t bytes = (size_t)s->IJK * sizeof(float);
+  float *tmp = NULL;
+  if ((rc = dalloc(s, (void **)&tmp, bytes))) return rc;
+  for (int a = 0; a < 3; ++a) {
+    if (!s->d_mu[a] && (rc = dalloc(s, (void **)&s->d_mu[a], bytes))) {
+      cudaFree(tmp);
+      return rc;
+    }
+    CU(cudaMemcpyAsync(tmp, mu[a], bytes, cudaMemcpyHostToDevice, s->stream));
+    KL(fdtdk_compute_mu(s->d_mu[a], tmp, s->d_den_hx, s->IJK, s->I, s->delT, 0.0f, s->stream));
+  }
+  CU(cudaStreamSynchronize(s->stream));
+  cudaFree(tmp);
+  s->device_bytes -= bytes;
+  return FDTD_OK;
+}
+
+/* src/simulation.h:134-254 */
+int fdtd_init_1d(fdtd_handle h, float rate, const float *pw_source, size_t n) {
+  GET(h);
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "Init1D requires ReadySimulation");
+  if (!pw_source || n < (size_t)s->T)
+    return fail(FDTD_ERR_INVALID_ARG, "PW_source needs T=%d values", s->T);
+  int rc = flush(s);
+  if (rc) return rc;
+  int32_t S = s->I;
+  if (s->J > S) S = s->J;
+  if (s->K > S) S = s->K;
+  if (S < 2 * s->p + 4)
+    return fail(FDTD_ERR_UNSUPPORTED, "1D line of %d cells too short", S);
+  s->size1d = S;
+  const size_t tab = (size_t)s->T * (size_t)S * sizeof(float);
+  for (int a = 0; a < 4; ++a) {
+    if (!s->d_inc[a] && (rc = dalloc(s, (void **)&s->d_inc[a], tab))) return rc;
+  }
+  float *pw = (float *)malloc((size_t)s->T * sizeof(float));
+  if (!pw) return fail(FDTD_ERR_OOM, "out of host memory");
+  for (int t = 0; t < s->T; ++t) pw[t] = pw_source[t] * rate; /* :194-197 */
+  float *d_pw = NULL, *scratch = NULL;
+  if ((rc = dalloc(s, (void **)&d_pw, (size_t)s->T * sizeof(float)))) {
+    free(pw);
+    return rc;
+  }
+  const size_t smem = 2 * (size_t)S * sizeof(float);
+  if (smem > fdtdk_init_1d_smem_limit()) {
+    if ((rc = dalloc(s, (void **)&scratch, 4 * (size_t)S * sizeof(float)))) {
+      cudaFree(d_pw);
+      free(pw);
+      return rc;
+    }
+  }
+  cudaMemcpyAsync(d_pw, pw, (size_t)s->T * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+  fill_dev_struct(s);
+  const float Ceh = (float)((double)s->delT / K_EPS0 / (double)s->delX); /* :144 */
+  int e = fdtdk_init_1d(&s->dev, s->d_inc, d_pw, Ceh, scratch, s->stream);
+  cudaError_t se = cudaStreamSynchronize(s->stream);
+  cudaFree(d_pw);
+  s->device_bytes -= (size_t)s->T * sizeof(float);
+  if (scratch) {
+    cudaFree(scratch);
+    s->device_bytes -= 4 * (size_t)S * sizeof(float);
+  }
+  free(pw);
+  if (e) return fail(FDTD_ERR_CUDA, "init_1d launch: %s", cudaGetErrorString((cudaError_t)e));
+  if (se != cudaSuccess) return fail(FDTD_ERR_CUDA, "init_1d: %s", cudaGetErrorString(se));
+  s->init_1d = 1;
+  return FDTD_OK;
+}
+
+/* ------------------------------------------------------------ step ops */
+
+static int issue(sim *s, int hfam, const fdtd_op *op) {
+  if (hfam) KL(fdtdk_half_h(&s->dev, op, s->stream));
+  else KL(fdtdk_half_e(&s->dev, op, s->stream));
+  return FDTD_OK;
+}
+
+static int flush(sim *s) {
+  if (!s->pend.active) return FDTD_OK;
+  s->pend.active = 0;
+  return issue(s, s->pend.h, &s->pend.op);
+}
+
+static int need_ready(sim *s) {
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "operation requires ReadySimulation");
+  return FDTD_OK;
+}
+
+static int tfsf_check(sim *s, int32_t step, int32_t mode) {
+  if (!s->init_1d) return fail(FDTD_ERR_STATE, "PlaneWave update requires Init1D");
+  if (step < 0 || step >= s->T)
+    return fail(FDTD_ERR_INVALID_ARG, "time step %d outside [0, %d)", step, s->T);
+  if (mode >= 1 && mode <= 4) {
+    if (s->i0 < 1 || s->j0 < 1 || s->k0 < 1 || s->i1 <= s->i0 || s->j1 <= s->j0 ||
+        s->k1 <= s->k0)
+      return fail(FDTD_ERR_UNSUPPORTED, "TF/SF box does not fit the grid");
+  }
+  return FDTD_OK;
+}
+
+/* Queue stage ranks: curl 1, tfsf 2, pml 3, current 4. */
+static int pend_rank(const fdtd_op *op) {
+  if (op->cur_mode) return 4;
+  if (op->pml) return 3;
+  if (op->tfsf_mode) return 2;
+  if (op->curl) return 1;
+  return 0;
+}
+
+/* Adds one stage to the pending half-step, flushing first when the stage
+ * would not follow the queued ones in the reference order. */
+static int enqueue(sim *s, int hfam, int rank, const fdtd_op *stage) {
+  /* stages that carry a step index (TF/SF, current) merge only with a
+   * queue that refers to the same step */
+  const int step_clash = (rank == 2 || rank == 4) && stage->step != s->pend.op.step &&
+                         (s->pend.op.tfsf_mode || s->pend.op.cur_mode);
+  if (s->pend.active &&
+      (s->pend.h != hfam || pend_rank(&s->pend.op) >= rank || step_clash)) {
+    int rc = flush(s);
+    if (rc) return rc;
+  }
+  if (!s->pend.active) {
+    memset(&s->pend, 0, sizeof(s->pend));
+    s->pend.active = 1;
+    s->pend.h = hfam;
+  }
+  fdtd_op *o = &s->pend.op;
+  if (rank == 1) o->curl = 1;
+  if (rank == 2) {
+    o->tfsf_mode = stage->tfsf_mode;
+    o->step = stage->step;
+  }
+  if (rank == 3) o->pml = 1;
+  if (rank == 4) {
+    o->cur_mode = stage->cur_mode;
+    memcpy(o->cur_box, stage->cur_box, sizeof(o->cur_box));
+    o->step = stage->step;
+  }
+  return FDTD_OK;
+}
+
+/* src/simulation.h:371-385; also records the probe row of this step */
+int fdtd_update_h_all(fdtd_handle h) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  if ((rc = flush(s))) return rc;
+  if (s->dev.num_ant > 0) KL(fdtdk_probe_gather(&s->dev, s->stream));
+  fdtd_op st;
+  memset(&st, 0, sizeof(st));
+  return enqueue(s, 1, 1, &st);
+}
+
+/* src/simulation.h:386-391 */
+int fdtd_update_e_all(fdtd_handle h) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  fdtd_op st;
+  memset(&st, 0, sizeof(st));
+  return enqueue(s, 0, 1, &st);
+}
+
+/* src/simulation.h:392-403 */
+int fdtd_update_h_pml(fdtd_handle h) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  fdtd_op st;
+  memset(&st, 0, sizeof(st));
+  return enqueue(s, 1, 3, &st);
+}
+
+/* src/simulation.h:404-418 */
+int fdtd_update_e_pml(fdtd_handle h) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  fdtd_op st;
+  memset(&st, 0, sizeof(st));
+  return enqueue(s, 0, 3, &st);
+}
+
+/* src/simulation.h:330-349 */
+int fdtd_update_h_planewave(fdtd_handle h, int32_t step, int32_t mode) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  if ((rc = tfsf_check(s, step, mode))) return rc;
+  if (mode < 1 || mode > 4) return FDTD_OK;
+  fdtd_op st;
+  memset(&st, 0, sizeof(st));
+  st.tfsf_mode = mode;
+  st.step = step;
+  return enqueue(s, 1, 2, &st);
+}
+
+/* src/simulation.h:350-369 */
+int fdtd_update_e_planewave(fdtd_handle h, int32_t step, int32_t mode) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  if ((rc = tfsf_check(s, step, mode))) return rc;
+  if (mode < 1 || mode > 4) return FDTD_OK;
+  fdtd_op st;
+  memset(&st, 0, sizeof(st));
+  st.tfsf_mode = mode;
+  st.step = step;
+  return enqueue(s, 0, 2, &st);
+}
+
+/* src/simulation.h:256-286 */
+int fdtd_add_currents(fdtd_handle h, int32_t step, int32_t mode, const int32_t box[6]) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  if (!box) return fail(FDTD_ERR_INVALID_ARG, "time and indices required.");
+  if (!s->init_src) return fail(FDTD_ERR_STATE, "AddCurrents requires SetSource");
+  if (step < 0 || step >= s->T)
+    return fail(FDTD_ERR_INVALID_ARG, "time step %d outside [0, %d)", step, s->T);
+  if (mode < 1 || mode > 3) return FDTD_OK;
+  for (int a = 0; a < 6; ++a)
+    if (box[a] < 0) return FDTD_OK; /* reference: no cell is touched */
+  if (box[1] < box[0] || box[3] < box[2] || box[5] < box[4]) return FDTD_OK;
+  fdtd_op st;
+  memset(&st, 0, sizeof(st));
+  st.cur_mode = mode;
+  memcpy(st.cur_box, box, sizeof(st.cur_box));
+  st.step = step;
+  return enqueue(s, 0, 4, &st);
+}
+
+/* ------------------------------------------------------------ fused loop */
+
+static int step_ops(sim *s, int32_t step, int from_dev, int32_t mode, const fdtd_current *cur) {
+  fdtd_op oh, oe;
+  memset(&oh, 0, sizeof(oh));
+  oh.curl = 1;
+  oh.pml = 1;
+  oh.tfsf_mode = mode;
+  oh.step = step;
+  oh.step_from_dev = from_dev;
+  oe = oh;
+  if (cur && cur->mode >= 1 && cur->mode <= 3) {
+    int ok = 1;
+    for (int a = 0; a < 6; ++a) ok &= cur->box[a] >= 0;
+    ok &= cur->box[1] >= cur->box[0] && cur->box[3] >= cur->box[2] && cur->box[5] >= cur->box[4];
+    if (ok) {
+      oe.cur_mode = cur->mode;
+      memcpy(oe.cur_box, cur->box, sizeof(oe.cur_box));
+    }
+  }
+  if (s->dev.num_ant > 0) KL(fdtdk_probe_gather(&s->dev, s->stream));
+  int rc = issue(s, 1, &oh);
+  if (rc) return rc;
+  return issue(s, 0, &oe);
+}
+
+int fdtd_step_n(fdtd_handle h, int32_t first, int32_t count, int32_t mode,
+                const fdtd_current *cur) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  if (count < 0 || first < 0) return fail(FDTD_ERR_INVALID_ARG, "negative step range");
+  if (count == 0) return FDTD_OK;
+  if (mode < 1 || mode > 4) mode = 0;
+  const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
+  if ((mode || use_cur) && (int64_t)first + count > s->T)
+    return fail(FDTD_ERR_INVALID_ARG, "steps [%d, %d) exceed T=%d", first, first + count, s->T);
+  if (mode && (rc = tfsf_check(s, first, mode))) return rc;
+  if (use_cur && !s->init_src) return fail(FDTD_ERR_STATE, "current source requires SetSource");
+  if ((rc = flush(s))) return rc;
+  const int probes = s->dev.num_ant > 0;
+  int32_t done = 0;
+  if (count >= GRAPH_CHUNK) {
+    const int cm = use_cur ? cur->mode : 0;
+    int same = s->gexec && s->g_mode == mode && s->g_cur_mode == cm && s->g_probes == probes;
+    if (same && cm) same = memcmp(s->g_cur_box, cur->box, sizeof(s->g_cur_box)) == 0;
+    if (!same) {
+      if (s->gexec) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = NULL;
+      }
+      cudaGraph_t g;
+      const unsigned long long before = fdtdk_launch_count();
+      CU(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+      int crc = FDTD_OK;
+      for (int c = 0; c < GRAPH_CHUNK && !crc; ++c) crc = step_ops(s, c, 1, mode, cur);
+      if (!crc) crc = fdtdk_add_i32(s->d_ctr, GRAPH_CHUNK, s->stream) ? FDTD_ERR_CUDA : FDTD_OK;
+      cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+      if (crc) return crc;
+      if (ce != cudaSuccess) return fail(FDTD_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&s->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) {
+        s->gexec = NULL;
+        return fail(FDTD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+      }
+      s->g_kernels = fdtdk_launch_count() - before;
+      g_captured_kernels += s->g_kernels;
+      s->g_mode = mode;
+      s->g_cur_mode = cm;
+      s->g_probes = probes;
+      if (cm) memcpy(s->g_cur_box, cur->box, sizeof(s->g_cur_box));
+    }
+    KL(fdtdk_set_i32(s->d_ctr, first, s->stream));
+    while (count - done >= GRAPH_CHUNK) {
+      CU(cudaGraphLaunch(s->gexec, s->stream));
+      g_graph_kernels += s->g_kernels;
+      done += GRAPH_CHUNK;
+    }
+  }
+  for (; done < count; ++done)
+    if ((rc = step_ops(s, first + done, 0, mode, cur))) return rc;
+  return FDTD_OK;
+}
+
+int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t mode,
+                       const fdtd_current *cur, float ms_out[3]) {
+  GET(h);
+  int rc = need_ready(s);
+  if (rc) return rc;
+  if (!ms_out || count < 0) return fail(FDTD_ERR_INVALID_ARG, "bad profile arguments");
+  if (mode < 1 || mode > 4) mode = 0;
+  const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
+  if ((mode || use_cur) && (int64_t)first + count > s->T)
+    return fail(FDTD_ERR_INVALID_ARG, "steps [%d, %d) exceed T=%d", first, first + count, s->T);
+  if ((rc = flush(s))) return rc;
+  cudaEvent_t *ev = s->ev;
+  for (int32_t c = 0; c < count; ++c) {
+    fdtd_op oh, oe;
+    memset(&oh, 0, sizeof(oh));
+    oh.curl = 1;
+    oh.pml = 1;
+    oh.tfsf_mode = mode;
+    oh.step = first + c;
+    oe = oh;
+    if (use_cur) {
+      oe.cur_mode = cur->mode;
+      memcpy(oe.cur_box, cur->box, sizeof(oe.cur_box));
+    }
+    CU(cudaEventRecord(ev[8], s->stream));
+    if (s->dev.num_ant > 0) KL(fdtdk_probe_gather(&s->dev, s->stream));
+    CU(cudaEventRecord(ev[9], s->stream));
+    if ((rc = issue(s, 1, &oh))) return rc;
+    CU(cudaEventRecord(ev[10], s->stream));
+    if ((rc = issue(s, 0, &oe))) return rc;
+    CU(cudaEventRecord(ev[11], s->stream));
+    CU(cudaEventSynchronize(ev[11]));
+    float a = 0, b = 0, d = 0;
+    CU(cudaEventElapsedTime(&d, ev[8], ev[9]));
+    CU(cudaEventElapsedTime(&a, ev[9], ev[10]));
+    CU(cudaEventElapsedTime(&b, ev[10], ev[11]));
+    ms_out[0] += a;
+    ms_out[1] += b;
+    ms_out[2] += d;
+  }
+  return FDTD_OK;
+}
+
+int fdtd_set_device(int32_t device) {
+  CU(cudaSetDevice(device));
+  return FDTD_OK;
+}
+
+/* ------------------------------------------------------------ outputs */
+
+int fdtd_synchronize(fdtd_handle h) {
+  GET(h);
+  int rc = flush(s);
+  if (rc) return rc;
+  CU(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+/* src/simulation.h:572-619 */
+int fdtd_output_vis(fdtd_handle h, float *out, size_t n, int32_t flag) {
+  GET(h);
+  if (!out && n) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  if (!s->init_const) return fail(FDTD_ERR_STATE, "OutputVis requires SetConst");
+  const size_t cnt = n < (size_t)s->IJK ? n : (size_t)s->IJK;
+  if (flag <= 0 && flag >= -5) {
+    const int idx = -flag; /* 0,-1,-2 sigma_x,y,z; -3,-4,-5 eps_x,y,z */
+    memcpy(out, s->h_mat[idx], cnt * sizeof(float));
+    return FDTD_OK;
+  }
+  if (flag >= 1 && flag <= 6) {
+    if (!s->init_ready) return fail(FDTD_ERR_STATE, "OutputVis of fields requires ReadySimulation");
+    int rc = flush(s);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(out, s->d_f[flag - 1], cnt * sizeof(float), cudaMemcpyDeviceToHost,
+                       s->stream));
+    CU(cudaStreamSynchronize(s->stream));
+  }
+  return FDTD_OK;
+}
+
+int fdtd_output_probes(fdtd_handle h, float *out, size_t n) {
+  GET(h);
+  if (!out && n) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  if (!s->d_probes) return fail(FDTD_ERR_STATE, "Antenna data is not initialized.");
+  int rc = flush(s);
+  if (rc) return rc;
+  const size_t total = (size_t)s->T * s->num_ant * 6;
+  CU(cudaMemcpyAsync(out, s->d_probes, (n < total ? n : total) * sizeof(float),
+                     cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+/* src/simulation.h:621-638 */
+int fdtd_output_ant(fdtd_handle h, float *out, size_t n) {
+  GET(h);
+  if (!out && n) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  if (!s->d_probes) return fail(FDTD_ERR_STATE, "Antenna data is not initialized.");
+  const size_t rows = (size_t)s->T * s->num_ant;
+  float *all = (float *)malloc(rows * 6 * sizeof(float));
+  if (!all) return fail(FDTD_ERR_OOM, "out of host memory");
+  int rc = fdtd_output_probes(h, all, rows * 6);
+  if (!rc) {
+    const size_t cnt = n < rows ? n : rows;
+    for (size_t r = 0; r < cnt; ++r) out[r] = all[r * 6 + 2];
+  }
+  free(all);
+  return rc;
+}
+
+int fdtd_get_info(fdtd_handle h, fdtd_info *o) {
+  GET(h);
+  if (!o) return fail(FDTD_ERR_INVALID_ARG, "null info");
+  memset(o, 0, sizeof(*o));
+  o->I = s->I;
+  o->J = s->J;
+  o->K = s->K;
+  o->T = s->T;
+  o->num_ant = s->num_ant;
+  o->pml = s->p;
+  o->size_1d = s->size1d;
+  o->i0 = s->i0;
+  o->i1 = s->i1;
+  o->j0 = s->j0;
+  o->j1 = s->j1;
+  o->k0 = s->k0;
+  o->k1 = s->k1;
+  o->coef_mode = s->dev.coef_mode;
+  o->num_materials = 0;
+  o->device_bytes = s->device_bytes;
+  o->Chh = s->Chh;
+  o->Che = s->Che;
+  return FDTD_OK;
+}
+
+int fdtd_get_table(fdtd_handle h, int32_t which, float *out, size_t n) {
+  GET(h);
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "tables exist after ReadySimulation");
+  const float *src = NULL;
+  size_t cnt = 0;
+  switch (which) {
+    case 0: src = s->bE; cnt = 2 * (size_t)s->p; break;
+    case 1: src = s->cE; cnt = 2 * (size_t)s->p; break;
+    case 2: src = s->bH; cnt = 2 * (size_t)s->p; break;
+    case 3: src = s->cH; cnt = 2 * (size_t)s->p; break;
+    case 4: src = s->h_den_ex; cnt = (size_t)s->I; break;
+    case 5: src = s->h_den_hx; cnt = (size_t)s->I; break;
+    default: return fail(FDTD_ERR_INVALID_ARG, "unknown table %d", which);
+  }
+  if (!out || n < cnt) return fail(FDTD_ERR_INVALID_ARG, "table needs %zu values", cnt);
+  memcpy(out, src, cnt * sizeof(float));
+  return FDTD_OK;
+}
+
+int fdtd_event_record(fdtd_handle h, int32_t slot) {
+  GET(h);
+  if (slot < 0 || slot >= MAX_EVENTS) return fail(FDTD_ERR_INVALID_ARG, "event slot");
+  int rc = flush(s);
+  if (rc) return rc;
+  CU(cudaEventRecord(s->ev[slot], s->stream));
+  return FDTD_OK;
+}
+
+int fdtd_event_elapsed_ms(fdtd_handle h, int32_t a, int32_t b, float *ms) {
+  GET(h);
+  if (a < 0 || a >= MAX_EVENTS || b < 0 || b >= MAX_EVENTS || !ms)
+    return fail(FDTD_ERR_INVALID_ARG, "event slot");
+  CU(cudaEventSynchronize(s->ev[b]));
+  CU(cudaEventElapsedTime(ms, s->ev[a], s->ev[b]));
+  return FDTD_OK;
+}
+
+/* src/cpucode/FunLib.cpp:26-44 */
+int fdtd_create_signal(double fctr, double delT, double percentage_bw, double num_side_lobes,
+                       size_t time_steps, double *out, double *fmaxx_out) {
+  if (!out && time_steps) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  const double fmaxx = fctr * percentage_bw / 2.0;
+  if (fmaxx_out) *fmaxx_out = fmaxx;
+  const double spread = 1.0 / (2.0 * delT * fmaxx);
+  const double tto = num_side_lobes * spread;
+  for (size_t n = 0; n < time_steps; ++n) {
+    const double nn = (double)n + 1.0;
+    double v = 0.0;
+    if (nn < 2.0 * tto) {
+      const double arg = 2.0 * K_PI * fmaxx * (nn - tto) * delT;
+      const double den = (fabs(arg) < 1e-14) ? 1e-14 : arg;
+      v = sin(arg) / den * sin(2.0 * K_PI * fctr * (nn - tto) * delT);
+    }
+    v *= cos(((nn - 1.0) / (double)time_steps) * (K_PI / 2.0));
+    out[n] = v;
+  }
+  return FDTD_OK;
+}

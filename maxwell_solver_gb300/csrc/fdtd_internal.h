@@ -1,0 +1,87 @@
+/*
+ * fdtd_internal.h -- the thin C ABI between the host solver (fdtd_host.c,
+ * plain C) and the sm_103a kernels (fdtd_kernels.cu).  Plain C structs
+ * passed by value to the kernels; no C++ or torch types.
+ */
+#ifndef FDTD_INTERNAL_H
+#define FDTD_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDTD_MAX_PML 32
+#define FDTD_NUM_PSI 12
+
+/* psi slots (one per field component x CPML axis) */
+enum {
+  PSI_EXY = 0, PSI_EXZ, PSI_EYX, PSI_EYZ, PSI_EZX, PSI_EZY,
+  PSI_HXY, PSI_HXZ, PSI_HYX, PSI_HYZ, PSI_HZX, PSI_HZY
+};
+
+/* Everything a kernel needs to know about one grid (by value). */
+typedef struct {
+  int32_t I, J, K, p;
+  int64_t IJ, IJK;
+  int32_t i0, i1, j0, j1, k0, k1;   /* TF/SF box */
+  int32_t size1d, T;
+  float Chh, Che, dx;
+  float bE[2 * FDTD_MAX_PML], cE[2 * FDTD_MAX_PML];
+  float bH[2 * FDTD_MAX_PML], cH[2 * FDTD_MAX_PML];
+  float *f[6];              /* Ex Ey Ez Hx Hy Hz, x-fastest IJK each */
+  const float *ce[6];       /* Cexe Ceye Ceze Cexh Ceyh Cezh (coef_mode 0) */
+  int32_t coef_mode;        /* 0: per-cell arrays; 1: material-indexed */
+  const uint16_t *mat;      /* coef_mode 1: material id per cell */
+  const float *mat_tab;     /* coef_mode 1: [n_mat][n_xclass][6] */
+  const uint8_t *xclass;    /* coef_mode 1: x-class of each i (Imax) */
+  int32_t n_xclass;
+  float *psi[FDTD_NUM_PSI];
+  const float *inc[4];      /* Ez_1D, Hy_1D, E_inv_1D, H_inv_1D: [T][size1d] */
+  const float *src;         /* current-source waveform [T] */
+  int32_t *step_base;       /* device step base for graph-replayed steps */
+  int32_t *probe_row;       /* device probe row counter */
+  float *probes;            /* [T][num_ant][6] */
+  const int64_t *probe_idx; /* [num_ant] cell index, -1 if outside */
+  int32_t num_ant;
+} fdtd_dev;
+
+/* One fused half-step: which parts run, for which step. */
+typedef struct {
+  int32_t curl;             /* Yee curl update */
+  int32_t pml;              /* CPML psi recurrences + corrections */
+  int32_t tfsf_mode;        /* 0 none, 1..4 reference plane-wave modes */
+  int32_t step;             /* step index (offset when step_from_dev) */
+  int32_t step_from_dev;    /* step = *step_base + step */
+  int32_t cur_mode;         /* 0 none, 1..3 Ex/Ey/Ez current source */
+  int32_t cur_box[6];
+} fdtd_op;
+
+/* Launchers (fdtd_kernels.cu).  Return cudaError_t as int. */
+int fdtdk_half_h(const fdtd_dev *d, const fdtd_op *op, cudaStream_t s);
+int fdtdk_half_e(const fdtd_dev *d, const fdtd_op *op, cudaStream_t s);
+int fdtdk_probe_gather(const fdtd_dev *d, cudaStream_t s);
+int fdtdk_set_i32(int32_t *dst, int32_t v, cudaStream_t s);
+int fdtdk_add_i32(int32_t *dst, int32_t v, cudaStream_t s);
+/* Per-cell E coefficients from device eps/sigma (src/simulation.h:924-938). */
+int fdtdk_compute_ce(const fdtd_dev *d, float *const ce[6],
+                     const float *const eps[3], const float *const sig[3],
+                     const float *den_ex, float delT, cudaStream_t s);
+/* Forward + inverse 1D incident runs (src/simulation.h:134-254). */
+int fdtdk_init_1d(const fdtd_dev *d, float *tab[4], const float *pw,
+                  float Ceh, float *scratch, cudaStream_t s);
+size_t fdtdk_init_1d_smem_limit(void);
+/* Per-cell mu coefficients (src/simulation.h:43-63). */
+int fdtdk_compute_mu(float *out, const float *mu, const float *den_hx,
+                     int64_t IJK, int32_t I, float delT, float sigma_m,
+                     cudaStream_t s);
+unsigned long long fdtdk_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

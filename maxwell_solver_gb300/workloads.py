@@ -1,0 +1,165 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+No public dataset is involved: every input (materials, sources, probe
+positions) is generated from a seed with the sizes and value distributions
+the configurations name.
+
+  c1  64^3, 10-cell CPML, vacuum, TF/SF, 500 steps, 8 probes
+  c2  256^3, 12-cell CPML, 40 dielectric/lossy spheres (radius U[4,20],
+      eps_r U[1.5,10], sigma log-U[1e-4,1] S/m), TF/SF, 2000 steps, 64 probes
+  c3  512x512x448, 16-cell CPML, 6-layer conductive half-space below air
+      (thickness U[10,80], sigma log-U[1e-4,1], eps_r U[5,30]), vertical
+      incidence, 4000 steps, 256-cell surface probe line
+
+Materials are returned as the six per-component arrays the reference's
+UpdateMaterial op takes (sigma_x,y,z, eps_x,y,z), flattened x-fastest.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+C0 = 299792458.0
+
+
+@dataclass(frozen=True)
+class Workload:
+    name: str
+    dims: tuple          # (I, J, K) including the CPML
+    steps: int
+    pml: int
+    mode: int            # TF/SF mode of the reference (1..4)
+    media: str           # vacuum | spheres | layers
+    n_probes: int
+    seed: int
+    delX: float = 1e-3
+    fctr: float = 30e9
+
+    @property
+    def delT(self) -> float:
+        return 0.99 * self.delX / (math.sqrt(3.0) * C0)
+
+    @property
+    def cells(self) -> int:
+        return int(np.prod(self.dims))
+
+
+WORKLOADS = {
+    "c1": Workload("c1", (64, 64, 64), 500, 10, 3, "vacuum", 8, 0),
+    "c2": Workload("c2", (256, 256, 256), 2000, 12, 3, "spheres", 64, 1),
+    "c3": Workload("c3", (512, 512, 448), 4000, 16, 1, "layers", 256, 2, delX=5e-3, fctr=1e9),
+}
+
+
+def rng(seed: int) -> np.random.Generator:
+    return np.random.default_rng(np.random.PCG64(seed))
+
+
+def materials(w: Workload):
+    """dict flag -> float32 array (F-order flattened), flags 1..6."""
+    I, J, K = w.dims
+    r = rng(w.seed)
+    if w.media == "vacuum":
+        eps = np.ones((I, J, K), dtype=np.float32, order="F")
+        sig = np.zeros((I, J, K), dtype=np.float32, order="F")
+    elif w.media == "spheres":
+        eps = np.ones((I, J, K), dtype=np.float32, order="F")
+        sig = np.zeros((I, J, K), dtype=np.float32, order="F")
+        lo = w.pml + 4
+        for _ in range(40):
+            rad = r.uniform(4, 20)
+            c = [r.uniform(lo + rad, n - lo - rad) for n in (I, J, K)]
+            e = np.float32(r.uniform(1.5, 10.0))
+            s = np.float32(10.0 ** r.uniform(-4, 0))
+            b0 = [max(0, int(math.floor(c[a] - rad))) for a in range(3)]
+            b1 = [min(n, int(math.ceil(c[a] + rad)) + 1) for a, n in enumerate((I, J, K))]
+            x = np.arange(b0[0], b1[0]) + 0.5 - c[0]
+            y = np.arange(b0[1], b1[1]) + 0.5 - c[1]
+            z = np.arange(b0[2], b1[2]) + 0.5 - c[2]
+            inside = (x[:, None, None] ** 2 + y[None, :, None] ** 2 + z[None, None, :] ** 2) <= rad * rad
+            sl = (slice(b0[0], b1[0]), slice(b0[1], b1[1]), slice(b0[2], b1[2]))
+            eps[sl][inside] = e
+            sig[sl][inside] = s
+    elif w.media == "layers":
+        eps_z = np.ones(K, dtype=np.float32)
+        sig_z = np.zeros(K, dtype=np.float32)
+        z = K - w.pml - 2 - int(0.45 * K)  # air above, earth below this plane
+        top = z
+        for _ in range(6):
+            t = int(r.integers(10, 81))
+            lo = max(0, top - t)
+            eps_z[lo:top] = np.float32(r.uniform(5, 30))
+            sig_z[lo:top] = np.float32(10.0 ** r.uniform(-4, 0))
+            top = lo
+            if top == 0:
+                break
+        if top > 0:
+            eps_z[:top] = eps_z[top]
+            sig_z[:top] = sig_z[top]
+        eps = np.broadcast_to(eps_z[None, None, :], (I, J, K))
+        sig = np.broadcast_to(sig_z[None, None, :], (I, J, K))
+    else:
+        raise ValueError(w.media)
+    e = np.asarray(eps, dtype=np.float32).ravel(order="F")
+    s = np.asarray(sig, dtype=np.float32).ravel(order="F")
+    return {1: s, 2: s, 3: s, 4: e, 5: e, 6: e}
+
+
+def sources(w: Workload, steps: int | None = None):
+    """(plane-wave waveform, current waveform) float32 of length T."""
+    T = w.steps if steps is None else steps
+    n = np.arange(T, dtype=np.float64)
+    dt = np.float32(w.delT)
+    if w.media == "layers":
+        # Gaussian-derivative pulse, >= 20 cells per shortest wavelength in air
+        fmax = C0 / (20 * w.delX)
+        tau = 1.0 / (math.pi * fmax)
+        t0 = 4 * tau
+        t = n * float(dt)
+        pw = -(t - t0) / tau * np.exp(-((t - t0) / tau) ** 2)
+    else:
+        # Gaussian-modulated sine, f0 = fctr, 10 ps spread
+        spread = 10e-12
+        t = n * float(dt)
+        t0 = 4 * spread
+        pw = np.sin(2 * math.pi * w.fctr * (t - t0)) * np.exp(-((t - t0) / spread) ** 2)
+    cur = np.exp(-((n - 0.3 * T) ** 2) / (2 * (0.08 * T) ** 2))
+    return pw.astype(np.float32), cur.astype(np.float32)
+
+
+def probe_locations(w: Workload) -> np.ndarray:
+    """numAnt x 3 int32 (x, y, z) offsets inside the CPML, as
+    SetAntennaLocations takes them."""
+    I, J, K = w.dims
+    p = w.pml
+    if w.media == "layers":
+        # surface probe line along x at the air/earth interface
+        z = K - w.pml - 2 - int(0.45 * K) - p
+        xs = np.linspace(2, I - 2 * p - 3, w.n_probes).astype(np.int32)
+        return np.stack([xs, np.full_like(xs, (J - 2 * p) // 2), np.full_like(xs, z)], axis=1)
+    r = rng(w.seed + 7)
+    lim = np.array([I, J, K]) - 2 * p - 2
+    return np.stack([r.integers(1, lim[a], w.n_probes) for a in range(3)], axis=1).astype(np.int32)
+
+
+def setup(api, w: Workload, steps: int | None = None, params=None):
+    """Creates and readies a simulation for the workload through a simFDTD
+    style callable (this package's simFDTD or a MEX driver); returns P."""
+    T = w.steps if steps is None else steps
+    I, J, K = w.dims
+    P = api("CreateSimulation")
+    # TF/SF box 5 cells inside the CPML (15 for the reference's 10 cells)
+    api("SetParams", P, np.float64(params if params is not None
+                                   else [w.pml, w.pml + 5, 3, 1, 0.08, 1, 0.8, 0]))
+    api("SetConst", P, np.float32([w.fctr, w.delX, w.delT]), np.int32([T, I, J, K, w.n_probes]))
+    pw, cur = sources(w, T)
+    api("SetSource", P, cur)
+    if w.n_probes:
+        api("SetAntennaLocations", P, np.asfortranarray(probe_locations(w)))
+    for flag, arr in materials(w).items():
+        api("UpdateMaterial", P, np.int32(flag), arr)
+    api("ReadySimulation", P)
+    api("Init1D", P, np.float32(1.0), pw)
+    return P

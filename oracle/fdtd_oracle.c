@@ -20,7 +20,7 @@
  *
  * Extensions over the reference (all default to the reference's constants):
  * runtime CPML thickness / grading, TF/SF inset, and a probe gather that
- * records (Ex,Ey,Ez,Hx,Hy,Hz) at each probe after the E-field CPML update.
+ * records (Ex,Ey,Ez,Hx,Hy,Hz) at each probe at the start of every step.
  */
 #define _GNU_SOURCE
 #include <math.h>
@@ -433,8 +433,10 @@ int OR(init_1d)(or_sim *s, float rate, const float *pw_source) {
   s->Hinv1d = (real *)xcalloc(s->T * S, sizeof(real));
   real *pw = (real *)xcalloc(s->T, sizeof(real));
   for (size_t n = 0; n < s->T; ++n) pw[n] = (real)((real)pw_source[n] * (real)rate);
-  run_1d(s, s->Ez1d, s->Hy1d, S - 13, pw);
-  run_1d(s, s->Einv1d, s->Hinv1d, 13, pw);
+  /* sources at S-13 / 13 for the reference's 10-cell CPML: 3 cells inside
+   * the 1D CPML, kept so for other thicknesses (extension) */
+  run_1d(s, s->Ez1d, s->Hy1d, S - (s->p + 3), pw);
+  run_1d(s, s->Einv1d, s->Hinv1d, s->p + 3, pw);
   free(pw);
   s->init_1d = 1;
   return 0;
@@ -760,8 +762,8 @@ int OR(add_currents)(or_sim *s, int n, int mode, const int32_t *ind) {
   return 0;
 }
 
-/* Extension: probe gather after the E-field update of step n; row n of the
- * [T][numAnt][6] record. */
+/* Extension: probe gather.  Row n of the [T][numAnt][6] record holds the six
+ * components at each probe at the start of step n (before its H update). */
 int OR(sample_probes)(or_sim *s, int n) {
   if (!s->probes || n < 0 || (size_t)n >= s->T) return -1;
   for (size_t a = 0; a < s->numAnt; ++a) {
@@ -773,15 +775,15 @@ int OR(sample_probes)(or_sim *s, int n) {
   return 0;
 }
 
-/* One full step in the order of highfrequency.m:85-91 (+ probe sample). */
+/* One full step in the order of highfrequency.m:85-91 (probe row first). */
 int OR(step)(or_sim *s, int n, int mode) {
+  if (s->probes) OR(sample_probes)(s, n);
   OR(update_h_all)(s);
   if (mode) OR(update_h_planewave)(s, n, mode);
   OR(update_h_pml)(s);
   OR(update_e_all)(s);
   if (mode) OR(update_e_planewave)(s, n, mode);
   OR(update_e_pml)(s);
-  if (s->probes) OR(sample_probes)(s, n);
   return 0;
 }
 

@@ -219,6 +219,8 @@ def run_oracle(sc: Scenario, precision="f32", inp=None, steps=None):
     o.update_cuda()
     o.reset_field_all()
     for n in range(sc.steps if steps is None else steps):
+        if inp["probes"] is not None and o.dim("numAnt"):
+            o.sample_probes(n)  # row n: state at the start of step n
         for op in sc.step_ops:
             if op == "H":
                 o.update_h_all()
@@ -234,6 +236,4 @@ def run_oracle(sc: Scenario, precision="f32", inp=None, steps=None):
                 o.update_e_pml()
             elif op == "CUR":
                 o.add_currents(n, sc.cur_mode, sc.cur_box)
-        if inp["probes"] is not None and o.dim("numAnt"):
-            o.sample_probes(n)
     return o

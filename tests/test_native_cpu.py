@@ -1,0 +1,114 @@
+"""CPU-side checks of the native library: it builds, loads, exports every
+entry point of include/fdtd_gb300.h, and its host-only paths (argument and
+handle validation, the source-waveform generator, the MEX dispatcher's
+error identifiers) behave as the reference's interface specifies.  No
+compute call is made (there is no GPU here)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from scenarios import create_signal as np_create_signal
+
+HEADER = os.path.join(ROOT, "include", "fdtd_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fdtd_[a-z0-9_]+)\s*\(", text)))
+
+
+def exported_symbols(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
+                         check=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if line.strip()}
+
+
+def test_header_entry_points_are_exported(native_lib):
+    from maxwell_solver_gb300.build import LIB
+
+    names = declared_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if n not in exported_symbols(LIB)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(native_lib):
+    from maxwell_solver_gb300._native import SIGNATURES
+
+    assert set(declared_functions()) == set(SIGNATURES)
+
+
+def test_create_signal_matches_funlib_formula(native_lib):
+    from maxwell_solver_gb300 import create_signal
+
+    for args in ((5.5e9, 1.9e-13, 8e9 / 5.5e9, 2, 400), (30e9, 1.9e-12, 0.5, 1, 120)):
+        fmaxx, got = create_signal(*args)
+        want = np_create_signal(*args)
+        assert fmaxx == args[0] * args[2] / 2.0
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
+
+
+def test_invalid_handle_is_rejected(native_lib):
+    for fn in ("fdtd_update_h_all", "fdtd_update_e_all", "fdtd_ready_simulation",
+               "fdtd_destroy", "fdtd_synchronize"):
+        assert getattr(native_lib, fn)(0xDEADBEEF00000001) == 1
+    assert native_lib.fdtd_update_h_planewave(0, 0, 3) == 1
+    assert b"invalid simulation handle" in native_lib.fdtd_last_error()
+
+
+def test_default_params_are_reference_constants(native_lib):
+    p = native_lib.fdtd_default_params()
+    assert (p.pml, p.tfsf_width) == (10, 15)
+    assert (p.poly_m, p.alpha_m, p.alpha_max, p.kappa_max, p.sig_factor, p.r0) == \
+        (3.0, 1.0, 0.08, 1.0, 0.8, 0.0)
+
+
+def test_python_dispatcher_errors(native_lib):
+    from maxwell_solver_gb300 import SimFDTDError, simFDTD
+
+    bogus = np.array([0xDEADBEEF00000001], dtype=np.uint64)
+    with pytest.raises(SimFDTDError) as e:
+        simFDTD("NoSuchOp", bogus)
+    assert e.value.identifier == "simFDTD:UnknownOperation"
+    with pytest.raises(SimFDTDError) as e:
+        simFDTD("UpdateH_All")
+    assert e.value.identifier == "simFDTD:InvalidInput"
+    with pytest.raises(SimFDTDError) as e:
+        simFDTD("SetConst", bogus)
+    assert e.value.identifier == "simFDTD:InvalidInput"
+    with pytest.raises(SimFDTDError) as e:
+        simFDTD("updateh_all", bogus)  # op strings are case-insensitive
+    assert e.value.identifier == "simFDTD:InvalidHandle"
+
+
+def test_mex_dispatcher_errors(mex):
+    from mexstub.mexdrv import MexError
+
+    bogus = np.array([0xDEADBEEF00000001], dtype=np.uint64)
+    with pytest.raises(MexError) as e:
+        mex("NoSuchOp", bogus)
+    assert e.value.identifier == "simFDTD:UnknownOperation"
+    assert "nosuchop" in e.value.message
+    with pytest.raises(MexError) as e:
+        mex(nlhs=1)
+    assert e.value.identifier == "simFDTD:InvalidInput"
+    with pytest.raises(MexError) as e:
+        mex("UpdateE_All")
+    assert e.value.identifier == "simFDTD:InvalidInput"
+    for op, args in (("AddCurrents", (np.int32([0, 1]),)), ("UpdateH_PlaneWave", ()),
+                     ("SetConst", (np.float32([1, 2, 3]),)), ("Init1D", (np.float32([1]),)),
+                     ("OutputVis", (np.uint32(8),)), ("CreateMu", ()),
+                     ("UpdateMaterial", (np.int32(1),)), ("SetSource", ()),
+                     ("SetAntennaLocations", ()), ("OutputAnt", ())):
+        with pytest.raises(MexError) as e:
+            mex(op, bogus, *args)
+        assert e.value.identifier == "simFDTD:InvalidInput", op
+    with pytest.raises(MexError) as e:
+        mex("UpdateH_All", bogus)
+    assert e.value.identifier == "simFDTD:InvalidHandle"
