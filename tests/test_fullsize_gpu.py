@@ -1,0 +1,113 @@
+"""Parity and size-independent properties at the benchmark configurations'
+full sizes (c2: 256^3 with a 12-cell CPML and 40 spheres; c3: 512x512x448
+with a 16-cell CPML and a 6-layer earth).
+
+- a few steps against the FP32 oracle, bit for bit (the oracle finishes
+  these in seconds on the host cores);
+- exact linearity: doubling the plane-wave amplitude (Init1D rate 2) doubles
+  every field bit for bit, over hundreds of steps;
+- TF/SF leakage: in vacuum the scattered-field region stays at the rounding
+  floor (the reference algorithm leaks ~7e-6 of the total-field RMS).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+
+
+def oracle_for(w, T):
+    import oracle
+    from maxwell_solver_gb300.workloads import materials, probe_locations, sources
+
+    o = oracle.OracleSim("f32")
+    o.set_params(pml=w.pml, tfsf_width=w.pml + 5)
+    I, J, K = w.dims
+    o.set_const(np.float32([w.fctr, w.delX, w.delT]), np.int32([T, I, J, K, w.n_probes]))
+    pw, cur = sources(w, T)
+    o.set_source(cur)
+    if w.n_probes:
+        o.set_antenna_locations(np.asfortranarray(probe_locations(w)))
+    for flag, arr in materials(w).items():
+        o.update_material(flag, arr)
+    o.ready_simulation()
+    o.init_1d(1.0, pw)
+    return o
+
+
+@pytest.mark.parametrize("name,steps", [("c2", 6), ("c3", 3)])
+def test_full_size_steps_match_oracle(name, steps):
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.workloads import WORKLOADS, setup
+
+    w = WORKLOADS[name]
+    T = 40
+    P = setup(simFDTD, w, steps=T)
+    # advance into the run so that the incident wave is inside the grid
+    # (the oracle replays the same steps)
+    simFDTD("StepN", P, np.int32([0, steps, w.mode]))
+    o = oracle_for(w, T)
+    for n in range(steps):
+        o.step(n, w.mode)
+    ijk = w.cells
+    for f, n in zip(range(1, 7), FIELDS):
+        got = simFDTD("OutputVis", P, np.uint32(ijk), np.int32(f))
+        np.testing.assert_array_equal(got, o.field(n), err_msg=n)
+    rec = simFDTD("OutputProbes", P, np.uint32(T * w.n_probes * 6))
+    np.testing.assert_array_equal(rec, o.array("probes"))
+    simFDTD("DeleteSimulation", P)
+    o.close()
+
+
+def test_c2_exact_linearity():
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.workloads import WORKLOADS, materials, probe_locations, sources
+
+    w = WORKLOADS["c2"]
+    T = 300
+    out = []
+    for rate in (1.0, 2.0):
+        I, J, K = w.dims
+        P = simFDTD("CreateSimulation")
+        simFDTD("SetParams", P, np.float64([w.pml, w.pml + 5]))
+        simFDTD("SetConst", P, np.float32([w.fctr, w.delX, w.delT]), np.int32([T, I, J, K, 0]))
+        pw, cur = sources(w, T)
+        simFDTD("SetSource", P, cur)
+        for flag, arr in materials(w).items():
+            simFDTD("UpdateMaterial", P, np.int32(flag), arr)
+        simFDTD("ReadySimulation", P)
+        simFDTD("Init1D", P, np.float32(rate), pw)
+        simFDTD("StepN", P, np.int32([0, T, w.mode]))
+        out.append([simFDTD("OutputVis", P, np.uint32(w.cells), np.int32(f)) for f in range(1, 7)])
+        simFDTD("DeleteSimulation", P)
+    for a, b, n in zip(out[0], out[1], FIELDS):
+        assert np.abs(a).max() > 0, n if n in ("Ez", "Hy") else None
+        np.testing.assert_array_equal(2 * a, b, err_msg=n)
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3, 4])
+def test_tfsf_leakage_vacuum(mode):
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.workloads import WORKLOADS, sources
+
+    w = WORKLOADS["c1"]
+    T = 300
+    I, J, K = w.dims
+    P = simFDTD("CreateSimulation")
+    simFDTD("SetConst", P, np.float32([w.fctr, w.delX, w.delT]), np.int32([T, I, J, K, 0]))
+    pw, cur = sources(w, T)
+    simFDTD("SetSource", P, cur)
+    simFDTD("ReadySimulation", P)
+    simFDTD("Init1D", P, np.float32(1), pw)
+    simFDTD("StepN", P, np.int32([0, T, mode]))
+    e2 = sum(simFDTD("OutputVis", P, np.uint32(w.cells), np.int32(f)).astype(np.float64) ** 2
+             for f in (1, 2, 3)).reshape((I, J, K), order="F")
+    simFDTD("DeleteSimulation", P)
+    inside = e2[16:48, 16:48, 16:48]
+    shell = np.zeros_like(e2, dtype=bool)
+    shell[11:53, 11:53, 11:53] = True
+    shell[14:50, 14:50, 14:50] = False
+    ratio = np.sqrt(e2[shell].mean() / inside.mean())
+    assert inside.mean() > 0
+    assert ratio < 1e-4, ratio
