@@ -1,0 +1,334 @@
+/*
+ * fdtd_device.cuh -- per-cell update functions shared by the direct
+ * kernels (fdtd_kernels.cu) and the TMA-pipelined kernels (fdtd_tma.cu).
+ *
+ * Each function applies, to one cell, the reference's operations in the
+ * reference's order (enricoballini/maxwell_solver src/gpu.h): the Yee curl,
+ * then the TF/SF face correction, then the CPML axes in the order the
+ * reference launches them, then (E only) the current source.  Every
+ * operation is rounded separately (the library is built with --fmad=false),
+ * so any kernel built from these functions reproduces the reference bit
+ * for bit, however it stages its loads.
+ */
+#pragma once
+#include <stdint.h>
+
+#include "fdtd_internal.h"
+
+namespace fdtd {
+
+__device__ __forceinline__ bool in_range(int v, int lo, int hi) { return v >= lo && v <= hi; }
+
+// Slab position of index v in a CPML of thickness p on an axis of length n.
+// H cells: low side [0,p) -> v, high side [n-p, n-2] -> v-n+2p
+// (src/gpu.h:615-617, :654-656, :698-700).
+__device__ __forceinline__ int slab_h(int v, int n, int p) {
+  if (v < p) return v;
+  if (v >= n - p && v <= n - 2) return v - n + 2 * p;
+  return -1;
+}
+// E cells: low side [1,p) -> v, high side [n-p, n-1] -> v-n+2p
+// (src/gpu.h:776-778, :800-802, :839-841).
+__device__ __forceinline__ int slab_e(int v, int n, int p) {
+  if (v >= 1 && v < p) return v;
+  if (v >= n - p && v <= n - 1) return v - n + 2 * p;
+  return -1;
+}
+
+__device__ __forceinline__ int op_step(const fdtd_dev &d, const fdtd_op &op) {
+  return op.step_from_dev ? (*d.step_base + op.step) : op.step;
+}
+
+// Incident-table row used by the H side at step n (src/simulation.h:330-349).
+__device__ __forceinline__ const float *inc_h_row(const fdtd_dev &d, int mode, int n) {
+  const int64_t S = d.size1d;
+  switch (mode) {
+    case 1:
+    case 2: return d.inc[0] + (int64_t)n * S + S - d.K;
+    case 3: return d.inc[0] + (int64_t)n * S + S - d.I;
+    case 4: return d.inc[2] + (int64_t)n * S + S - d.I;
+  }
+  return nullptr;
+}
+// ... and by the E side (src/simulation.h:350-369).
+__device__ __forceinline__ const float *inc_e_row(const fdtd_dev &d, int mode, int n) {
+  const int64_t S = d.size1d;
+  switch (mode) {
+    case 1:
+    case 2: return d.inc[1] + (int64_t)n * S + S - d.K;
+    case 3: return d.inc[1] + (int64_t)n * S + S - d.I;
+    case 4: return d.inc[3] + (int64_t)n * S + S - d.I;
+  }
+  return nullptr;
+}
+
+// H-side TF/SF corrections of one cell (all launchers pass c = +1):
+// mode 3 gpu.h:152-182, mode 4 :217-247, mode 1 :424-477, mode 2 :512-541.
+__device__ __forceinline__ void tfsf_h(const fdtd_dev &d, int mode, const float *inc, int i,
+                                       int j, int k, float &hx, float &hy, float &hz) {
+  const float Ch = d.Che;
+  const int i0 = d.i0, i1 = d.i1, j0 = d.j0, j1 = d.j1, k0 = d.k0, k1 = d.k1;
+  if (mode == 3) {
+    if (in_range(i, i0, i1) && in_range(k, k0, k1 - 1)) {
+      if (j == j0 - 1) hx = hx + Ch * inc[i];
+      if (j == j1) hx = hx - Ch * inc[i];
+    }
+    if (in_range(j, j0, j1) && in_range(k, k0, k1 - 1)) {
+      if (i == i0 - 1) hy = hy - Ch * inc[i0];
+      if (i == i1) hy = hy + Ch * inc[i1];
+    }
+  } else if (mode == 4) {
+    if (in_range(i, i0, i1) && in_range(j, j0, j1 - 1)) {
+      if (k == k0 - 1) hx = hx - Ch * inc[i];
+      if (k == k1) hx = hx + Ch * inc[i];
+    }
+    if (in_range(j, j0, j1 - 1) && in_range(k, k0, k1)) {
+      if (i == i0 - 1) hz = hz + Ch * inc[i0];
+      if (i == i1) hz = hz - Ch * inc[i1];
+    }
+  } else if (mode == 1) {
+    if (in_range(i, i0, i1) && in_range(j, j0, j1 - 1)) {
+      if (k == k0 - 1) hx = hx - Ch * inc[k0];
+      if (k == k1) hx = hx + Ch * inc[k1];
+    }
+    if (in_range(j, j0, j1 - 1) && in_range(k, k0, k1)) {
+      if (i == i0 - 1) hz = hz + Ch * inc[k];
+      if (i == i1) hz = hz - Ch * inc[k];
+    }
+  } else if (mode == 2) {
+    if (in_range(i, i0, i1 - 1) && in_range(j, j0, j1)) {
+      if (k == k0 - 1) hy = hy + Ch * inc[k0];
+      if (k == k1) hy = hy - Ch * inc[k1];
+    }
+    if (in_range(i, i0, i1 - 1) && in_range(k, k0, k1)) {
+      if (j == j0 - 1) hz = hz - Ch * inc[k];
+      if (j == j1) hz = hz + Ch * inc[k];
+    }
+  }
+}
+
+// E-side TF/SF corrections of one cell.  Modes 1 and 3 are launched with
+// c = +1, modes 2 and 4 with c = -1 (src/simulation.h:493-570); x - (a*-1)
+// is computed as x + a, which IEEE arithmetic makes identical.
+// mode 3 gpu.h:184-214, mode 4 :249-291, mode 1 :479-509, mode 2 :543-573.
+__device__ __forceinline__ void tfsf_e(const fdtd_dev &d, int mode, const float *inc, int i,
+                                       int j, int k, float cxh, float cyh, float czh,
+                                       float &ex, float &ey, float &ez) {
+  const int i0 = d.i0, i1 = d.i1, j0 = d.j0, j1 = d.j1, k0 = d.k0, k1 = d.k1;
+  if (mode == 3) {
+    if (in_range(i, i0, i1 - 1) && in_range(j, j0, j1)) {
+      if (k == k0) ex = ex + cxh * inc[i];
+      if (k == k1) ex = ex - cxh * inc[i];
+    }
+    if (in_range(j, j0, j1) && in_range(k, k0, k1 - 1)) {
+      if (i == i0) ez = ez - czh * inc[i0 - 1];
+      if (i == i1) ez = ez + czh * inc[i1];
+    }
+  } else if (mode == 4) {
+    if (in_range(i, i0, i1 - 1) && in_range(k, k0, k1)) {
+      if (j == j0) ex = ex + cxh * inc[i];
+      if (j == j1) ex = ex - cxh * inc[i];
+    }
+    if (in_range(j, j0, j1 - 1) && in_range(k, k0, k1)) {
+      if (i == i0) ey = ey - cyh * inc[i0 - 1];
+      if (i == i1) ey = ey + cyh * inc[i1];
+    }
+  } else if (mode == 1) {
+    if (in_range(i, i0, i1) && in_range(j, j0, j1 - 1)) {
+      if (k == k0) ey = ey - cyh * inc[k0 - 1];
+      if (k == k1) ey = ey + cyh * inc[k1];
+    }
+    if (in_range(i, i0, i1) && in_range(k, k0, k1 - 1)) {
+      if (j == j0) ez = ez + czh * inc[k];
+      if (j == j1) ez = ez - czh * inc[k];
+    }
+  } else if (mode == 2) {
+    if (in_range(i, i0, i1 - 1) && in_range(j, j0, j1)) {
+      if (k == k0) ex = ex - cxh * inc[k0 - 1];
+      if (k == k1) ex = ex + cxh * inc[k1];
+    }
+    if (in_range(j, j0, j1) && in_range(k, k0, k1 - 1)) {
+      if (i == i0) ez = ez + czh * inc[k];
+      if (i == i1) ez = ez - czh * inc[k];
+    }
+  }
+}
+
+// Does the TF/SF of `mode` touch cell (i,j,k)?  (Used by the variants that
+// skip the curl and visit only the cells other stages touch.)
+__device__ __forceinline__ bool tfsf_h_touches(const fdtd_dev &d, int mode, int i, int j, int k) {
+  if (!mode) return false;
+  return i == d.i0 - 1 || i == d.i1 || j == d.j0 - 1 || j == d.j1 || k == d.k0 - 1 ||
+         k == d.k1;
+}
+__device__ __forceinline__ bool tfsf_e_touches(const fdtd_dev &d, int mode, int i, int j, int k) {
+  if (!mode) return false;
+  return i == d.i0 || i == d.i1 || j == d.j0 || j == d.j1 || k == d.k0 || k == d.k1;
+}
+
+struct Coef6 {
+  float exe, eye, eze, exh, eyh, ezh;
+};
+
+__device__ __forceinline__ Coef6 coef_from_table(const fdtd_dev &d, int m) {
+  const float *t = d.mat_tab + (int64_t)m * 6;
+  Coef6 c;
+  c.exe = __ldg(t + 0);
+  c.eye = __ldg(t + 1);
+  c.eze = __ldg(t + 2);
+  c.exh = __ldg(t + 3);
+  c.eyh = __ldg(t + 4);
+  c.ezh = __ldg(t + 5);
+  return c;
+}
+
+__device__ __forceinline__ Coef6 coef_from_arrays(const fdtd_dev &d, int64_t n) {
+  Coef6 c;
+  c.exe = __ldg(d.ce[0] + n);
+  c.eye = __ldg(d.ce[1] + n);
+  c.eze = __ldg(d.ce[2] + n);
+  c.exh = __ldg(d.ce[3] + n);
+  c.eyh = __ldg(d.ce[4] + n);
+  c.ezh = __ldg(d.ce[5] + n);
+  return c;
+}
+
+__device__ __forceinline__ Coef6 load_coef(const fdtd_dev &d, int64_t n) {
+  return d.coef_mode == 0 ? coef_from_arrays(d, n) : coef_from_table(d, __ldg(d.mat + n));
+}
+
+// New H of one cell from its old H and the six forward E differences:
+// curl (gpu.h:575-602), TF/SF, CPML Y (gpu.h:644-685), X (:604-642),
+// Z (:687-725).  px/py/pz: H-slab positions (-1 outside).
+template <bool CURL, bool PML>
+__device__ __forceinline__ void update_h_cell(const fdtd_dev &d, int mode, const float *inc,
+                                              int i, int j, int k, int px, int py, int pz,
+                                              float &hx, float &hy, float &hz, float dEz_y,
+                                              float dEx_y, float dEz_x, float dEy_x,
+                                              float dEy_z, float dEx_z) {
+  const float Che = d.Che, dx = d.dx;
+  if (CURL) {
+    const float Chh = d.Chh;
+    hx = Chh * hx + Che * (-dEz_y + dEy_z);
+    hy = Chh * hy + Che * (-dEx_z + dEz_x);
+    hz = Chh * hz + Che * (-dEy_x + dEx_y);
+  }
+  if (mode) tfsf_h(d, mode, inc, i, j, k, hx, hy, hz);
+  if (PML) {
+    const int64_t I = d.I, J = d.J, pj = 2 * (int64_t)d.p;
+    if (py >= 0) {
+      const int64_t t = i + py * I + k * pj * I;
+      const float b = d.bH[py], c = d.cH[py];
+      float *ps = d.psi[PSI_HXY] + t;
+      float v = b * *ps + c * dEz_y / dx;
+      *ps = v;
+      hx = hx - Che * v * dx;
+      ps = d.psi[PSI_HZY] + t;
+      v = b * *ps + c * dEx_y / dx;
+      *ps = v;
+      hz = hz + Che * v * dx;
+    }
+    if (px >= 0) {
+      const int64_t t = px + j * pj + k * pj * J;
+      const float b = d.bH[px], c = d.cH[px];
+      float *ps = d.psi[PSI_HYX] + t;
+      float v = b * *ps + c * dEz_x / dx;
+      *ps = v;
+      hy = hy + Che * v * dx;
+      ps = d.psi[PSI_HZX] + t;
+      v = b * *ps + c * dEy_x / dx;
+      *ps = v;
+      hz = hz - Che * v * dx;
+    }
+    if (pz >= 0) {
+      const int64_t t = i + j * I + pz * d.IJ;
+      const float b = d.bH[pz], c = d.cH[pz];
+      float *ps = d.psi[PSI_HXZ] + t;
+      float v = b * *ps + c * dEy_z / dx;
+      *ps = v;
+      hx = hx + Che * v * dx;
+      ps = d.psi[PSI_HYZ] + t;
+      v = b * *ps + c * dEx_z / dx;
+      *ps = v;
+      hy = hy - Che * v * dx;
+    }
+  }
+}
+
+// E-slab positions of cell (i,j,k) with the reference's exclusions of the
+// first and last planes of the other two axes (gpu.h:776-777, :800-801,
+// :839-840).
+__device__ __forceinline__ void e_slabs(const fdtd_dev &d, int i, int j, int k, int &px,
+                                        int &py, int &pz) {
+  const bool i_in = i >= 1 && i <= d.I - 2, j_in = j >= 1 && j <= d.J - 2,
+             k_in = k >= 1 && k <= d.K - 2;
+  px = (j_in && k_in) ? slab_e(i, d.I, d.p) : -1;
+  py = (i_in && k_in) ? slab_e(j, d.J, d.p) : -1;
+  pz = (i_in && j_in) ? slab_e(k, d.K, d.p) : -1;
+}
+
+// New E of one cell: curl with the reference's guards (gpu.h:727-763),
+// TF/SF, CPML Y (gpu.h:790-827), Z (:829-868), X (:765-788), then the
+// current source (gpu.h:55-82) when `cur` is set.
+template <bool CURL, bool PML>
+__device__ __forceinline__ void update_e_cell(const fdtd_dev &d, int mode, const float *inc,
+                                              int cur_mode, float cur_src, bool cur, int i,
+                                              int j, int k, int px, int py, int pz,
+                                              const Coef6 &C, float &ex, float &ey, float &ez,
+                                              float hx, float hy, float hz, float hz_jm,
+                                              float hx_jm, float hz_im, float hy_im,
+                                              float hx_km, float hy_km) {
+  const float dx = d.dx;
+  if (CURL) {
+    if (j != 0 && k != 0) ex = C.exe * ex + C.exh * (+(hz - hz_jm) - (hy - hy_km));
+    if (i != 0 && k != 0) ey = C.eye * ey + C.eyh * (+(hx - hx_km) - (hz - hz_im));
+    if (i != 0 && j != 0) ez = C.eze * ez + C.ezh * (+(hy - hy_im) - (hx - hx_jm));
+  }
+  if (mode) tfsf_e(d, mode, inc, i, j, k, C.exh, C.eyh, C.ezh, ex, ey, ez);
+  if (PML) {
+    const int64_t I = d.I, J = d.J, pj = 2 * (int64_t)d.p;
+    if (py >= 0) {
+      const int64_t t = i + py * I + k * pj * I;
+      const float b = d.bE[py], c = d.cE[py];
+      float *ps = d.psi[PSI_EXY] + t;
+      float v = b * *ps + c * (hz - hz_jm) / dx;
+      *ps = v;
+      ex = ex + C.exh * v * dx;
+      ps = d.psi[PSI_EZY] + t;
+      v = b * *ps + c * (hx - hx_jm) / dx;
+      *ps = v;
+      ez = ez - C.ezh * v * dx;
+    }
+    if (pz >= 0) {
+      const int64_t t = i + j * I + pz * d.IJ;
+      const float b = d.bE[pz], c = d.cE[pz];
+      float *ps = d.psi[PSI_EXZ] + t;
+      float v = b * *ps + c * (hy - hy_km) / dx;
+      *ps = v;
+      ex = ex - C.exh * v * dx;
+      ps = d.psi[PSI_EYZ] + t;
+      v = b * *ps + c * (hx - hx_km) / dx;
+      *ps = v;
+      ey = ey + C.eyh * v * dx;
+    }
+    if (px >= 0) {
+      const int64_t t = px + j * pj + k * pj * J;
+      const float b = d.bE[px], c = d.cE[px];
+      float *ps = d.psi[PSI_EYX] + t;
+      float v = b * *ps + c * (hz - hz_im) / dx;
+      *ps = v;
+      ey = ey - C.eyh * v * dx;
+      ps = d.psi[PSI_EZX] + t;
+      v = b * *ps + c * (hy - hy_im) / dx;
+      *ps = v;
+      ez = ez + C.ezh * v * dx;
+    }
+  }
+  if (cur) {  // E -= Ce?h * source * dx / dx / dx
+    if (cur_mode == 1) ex = ex - C.exh * cur_src * dx / dx / dx;
+    else if (cur_mode == 2) ey = ey - C.eyh * cur_src * dx / dx / dx;
+    else ez = ez - C.ezh * cur_src * dx / dx / dx;
+  }
+}
+
+}  // namespace fdtd

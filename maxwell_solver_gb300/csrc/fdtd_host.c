@@ -36,6 +36,8 @@ static const double k_c0 = 299792458;
 
 #define MAX_EVENTS 16
 #define GRAPH_CHUNK 32
+#define HASH_CAP 65536
+#define MAX_MATERIALS 32768
 
 /* ------------------------------------------------------------ errors */
 
@@ -80,7 +82,8 @@ typedef struct sim {
   fdtd_params prm;
   int init_const, init_ready, init_1d, init_src, init_ant, init_mu;
   int32_t I, J, K, T, num_ant, p, size1d;
-  int64_t IJ, IJK;
+  int32_t Ip;            /* row pitch of the device field arrays */
+  int64_t IJ, IJK, plane, cells;
   float fctr, delX, delT;
   float poly_m, alpha_m, sig_max, alpha_max, kappa_max;
   int32_t i0, i1, j0, j1, k0, k1;
@@ -100,6 +103,15 @@ typedef struct sim {
   float *d_den_ex, *d_den_hx, *d_inc[4], *d_src, *d_probes, *d_mu[3];
   int64_t *d_probe_idx;
   int32_t *d_ctr; /* [0] step base, [1] probe row */
+  int32_t *d_err; /* device error word (bounded-wait timeouts) */
+  uint16_t *d_mat;
+  float *d_tab;
+  unsigned long long *d_hkeys;
+  int64_t *d_hrep;
+  int32_t *d_hid, *d_hcnt;
+  int32_t coef_mode, num_mat;
+  int use_tma, allow_compress;
+  fdtd_maps maps;
   uint64_t device_bytes;
   fdtd_dev dev;
   pending_t pend;
@@ -153,6 +165,12 @@ int fdtd_create(fdtd_handle *out) {
   sim *s = (sim *)calloc(1, sizeof(sim));
   if (!s) return fail(FDTD_ERR_OOM, "out of host memory");
   s->prm = fdtd_default_params();
+  /* FDTD_KERNELS=direct selects the direct kernels, FDTD_COEF=arrays the
+   * per-cell coefficient arrays (both used by the comparison tests) */
+  const char *ek = getenv("FDTD_KERNELS");
+  const char *ec = getenv("FDTD_COEF");
+  s->use_tma = !(ek && strcmp(ek, "direct") == 0);
+  s->allow_compress = !(ec && strcmp(ec, "arrays") == 0);
   cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     free(s);
@@ -207,6 +225,13 @@ int fdtd_destroy(fdtd_handle h) {
   dfree(s->d_probes);
   dfree(s->d_probe_idx);
   dfree(s->d_ctr);
+  dfree(s->d_err);
+  dfree(s->d_mat);
+  dfree(s->d_tab);
+  dfree(s->d_hkeys);
+  dfree(s->d_hrep);
+  dfree(s->d_hid);
+  dfree(s->d_hcnt);
   free(s->h_src);
   free(s->h_probe_idx);
   free(s->h_den_ex);
@@ -273,6 +298,9 @@ int fdtd_set_const(fdtd_handle h, const float freqRes[3], const int32_t timeDim[
   s->p = p;
   s->IJ = (int64_t)I * J;
   s->IJK = s->IJ * K;
+  s->Ip = (I + 7) / 8 * 8;
+  s->plane = (int64_t)s->Ip * J;
+  s->cells = s->plane * K;
   const int32_t w = s->prm.tfsf_width;
   s->i0 = w;
   s->i1 = I - w - 1;
@@ -355,7 +383,7 @@ int fdtd_set_antenna_locations(fdtd_handle h, const int32_t *loc, size_t n) {
     const int64_t y = (int64_t)s->p + loc[a + 1 * s->num_ant];
     const int64_t z = (int64_t)s->p + loc[a + 2 * s->num_ant];
     const int inside = x >= 0 && x < s->I && y >= 0 && y < s->J && z >= 0 && z < s->K;
-    s->h_probe_idx[a] = inside ? x + y * s->I + z * s->IJ : -1;
+    s->h_probe_idx[a] = inside ? x + y * s->Ip + z * s->Ip * (int64_t)s->J : -1;
   }
   s->init_ant = 1;
   return FDTD_OK;
@@ -431,8 +459,11 @@ static void fill_dev_struct(sim *s) {
   d->J = s->J;
   d->K = s->K;
   d->p = s->p;
+  d->Ip = s->Ip;
   d->IJ = s->IJ;
   d->IJK = s->IJK;
+  d->plane = s->plane;
+  d->cells = s->cells;
   d->i0 = s->i0;
   d->i1 = s->i1;
   d->j0 = s->j0;
@@ -452,7 +483,10 @@ static void fill_dev_struct(sim *s) {
     d->f[a] = s->d_f[a];
     d->ce[a] = s->d_ce[a];
   }
-  d->coef_mode = 0;
+  d->coef_mode = s->coef_mode;
+  d->mat = s->d_mat;
+  d->mat_tab = s->d_tab;
+  d->err = s->d_err;
   for (int a = 0; a < FDTD_NUM_PSI; ++a) d->psi[a] = s->d_psi[a];
   for (int a = 0; a < 4; ++a) d->inc[a] = s->d_inc[a];
   d->src = s->d_src;
@@ -466,11 +500,12 @@ static void fill_dev_struct(sim *s) {
 /* Uploads the six material arrays into the coefficient buffers and turns
  * them into Cexe..Cezh in place (src/simulation.h:924-951 / :1099-1126). */
 static int upload_coefficients(sim *s) {
-  const size_t bytes = (size_t)s->IJK * sizeof(float);
   /* sigma_x -> ce[0], sigma_y -> ce[1], sigma_z -> ce[2], eps -> ce[3..5]:
    * the kernel reads both inputs of a component before writing its outputs */
   for (int a = 0; a < 6; ++a)
-    CU(cudaMemcpyAsync(s->d_ce[a], s->h_mat[a], bytes, cudaMemcpyHostToDevice, s->stream));
+    CU(cudaMemcpy2DAsync(s->d_ce[a], (size_t)s->Ip * sizeof(float), s->h_mat[a],
+                         (size_t)s->I * sizeof(float), (size_t)s->I * sizeof(float),
+                         (size_t)s->J * s->K, cudaMemcpyHostToDevice, s->stream));
   float *ce[6];
   const float *eps[3], *sig[3];
   for (int a = 0; a < 6; ++a) ce[a] = s->d_ce[a];
@@ -479,11 +514,30 @@ static int upload_coefficients(sim *s) {
     eps[a] = s->d_ce[3 + a];
   }
   KL(fdtdk_compute_ce(&s->dev, ce, eps, sig, s->d_den_ex, s->delT, s->stream));
+  /* material-indexed coefficients: the kernels then read a 2-byte id per
+   * cell instead of six floats; falls back to the arrays when the grid has
+   * more than MAX_MATERIALS distinct tuples */
+  s->coef_mode = 0;
+  s->num_mat = 0;
+  if (s->allow_compress) {
+    const float *cc[6];
+    for (int a = 0; a < 6; ++a) cc[a] = s->d_ce[a];
+    KL(fdtdk_compress_ce(&s->dev, cc, s->d_mat, s->d_tab, MAX_MATERIALS, s->d_hkeys, s->d_hrep,
+                         s->d_hid, HASH_CAP, s->d_hcnt, s->stream));
+    int32_t cnt[4];
+    CU(cudaMemcpyAsync(cnt, s->d_hcnt, sizeof(cnt), cudaMemcpyDeviceToHost, s->stream));
+    CU(cudaStreamSynchronize(s->stream));
+    if (!cnt[1] && !cnt[2] && cnt[0] > 0 && cnt[0] <= MAX_MATERIALS) {
+      s->coef_mode = 1;
+      s->num_mat = cnt[0];
+    }
+  }
+  fill_dev_struct(s);
   return FDTD_OK;
 }
 
 static int zero_state(sim *s) {
-  const size_t bytes = (size_t)s->IJK * sizeof(float);
+  const size_t bytes = (size_t)s->cells * sizeof(float);
   for (int a = 0; a < 6; ++a) CU(cudaMemsetAsync(s->d_f[a], 0, bytes, s->stream));
   const size_t psi_total = (size_t)(4 * 2 * (s->size_x + s->size_y + s->size_z)) * sizeof(float);
   CU(cudaMemsetAsync(s->d_psi_pool, 0, psi_total, s->stream));
@@ -535,12 +589,24 @@ int fdtd_ready_simulation(fdtd_handle h) {
     s->Chh = (float)((1 - q) / (1 + q));
     s->Che = (float)((double)s->delT / K_MU0 / (1 + q) / (double)s->delX);
   }
-  const size_t bytes = (size_t)s->IJK * sizeof(float);
+  const size_t bytes = (size_t)s->cells * sizeof(float);
   int rc;
   for (int a = 0; a < 6; ++a) {
     if ((rc = dalloc(s, (void **)&s->d_f[a], bytes))) return rc;
     if ((rc = dalloc(s, (void **)&s->d_ce[a], bytes))) return rc;
   }
+  if ((rc = dalloc(s, (void **)&s->d_mat, (size_t)s->cells * sizeof(uint16_t)))) return rc;
+  CU(cudaMemsetAsync(s->d_mat, 0, (size_t)s->cells * sizeof(uint16_t), s->stream));
+  if (s->allow_compress) {
+    if ((rc = dalloc(s, (void **)&s->d_tab, (size_t)MAX_MATERIALS * 6 * sizeof(float)))) return rc;
+    if ((rc = dalloc(s, (void **)&s->d_hkeys, (size_t)HASH_CAP * sizeof(unsigned long long))))
+      return rc;
+    if ((rc = dalloc(s, (void **)&s->d_hrep, (size_t)HASH_CAP * sizeof(int64_t)))) return rc;
+    if ((rc = dalloc(s, (void **)&s->d_hid, (size_t)HASH_CAP * sizeof(int32_t)))) return rc;
+    if ((rc = dalloc(s, (void **)&s->d_hcnt, 4 * sizeof(int32_t)))) return rc;
+  }
+  if ((rc = dalloc(s, (void **)&s->d_err, sizeof(int32_t)))) return rc;
+  CU(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream));
   const int64_t psi_n[FDTD_NUM_PSI] = {
       [PSI_EXY] = 2 * s->size_y, [PSI_EZY] = 2 * s->size_y, [PSI_HXY] = 2 * s->size_y,
       [PSI_HZY] = 2 * s->size_y, [PSI_EXZ] = 2 * s->size_z, [PSI_EYZ] = 2 * s->size_z,
@@ -574,6 +640,10 @@ int fdtd_ready_simulation(fdtd_handle h) {
   fill_dev_struct(s);
   if ((rc = upload_coefficients(s))) return rc;
   if ((rc = zero_state(s))) return rc;
+  if (s->use_tma) {
+    int e = fdtdk_make_maps(&s->dev, &s->maps);
+    if (e) s->maps.valid = 0; /* the direct kernels take over */
+  }
   CU(cudaStreamSynchronize(s->stream));
   s->init_ready = 1;
   return FDTD_OK;
@@ -686,8 +756,22 @@ int fdtd_init_1d(fdtd_handle h, float rate, const float *pw_source, size_t n) {
 /* ------------------------------------------------------------ step ops */
 
 static int issue(sim *s, int hfam, const fdtd_op *op) {
-  if (hfam) KL(fdtdk_half_h(&s->dev, op, s->stream));
-  else KL(fdtdk_half_e(&s->dev, op, s->stream));
+  if (hfam) KL(fdtdk_half_h(&s->dev, &s->maps, s->use_tma, op, s->stream));
+  else KL(fdtdk_half_e(&s->dev, &s->maps, s->use_tma, op, s->stream));
+  return FDTD_OK;
+}
+
+/* Reads the device error word after a synchronisation point. */
+static int check_device_error(sim *s) {
+  if (!s->d_err) return FDTD_OK;
+  int32_t e = 0;
+  CU(cudaMemcpyAsync(&e, s->d_err, sizeof(e), cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  if (e) {
+    cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream);
+    return fail(FDTD_ERR_CUDA, "a TMA pipeline wait timed out in a half-step kernel "
+                               "(device error word %d); the fields are not valid", e);
+  }
   return FDTD_OK;
 }
 
@@ -986,7 +1070,7 @@ int fdtd_synchronize(fdtd_handle h) {
   int rc = flush(s);
   if (rc) return rc;
   CU(cudaStreamSynchronize(s->stream));
-  return FDTD_OK;
+  return check_device_error(s);
 }
 
 /* src/simulation.h:572-619 */
@@ -1004,9 +1088,17 @@ int fdtd_output_vis(fdtd_handle h, float *out, size_t n, int32_t flag) {
     if (!s->init_ready) return fail(FDTD_ERR_STATE, "OutputVis of fields requires ReadySimulation");
     int rc = flush(s);
     if (rc) return rc;
-    CU(cudaMemcpyAsync(out, s->d_f[flag - 1], cnt * sizeof(float), cudaMemcpyDeviceToHost,
-                       s->stream));
+    /* device rows are pitched: whole rows by a 2D copy, then the tail */
+    const size_t rows = cnt / (size_t)s->I, tail = cnt % (size_t)s->I;
+    const float *src = s->d_f[flag - 1];
+    if (rows)
+      CU(cudaMemcpy2DAsync(out, (size_t)s->I * sizeof(float), src, (size_t)s->Ip * sizeof(float),
+                           (size_t)s->I * sizeof(float), rows, cudaMemcpyDeviceToHost, s->stream));
+    if (tail)
+      CU(cudaMemcpyAsync(out + rows * s->I, src + rows * s->Ip, tail * sizeof(float),
+                         cudaMemcpyDeviceToHost, s->stream));
     CU(cudaStreamSynchronize(s->stream));
+    return check_device_error(s);
   }
   return FDTD_OK;
 }
@@ -1021,7 +1113,7 @@ int fdtd_output_probes(fdtd_handle h, float *out, size_t n) {
   CU(cudaMemcpyAsync(out, s->d_probes, (n < total ? n : total) * sizeof(float),
                      cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
-  return FDTD_OK;
+  return check_device_error(s);
 }
 
 /* src/simulation.h:621-638 */
@@ -1058,8 +1150,8 @@ int fdtd_get_info(fdtd_handle h, fdtd_info *o) {
   o->j1 = s->j1;
   o->k0 = s->k0;
   o->k1 = s->k1;
-  o->coef_mode = s->dev.coef_mode;
-  o->num_materials = 0;
+  o->coef_mode = s->coef_mode;
+  o->num_materials = s->num_mat;
   o->device_bytes = s->device_bytes;
   o->Chh = s->Chh;
   o->Che = s->Che;

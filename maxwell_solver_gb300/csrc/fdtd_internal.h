@@ -24,10 +24,17 @@ enum {
   PSI_HXY, PSI_HXZ, PSI_HYX, PSI_HYZ, PSI_HZX, PSI_HZY
 };
 
-/* Everything a kernel needs to know about one grid (by value). */
+/* Everything a kernel needs to know about one grid (by value).
+ * Field, coefficient and material-id arrays are pitched: cell (i,j,k) is
+ * at i + j*Ip + k*Ip*J with Ip = I rounded up to a multiple of 8, so that
+ * every row starts 32-byte aligned and TMA strides are multiples of 16 B.
+ * CPML psi arrays and the 1D tables keep the reference's dense layouts. */
 typedef struct {
   int32_t I, J, K, p;
-  int64_t IJ, IJK;
+  int32_t Ip;               /* row pitch (elements) */
+  int64_t IJ, IJK;          /* logical I*J, I*J*K */
+  int64_t plane;            /* Ip*J: plane stride */
+  int64_t cells;            /* Ip*J*K: pitched array length */
   int32_t i0, i1, j0, j1, k0, k1;   /* TF/SF box */
   int32_t size1d, T;
   float Chh, Che, dx;
@@ -36,19 +43,32 @@ typedef struct {
   float *f[6];              /* Ex Ey Ez Hx Hy Hz, x-fastest IJK each */
   const float *ce[6];       /* Cexe Ceye Ceze Cexh Ceyh Cezh (coef_mode 0) */
   int32_t coef_mode;        /* 0: per-cell arrays; 1: material-indexed */
-  const uint16_t *mat;      /* coef_mode 1: material id per cell */
-  const float *mat_tab;     /* coef_mode 1: [n_mat][n_xclass][6] */
-  const uint8_t *xclass;    /* coef_mode 1: x-class of each i (Imax) */
-  int32_t n_xclass;
+  const uint16_t *mat;      /* coef_mode 1: coefficient-tuple id per cell */
+  const float *mat_tab;     /* coef_mode 1: [n][6] Cexe..Cezh per id */
   float *psi[FDTD_NUM_PSI];
   const float *inc[4];      /* Ez_1D, Hy_1D, E_inv_1D, H_inv_1D: [T][size1d] */
   const float *src;         /* current-source waveform [T] */
   int32_t *step_base;       /* device step base for graph-replayed steps */
   int32_t *probe_row;       /* device probe row counter */
   float *probes;            /* [T][num_ant][6] */
-  const int64_t *probe_idx; /* [num_ant] cell index, -1 if outside */
+  const int64_t *probe_idx; /* [num_ant] pitched cell index, -1 if outside */
   int32_t num_ant;
+  int32_t *err;             /* device error word (bounded-wait timeouts) */
 } fdtd_dev;
+
+/* TMA descriptors (CUtensorMap, 128 B each) of one grid: 0..5 = Ex Ey Ez Hx
+ * Hy Hz as E-half-step boxes, 6..11 the same arrays as H-half-step boxes,
+ * 12 = material ids.  Opaque to C. */
+#define FDTD_NUM_MAPS 13
+#ifdef __cplusplus
+#define FDTD_ALIGN64 alignas(64)
+#else
+#define FDTD_ALIGN64 _Alignas(64)
+#endif
+typedef struct {
+  FDTD_ALIGN64 unsigned char bytes[FDTD_NUM_MAPS][128];
+  int32_t valid;            /* 1 when every map encoded */
+} fdtd_maps;
 
 /* One fused half-step: which parts run, for which step. */
 typedef struct {
@@ -61,9 +81,26 @@ typedef struct {
   int32_t cur_box[6];
 } fdtd_op;
 
-/* Launchers (fdtd_kernels.cu).  Return cudaError_t as int. */
-int fdtdk_half_h(const fdtd_dev *d, const fdtd_op *op, cudaStream_t s);
-int fdtdk_half_e(const fdtd_dev *d, const fdtd_op *op, cudaStream_t s);
+/* Launchers (fdtd_kernels.cu).  Return cudaError_t as int.  With valid
+ * maps and op->curl set, the TMA-pipelined kernels run (fdtd_tma.cu);
+ * otherwise the direct kernels.  use_tma = 0 forces the direct kernels. */
+int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
+                 cudaStream_t s);
+int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
+                 cudaStream_t s);
+/* Encodes the TMA descriptors for the current device pointers (fdtd_tma.cu). */
+int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m);
+int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s);
+int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s);
+/* Material-indexed E coefficients: dedupes the per-cell tuples of ce[6]
+ * into mat[] ids and a [n][6] table.  Returns the number of distinct
+ * tuples in *n_out, or 0 when they do not fit max_mat / collide. */
+int fdtdk_compress_ce(const fdtd_dev *d, const float *const ce[6], uint16_t *mat,
+                      float *tab, int32_t max_mat, unsigned long long *hash_keys,
+                      int64_t *hash_rep, int32_t *hash_id, int32_t hash_cap,
+                      int32_t *counters, cudaStream_t s);
+/* Reads the compression counters: [0] distinct tuples, [1] overflow,
+ * [2] collision. */
 int fdtdk_probe_gather(const fdtd_dev *d, cudaStream_t s);
 int fdtdk_set_i32(int32_t *dst, int32_t v, cudaStream_t s);
 int fdtdk_add_i32(int32_t *dst, int32_t v, cudaStream_t s);

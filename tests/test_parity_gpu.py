@@ -129,3 +129,51 @@ def test_setup_tables_match_reference():
     inf = info(P)
     assert np.float32(inf["Chh"]) == g["Chh"] and np.float32(inf["Che"]) == g["Che"]
     simFDTD("DeleteSimulation", P)
+
+
+@pytest.fixture
+def kernel_env(monkeypatch):
+    """Selects the kernel family / coefficient storage for handles created
+    while the fixture is active (read by fdtd_create)."""
+    def set_env(kernels, coef):
+        monkeypatch.setenv("FDTD_KERNELS", kernels)
+        monkeypatch.setenv("FDTD_COEF", coef)
+    return set_env
+
+
+@pytest.mark.parametrize("kernels,coef", [("tma", "indexed"), ("tma", "arrays"),
+                                          ("direct", "indexed"), ("direct", "arrays")])
+@pytest.mark.parametrize("name", ["mode1_spheres", "mode3_probes_y_current", "gic_currents_x"])
+def test_kernel_variants_match_oracle(kernel_env, kernels, coef, name):
+    """TMA-pipelined and direct kernels, material-indexed and per-cell
+    coefficients: all bit-identical to the oracle."""
+    from maxwell_solver_gb300 import info, simFDTD
+
+    kernel_env(kernels, coef)
+    sc = by_name(name)
+    _, inp = _golden_inputs(name)
+    P = run_mex(simFDTD, sc, inp)
+    inf = info(P)
+    assert inf["coef_mode"] == (1 if coef == "indexed" else 0)
+    if coef == "indexed":
+        assert 0 < inf["num_materials"] <= 64
+    got = read_fields(simFDTD, P, sc.dims)
+    assert_parity(got, run_oracle(sc, "f32", inp=inp))
+    simFDTD("DeleteSimulation", P)
+
+
+def test_many_materials_fall_back_to_arrays():
+    """More distinct coefficient tuples than the id table holds: the solver
+    keeps the per-cell arrays and stays exact."""
+    from maxwell_solver_gb300 import info, simFDTD
+
+    sc = by_name("hf_mode3_vacuum")
+    inp = sc.inputs()
+    n = int(np.prod(sc.dims))
+    rng = np.random.default_rng(5)
+    inp["mats"][4] = (1.0 + rng.random(n)).astype(np.float32)  # ~49k distinct eps_x
+    P = run_mex(simFDTD, sc, inp)
+    assert info(P)["coef_mode"] == 0
+    got = read_fields(simFDTD, P, sc.dims)
+    assert_parity(got, run_oracle(sc, "f32", inp=inp))
+    simFDTD("DeleteSimulation", P)
