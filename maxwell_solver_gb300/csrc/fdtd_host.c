@@ -102,7 +102,7 @@ typedef struct sim {
   float *d_f[6], *d_ce[6], *d_psi_pool, *d_psi[FDTD_NUM_PSI];
   float *d_den_ex, *d_den_hx, *d_inc[4], *d_src, *d_probes, *d_mu[3];
   int64_t *d_probe_idx;
-  int32_t *d_ctr; /* [0] step base, [1] probe row */
+  int32_t *d_ctr; /* [0] step base, [1] probe row, [2..3] work queue */
   int32_t *d_err; /* device error word (bounded-wait timeouts) */
   uint16_t *d_mat;
   float *d_tab;
@@ -486,12 +486,14 @@ static void fill_dev_struct(sim *s) {
   d->coef_mode = s->coef_mode;
   d->mat = s->d_mat;
   d->mat_tab = s->d_tab;
+  d->n_mat = s->num_mat;
   d->err = s->d_err;
   for (int a = 0; a < FDTD_NUM_PSI; ++a) d->psi[a] = s->d_psi[a];
   for (int a = 0; a < 4; ++a) d->inc[a] = s->d_inc[a];
   d->src = s->d_src;
   d->step_base = s->d_ctr;
   d->probe_row = s->d_ctr ? s->d_ctr + 1 : NULL;
+  d->work = s->d_ctr ? s->d_ctr + 2 : NULL;
   d->probes = s->d_probes;
   d->probe_idx = s->d_probe_idx;
   d->num_ant = (s->init_ant && s->d_probes) ? s->num_ant : 0;
@@ -541,7 +543,7 @@ static int zero_state(sim *s) {
   for (int a = 0; a < 6; ++a) CU(cudaMemsetAsync(s->d_f[a], 0, bytes, s->stream));
   const size_t psi_total = (size_t)(4 * 2 * (s->size_x + s->size_y + s->size_z)) * sizeof(float);
   CU(cudaMemsetAsync(s->d_psi_pool, 0, psi_total, s->stream));
-  CU(cudaMemsetAsync(s->d_ctr, 0, 2 * sizeof(int32_t), s->stream));
+  CU(cudaMemsetAsync(s->d_ctr, 0, 4 * sizeof(int32_t), s->stream));
   return FDTD_OK;
 }
 
@@ -624,7 +626,7 @@ int fdtd_ready_simulation(fdtd_handle h) {
   }
   if ((rc = dalloc(s, (void **)&s->d_den_ex, (size_t)s->I * sizeof(float)))) return rc;
   if ((rc = dalloc(s, (void **)&s->d_den_hx, (size_t)s->I * sizeof(float)))) return rc;
-  if ((rc = dalloc(s, (void **)&s->d_ctr, 2 * sizeof(int32_t)))) return rc;
+  if ((rc = dalloc(s, (void **)&s->d_ctr, 4 * sizeof(int32_t)))) return rc;
   CU(cudaMemcpyAsync(s->d_den_ex, s->h_den_ex, (size_t)s->I * sizeof(float),
                      cudaMemcpyHostToDevice, s->stream));
   CU(cudaMemcpyAsync(s->d_den_hx, s->h_den_hx, (size_t)s->I * sizeof(float),

@@ -45,10 +45,13 @@ typedef struct {
   int32_t coef_mode;        /* 0: per-cell arrays; 1: material-indexed */
   const uint16_t *mat;      /* coef_mode 1: coefficient-tuple id per cell */
   const float *mat_tab;     /* coef_mode 1: [n][6] Cexe..Cezh per id */
+  int32_t n_mat;            /* coef_mode 1: number of ids */
   float *psi[FDTD_NUM_PSI];
   const float *inc[4];      /* Ez_1D, Hy_1D, E_inv_1D, H_inv_1D: [T][size1d] */
   const float *src;         /* current-source waveform [T] */
   int32_t *step_base;       /* device step base for graph-replayed steps */
+  int32_t *work;            /* [0] work-item counter, [1] finished producers
+                               (persistent kernels; zero between launches) */
   int32_t *probe_row;       /* device probe row counter */
   float *probes;            /* [T][num_ant][6] */
   const int64_t *probe_idx; /* [num_ant] pitched cell index, -1 if outside */

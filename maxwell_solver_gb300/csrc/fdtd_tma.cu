@@ -1,30 +1,40 @@
 /*
- * fdtd_tma.cu -- TMA-pipelined half-step kernels for sm_103a.
+ * fdtd_tma.cu -- persistent, warp-specialised TMA kernels of the two
+ * half-steps for sm_103a.
  *
- * Each block owns a 64 x 8 (x, y) tile of a z-chunk and marches up in z.
- * One elected thread streams every z-plane the tile needs into a 4-stage
- * shared-memory ring with cp.async.bulk.tensor (TMA) copies completing on
- * per-stage mbarriers, so three to four planes of all fields are in flight
- * per block whatever the register count; the 256 threads compute from
- * shared memory (two cells each) and store their results with coalesced
- * stores.  The per-cell arithmetic is fdtd_device.cuh's, so results equal
- * the direct kernels' and the reference's bit for bit.
+ * Work: the grid is cut into items of one 64 x 8 (x, y) tile and a run of
+ * z-planes.  A launch is persistent (as many blocks as fit, at most one
+ * per item): in every block one producer warp takes items from a global
+ * atomic counter and streams every z-plane the item needs into a
+ * shared-memory ring with cp.async.bulk.tensor (TMA) copies that complete
+ * on the stage's "full" mbarrier; eight consumer warps wait on "full",
+ * compute their cells from shared memory and release the stage on its
+ * "empty" mbarrier.  There is no block-wide barrier in the steady state,
+ * the ring stays full across item boundaries, and the dynamic queue keeps
+ * the blocks busy to the end of the launch.  The producer that finishes
+ * last rewinds the counter for the next launch.
  *
  *   E half-step, plane k: E tile (64x8) + H tile with the x-1 / y-1 halo
  *     (68x9, box origin (x0-4, y0-1): the x origin stays 16-byte aligned)
  *     + the material-id tile; Hx, Hy of plane k-1 are carried in registers.
  *   H half-step, plane k: E tile with the x+1 / y+1 halo (68x9 at (x0, y0))
- *     + H tile; Ex, Ey of plane k+1 come from the next stage of the ring.
+ *     + H tile; Ex, Ey of plane k+1 come from the item's next load.
  *
- * Out-of-range boxes (grid edges, x < 0) are zero-filled by the TMA unit.
- * Every wait on an mbarrier is bounded: on a timeout the block drains its
- * own copies in flight (also bounded), raises the device error word and
- * returns.
+ * Cells with no CPML, TF/SF face or source in their warp take a lean
+ * curl-only path; the others go through fdtd_device.cuh's full per-cell
+ * functions.  Both compute the reference's operations in the reference's
+ * order, so results equal the direct kernels' and the reference's bit for
+ * bit.  Out-of-range boxes (grid edges, x < 0) are zero-filled by TMA.
+ *
+ * Every mbarrier wait is bounded.  A consumer that times out raises the
+ * device error word and leaves; the producer, whose waits are bounded too,
+ * then gives up, waits (bounded) for its own copies in flight and leaves.
  */
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "fdtd_device.cuh"
@@ -36,52 +46,61 @@ extern "C" void fdtdk_count_launches(unsigned long long n);
 
 namespace {
 
-constexpr int BX = 64, BY = 8, NT = 256, NS = 4;
-constexpr int HW = BX + 4;                  // halo box row (floats)
-constexpr int HH = BY + 1;                  // halo box rows
-constexpr int TILE_B = BX * BY * 4;         // 2048 B
-constexpr int HALO_B = HW * HH * 4;         // 2448 B transferred
-constexpr int HALO_SLOT = 2560;             // 128-byte aligned slot
-constexpr int MAT_B = BX * BY * 2;          // 1024 B
+constexpr int BX = 64, BY = 8;
+constexpr int NCW = 8;                       // consumer warps
+constexpr int NT = (NCW + 1) * 32;           // + one producer warp
+constexpr int NSE = 4, NSH = 5;              // ring stages (E, H)
+constexpr int HW = BX + 4;                   // halo box row (floats)
+constexpr int HH = BY + 1;                   // halo box rows
+constexpr int TILE_B = BX * BY * 4;          // 2048 B
+constexpr int HALO_B = HW * HH * 4;          // 2448 B transferred
+constexpr int HALO_SLOT = 2560;              // 128-byte aligned slot
+constexpr int MAT_B = BX * BY * 2;           // 1024 B
 constexpr int E_OFF_H = 3 * TILE_B;
 constexpr int E_OFF_M = E_OFF_H + 3 * HALO_SLOT;
-constexpr int E_STAGE = E_OFF_M + MAT_B;    // 14848 B
+constexpr int E_STAGE = E_OFF_M + MAT_B;     // 14848 B
 constexpr int H_OFF_H = 3 * HALO_SLOT;
 constexpr int H_STAGE = H_OFF_H + 3 * TILE_B;  // 13824 B
-constexpr int E_SMEM = NS * E_STAGE + 64;
-constexpr int H_SMEM = NS * H_STAGE + 64;
-constexpr unsigned kSpinLimit = 1u << 22;   // bounded mbarrier waits
+constexpr int kSmemTabMax = 512;             // coefficient ids staged in shared memory
+constexpr int CTRL_B = 256;                  // barriers + stage metadata
+constexpr int E_SMEM = NSE * E_STAGE + CTRL_B + kSmemTabMax * 6 * 4;
+constexpr int H_SMEM = NSH * H_STAGE + CTRL_B;
+constexpr unsigned kSpinLimit = 1u << 22;    // bounded mbarrier waits
 static_assert(E_STAGE % 128 == 0 && H_STAGE % 128 == 0, "stage alignment");
 static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
               "TMA inner box extents must be multiples of 16 bytes");
+static_assert(NSH * (8 + 8 + 16) <= CTRL_B && NSE * (8 + 8 + 16) <= CTRL_B, "control block");
 
 struct Maps {
   CUtensorMap m[FDTD_NUM_MAPS];
 };
 
+// Per-launch geometry of the work items.
+struct Items {
+  int tiles_x, tiles_y, zchunk, nk, n_items;
+};
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
-
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
                : "memory");
 }
-
 __device__ __forceinline__ void mbar_init_fence() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-
 __device__ __forceinline__ void proxy_fence() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
-
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes)
                : "memory");
 }
-
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -93,14 +112,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-
 // Bounded wait for phase `parity` of an mbarrier; false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   for (unsigned it = 0; it < kSpinLimit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
-
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar,
                                             int x, int y, int z) {
   asm volatile(
@@ -110,77 +127,154 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, u
       : "memory");
 }
 
-// Timeout path of thread 0: wait (bounded) for the planes [from, issued)
-// still in flight so no copy lands after the block is gone, then raise
-// the error word.  A plane whose copies already completed returns at once
-// (its stage has not been re-armed).
-__device__ void drain_and_flag(uint64_t *bars, int from, int issued, int32_t *err, int code) {
-  for (int q = from; q < issued; ++q) mbar_wait(&bars[q % NS], (uint32_t)((q / NS) & 1));
-  if (err) atomicExch(err, code);
+__device__ __forceinline__ void decode_item(const Items &it, int w, int &x0, int &y0, int &kb,
+                                            int &np) {
+  const int nt = it.tiles_x * it.tiles_y;
+  const int chunk = w / nt, tile = w - chunk * nt;
+  x0 = (tile % it.tiles_x) * BX;
+  y0 = (tile / it.tiles_x) * BY;
+  kb = chunk * it.zchunk;
+  np = min(it.zchunk, it.nk - kb);
+}
+
+// Producer side of one launch (lane 0 of the producer warp).  `extra` more
+// loads follow each item's np planes (the H half-step reads plane k+1).
+// Ends with a sentinel stage, rewinds the work counter when it is the last
+// producer, and waits for its own copies before returning.
+template <int NS, class IssueFn>
+__device__ void produce(const fdtd_dev &d, const Items &it, int extra, uint64_t *full,
+                        uint64_t *empty, int4 *meta, IssueFn issue) {
+  int q = 0;
+  bool ok = true;
+  for (;;) {
+    const int w = atomicAdd(&d.work[0], 1);
+    if (w >= it.n_items) break;
+    int x0, y0, kb, np;
+    decode_item(it, w, x0, y0, kb, np);
+    for (int t = 0; t < np + extra && ok; ++t, ++q) {
+      const int s = q % NS;
+      if (q >= NS) ok = mbar_wait(&empty[s], (uint32_t)(((q / NS) - 1) & 1));
+      if (!ok) break;
+      meta[s] = make_int4(w, t, np, kb);
+      issue(s, x0, y0, kb + t);
+    }
+    if (!ok) break;
+  }
+  if (atomicAdd(&d.work[1], 1) == (int)gridDim.x - 1) {  // last producer: rewind
+    atomicExch(&d.work[0], 0);
+    atomicExch(&d.work[1], 0);
+  }
+  if (ok) {  // sentinel: tells the consumers there is no more work
+    const int s = q % NS;
+    if (q >= NS) ok = mbar_wait(&empty[s], (uint32_t)(((q / NS) - 1) & 1));
+    if (ok) {
+      meta[s] = make_int4(-1, 0, 0, 0);
+      mbar_arrive(&full[s]);
+      ++q;
+    }
+  }
+  if (!ok && d.err) atomicExch(d.err, 3);
+  // drain: every copy issued by this block has landed before it retires
+  for (int r = (q > NS ? q - NS : 0); r < q; ++r) mbar_wait(&full[r % NS], (uint32_t)((r / NS) & 1));
+}
+
+// Thread -> cell map of the consumer warps: warp w covers one 32-cell x run
+// (half w & 1 of the 64-wide tile) of rows w >> 1 and (w >> 1) + 4, so that
+// whole warps fall inside or outside the CPML x slabs and TF/SF x faces.
+__device__ __forceinline__ void cell_map(int tid, int &xo, int &r0) {
+  const int w = tid >> 5;
+  xo = 32 * (w & 1) + (tid & 31);
+  r0 = w >> 1;
 }
 
 // ----------------------------------------------------------------- E half
 
 template <bool PML>
 __global__ void __launch_bounds__(NT, 3)
-    k_half_e_tma(const fdtd_dev d, const fdtd_op op, const __grid_constant__ Maps mp, int zchunk) {
+    k_half_e_tma(const fdtd_dev d, const fdtd_op op, const __grid_constant__ Maps mp,
+                 const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NS * E_STAGE);
-  const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
-  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
-  const int I = d.I, J = d.J, K = d.K;
-  const int kb = blockIdx.z * zchunk, ke = min(kb + zchunk, K);
-  if (kb >= ke) return;
-  const int np = ke - kb;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSE * E_STAGE);
+  uint64_t *empty = full + NSE;
+  int4 *meta = reinterpret_cast<int4 *>(empty + NSE);
+  float *stab = reinterpret_cast<float *>(smem + NSE * E_STAGE + CTRL_B);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool use_mat = d.coef_mode == 1;
-  const uint32_t tx_bytes = 3 * TILE_B + 3 * HALO_B + (use_mat ? MAT_B : 0);
-  int issued = 0;  // thread 0 only
+  const bool tab_in_smem = use_mat && d.n_mat <= kSmemTabMax;
 
   if (tid == 0) {
-    for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < NSE; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NCW);
+    }
     mbar_init_fence();
   }
+  if (tab_in_smem)
+    for (int t = tid; t < d.n_mat * 6; t += NT) stab[t] = __ldg(d.mat_tab + t);
   __syncthreads();
-  auto issue = [&](int q) {  // plane kb + q into stage q % NS
-    unsigned char *st = smem + (q % NS) * E_STAGE;
-    uint64_t *bar = &bars[q % NS];
-    const int k = kb + q;
-    proxy_fence();
-    mbar_expect_tx(bar, tx_bytes);
-    for (int c = 0; c < 3; ++c) tma_load_3d(st + c * TILE_B, &mp.m[c], bar, x0, y0, k);
-    for (int c = 0; c < 3; ++c)
-      tma_load_3d(st + E_OFF_H + c * HALO_SLOT, &mp.m[3 + c], bar, x0 - 4, y0 - 1, k);
-    if (use_mat) tma_load_3d(st + E_OFF_M, &mp.m[12], bar, x0, y0, k);
-  };
-  if (tid == 0)
-    for (; issued < NS && issued < np; ++issued) issue(issued);
 
-  const int j = y0 + ty;
+  if (warp == NCW) {  // ------------------------------------- producer
+    if (lane == 0) {
+      const uint32_t tx_bytes = 3 * TILE_B + 3 * HALO_B + (use_mat ? MAT_B : 0);
+      produce<NSE>(d, it, 0, full, empty, meta, [&](int s, int x0, int y0, int k) {
+        unsigned char *st = smem + s * E_STAGE;
+        proxy_fence();
+        mbar_expect_tx(&full[s], tx_bytes);
+        for (int c = 0; c < 3; ++c) tma_load_3d(st + c * TILE_B, &mp.m[c], &full[s], x0, y0, k);
+        for (int c = 0; c < 3; ++c)
+          tma_load_3d(st + E_OFF_H + c * HALO_SLOT, &mp.m[3 + c], &full[s], x0 - 4, y0 - 1, k);
+        if (use_mat) tma_load_3d(st + E_OFF_M, &mp.m[12], &full[s], x0, y0, k);
+      });
+    }
+    return;
+  }
+
+  // ------------------------------------------------------------ consumers
+  const int I = d.I, J = d.J, K = d.K;
+  int xo, r0;
+  cell_map(tid, xo, r0);
   const int mode = op.tfsf_mode;
   const int cm = op.cur_mode;
   const int step = (mode || cm) ? op_step(d, op) : 0;
   const float *inc = mode ? inc_e_row(d, mode, step) : nullptr;
-  float hx_km[2] = {0.f, 0.f}, hy_km[2] = {0.f, 0.f};
-  bool cur_col[2];
-  float cur_src = 0.f;
-#pragma unroll
-  for (int c = 0; c < 2; ++c) {
-    const int i = x0 + lane + 32 * c;
-    cur_col[c] = cm && in_range(i, op.cur_box[0], op.cur_box[1]) &&
-                 in_range(j, op.cur_box[2], op.cur_box[3]);
-    if (kb > 0 && i < I && j < J) {
-      const int64_t n = i + (int64_t)j * d.Ip + (int64_t)(kb - 1) * d.plane;
-      hx_km[c] = d.f[3][n];
-      hy_km[c] = d.f[4][n];
-    }
-  }
-  if (cm && (cur_col[0] || cur_col[1])) cur_src = d.src[step];
+  const float cur_src = cm ? d.src[step] : 0.f;
 
-  bool timeout = false;
-  for (int t = 0; t < np; ++t) {
-    const int s = t % NS;
-    if (!timeout) timeout = !mbar_wait(&bars[s], (uint32_t)((t / NS) & 1));
-    const int k = kb + t;
+  int i = 0, y0 = 0, kb = 0;
+  bool valid[2] = {false, false}, col_special[2] = {false, false}, cur_col[2] = {false, false};
+  float hx_km[2] = {0.f, 0.f}, hy_km[2] = {0.f, 0.f};
+  int64_t n0[2] = {0, 0};
+
+  for (int q = 0;; ++q) {
+    const int s = q % NSE;
+    if (!mbar_wait(&full[s], (uint32_t)((q / NSE) & 1))) {
+      if (d.err) atomicExch(d.err, 1);
+      return;
+    }
+    const int4 m = meta[s];
+    if (m.x < 0) return;  // sentinel
+    if (m.y == 0) {       // first plane of a new item: column constants
+      int x0, np;
+      decode_item(it, m.x, x0, y0, kb, np);
+      i = x0 + xo;
+      const bool cur_x = cm && in_range(i, op.cur_box[0], op.cur_box[1]);
+      const bool x_special =
+          (PML && slab_e(i, I, d.p) >= 0) || (mode && (i == d.i0 || i == d.i1)) || i == 0;
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int j = y0 + r0 + 4 * c;
+        valid[c] = i < I && j < J;
+        cur_col[c] = cur_x && in_range(j, op.cur_box[2], op.cur_box[3]);
+        col_special[c] = x_special || (PML && slab_e(j, J, d.p) >= 0) ||
+                         (mode && (j == d.j0 || j == d.j1)) || cur_col[c] || j == 0;
+        n0[c] = valid[c] ? i + (int64_t)j * d.Ip + (int64_t)kb * d.plane : 0;
+        hx_km[c] = hy_km[c] = 0.f;
+        if (kb > 0 && valid[c]) {
+          hx_km[c] = d.f[3][n0[c] - d.plane];
+          hy_km[c] = d.f[4][n0[c] - d.plane];
+        }
+      }
+    }
+    const int k = kb + m.y;
     const unsigned char *st = smem + s * E_STAGE;
     const float *sEx = reinterpret_cast<const float *>(st);
     const float *sEy = sEx + BX * BY;
@@ -189,35 +283,57 @@ __global__ void __launch_bounds__(NT, 3)
     const float *sHy = sHx + HALO_SLOT / 4;
     const float *sHz = sHy + HALO_SLOT / 4;
     const uint16_t *sM = reinterpret_cast<const uint16_t *>(st + E_OFF_M);
+    const bool plane_special = (PML && slab_e(k, K, d.p) >= 0) ||
+                               (mode && (k == d.k0 || k == d.k1)) || k == 0 ||
+                               (cm && in_range(k, op.cur_box[4], op.cur_box[5]));
+    const int64_t off = (int64_t)m.y * d.plane;
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-      const int xo = lane + 32 * c;
-      const int i = x0 + xo;
-      if (i < I && j < J && !timeout) {
-        const int hb = (ty + 1) * HW + xo + 4;  // own cell in the halo tile
-        const int eb = ty * BX + xo;            // own cell in the plain tile
-        const float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
-        const int64_t n = i + (int64_t)j * d.Ip + (int64_t)k * d.plane;
-        const Coef6 C = use_mat ? coef_from_table(d, sM[eb]) : coef_from_arrays(d, n);
-        float ex = sEx[eb], ey = sEy[eb], ez = sEz[eb];
-        int px = -1, py = -1, pz = -1;
-        if (PML) e_slabs(d, i, j, k, px, py, pz);
-        const bool cur = cur_col[c] && in_range(k, op.cur_box[4], op.cur_box[5]);
-        update_e_cell<true, PML>(d, mode, inc, cm, cur_src, cur, i, j, k, px, py, pz, C, ex,
-                                 ey, ez, hx, hy, hz, sHz[hb - HW], sHx[hb - HW], sHz[hb - 1],
-                                 sHy[hb - 1], hx_km[c], hy_km[c]);
-        d.f[0][n] = ex;
-        d.f[1][n] = ey;
-        d.f[2][n] = ez;
-        hx_km[c] = hx;
-        hy_km[c] = hy;
+      const int ty = r0 + 4 * c;
+      const bool act = valid[c];
+      const int hb = (ty + 1) * HW + xo + 4;  // own cell in the halo tile
+      const int eb = ty * BX + xo;            // own cell in the plain tile
+      Coef6 C = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (use_mat) {
+        const int mi = sM[eb];
+        if (tab_in_smem) {
+          const float *r = stab + mi * 6;
+          C.exe = r[0]; C.eye = r[1]; C.eze = r[2]; C.exh = r[3]; C.eyh = r[4]; C.ezh = r[5];
+        } else {
+          C = coef_from_table(d, mi);
+        }
+      } else if (act) {
+        C = coef_from_arrays(d, n0[c] + off);
       }
+      const float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
+      const float hz_jm = sHz[hb - HW], hx_jm = sHx[hb - HW];
+      const float hz_im = sHz[hb - 1], hy_im = sHy[hb - 1];
+      float ex = sEx[eb], ey = sEy[eb], ez = sEz[eb];
+      if (__any_sync(0xffffffffu, act && (col_special[c] || plane_special))) {
+        if (act) {
+          const int j = y0 + ty;
+          int px = -1, py = -1, pz = -1;
+          if (PML) e_slabs(d, i, j, k, px, py, pz);
+          const bool cur = cur_col[c] && in_range(k, op.cur_box[4], op.cur_box[5]);
+          update_e_cell<true, PML>(d, mode, inc, cm, cur_src, cur, i, j, k, px, py, pz, C, ex,
+                                   ey, ez, hx, hy, hz, hz_jm, hx_jm, hz_im, hy_im, hx_km[c],
+                                   hy_km[c]);
+        }
+      } else {  // interior warp: i, j, k >= 1, no CPML, TF/SF face or source
+        ex = C.exe * ex + C.exh * (+(hz - hz_jm) - (hy - hy_km[c]));
+        ey = C.eye * ey + C.eyh * (+(hx - hx_km[c]) - (hz - hz_im));
+        ez = C.eze * ez + C.ezh * (+(hy - hy_im) - (hx - hx_jm));
+      }
+      if (act) {
+        d.f[0][n0[c] + off] = ex;
+        d.f[1][n0[c] + off] = ey;
+        d.f[2][n0[c] + off] = ez;
+      }
+      hx_km[c] = hx;
+      hy_km[c] = hy;
     }
-    if (__syncthreads_or(timeout)) {
-      if (tid == 0) drain_and_flag(bars, t, issued, d.err, 1);
-      return;
-    }
-    if (tid == 0 && issued < np) issue(issued++);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
@@ -225,116 +341,172 @@ __global__ void __launch_bounds__(NT, 3)
 
 template <bool PML>
 __global__ void __launch_bounds__(NT, 3)
-    k_half_h_tma(const fdtd_dev d, const fdtd_op op, const __grid_constant__ Maps mp, int zchunk) {
+    k_half_h_tma(const fdtd_dev d, const fdtd_op op, const __grid_constant__ Maps mp,
+                 const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NS * H_STAGE);
-  const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
-  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
-  const int I = d.I, J = d.J, K = d.K, p = d.p;
-  const int kb = blockIdx.z * zchunk, ke = min(kb + zchunk, K - 1);
-  if (kb >= ke) return;
-  const int np = ke - kb;  // planes computed
-  const int nl = np + 1;   // planes loaded (E of plane k+1 is read)
-  const uint32_t tx_bytes = 3 * HALO_B + 3 * TILE_B;
-  int issued = 0;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSH * H_STAGE);
+  uint64_t *empty = full + NSH;
+  int4 *meta = reinterpret_cast<int4 *>(empty + NSH);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
-    for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < NSH; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NCW);
+    }
     mbar_init_fence();
   }
   __syncthreads();
-  auto issue = [&](int q) {
-    unsigned char *st = smem + (q % NS) * H_STAGE;
-    uint64_t *bar = &bars[q % NS];
-    const int k = kb + q;
-    proxy_fence();
-    mbar_expect_tx(bar, tx_bytes);
-    for (int c = 0; c < 3; ++c) tma_load_3d(st + c * HALO_SLOT, &mp.m[6 + c], bar, x0, y0, k);
-    for (int c = 0; c < 3; ++c)
-      tma_load_3d(st + H_OFF_H + c * TILE_B, &mp.m[9 + c], bar, x0, y0, k);
-  };
-  if (tid == 0)
-    for (; issued < NS && issued < nl; ++issued) issue(issued);
 
-  const int j = y0 + ty;
+  if (warp == NCW) {  // ------------------------------------- producer
+    if (lane == 0) {
+      const uint32_t tx_bytes = 3 * HALO_B + 3 * TILE_B;
+      produce<NSH>(d, it, 1, full, empty, meta, [&](int s, int x0, int y0, int k) {
+        unsigned char *st = smem + s * H_STAGE;
+        proxy_fence();
+        mbar_expect_tx(&full[s], tx_bytes);
+        for (int c = 0; c < 3; ++c)
+          tma_load_3d(st + c * HALO_SLOT, &mp.m[6 + c], &full[s], x0, y0, k);
+        for (int c = 0; c < 3; ++c)
+          tma_load_3d(st + H_OFF_H + c * TILE_B, &mp.m[9 + c], &full[s], x0, y0, k);
+      });
+    }
+    return;
+  }
+
+  // ------------------------------------------------------------ consumers
+  const int I = d.I, J = d.J, K = d.K, p = d.p;
+  int xo, r0;
+  cell_map(tid, xo, r0);
   const int mode = op.tfsf_mode;
   const float *inc = mode ? inc_h_row(d, mode, op_step(d, op)) : nullptr;
-  const int py = PML ? slab_h(j, J, p) : -1;
+  const float Chh = d.Chh, Che = d.Che;
 
-  bool timeout = !mbar_wait(&bars[0], 0u);
-  for (int t = 0; t < np; ++t) {
-    const int s0 = t % NS, s1 = (t + 1) % NS;
-    if (!timeout) timeout = !mbar_wait(&bars[s1], (uint32_t)(((t + 1) / NS) & 1));
-    const int k = kb + t;
-    const unsigned char *st0 = smem + s0 * H_STAGE;
-    const unsigned char *st1 = smem + s1 * H_STAGE;
-    const float *sEx = reinterpret_cast<const float *>(st0);
-    const float *sEy = sEx + HALO_SLOT / 4;
-    const float *sEz = sEy + HALO_SLOT / 4;
-    const float *sEx1 = reinterpret_cast<const float *>(st1);
-    const float *sEy1 = sEx1 + HALO_SLOT / 4;
-    const float *sHx = reinterpret_cast<const float *>(st0 + H_OFF_H);
-    const float *sHy = sHx + BX * BY;
-    const float *sHz = sHy + BX * BY;
-    const int pz = PML ? slab_h(k, K, p) : -1;
+  int q = 0;
+  for (;;) {
+    int s = q % NSH;
+    if (!mbar_wait(&full[s], (uint32_t)((q / NSH) & 1))) {
+      if (d.err) atomicExch(d.err, 2);
+      return;
+    }
+    const int4 m = meta[s];
+    if (m.x < 0) return;  // sentinel
+    int x0, y0, kb, np;
+    decode_item(it, m.x, x0, y0, kb, np);
+    const int i = x0 + xo;
+    const int px = PML ? slab_h(i, I, p) : -1;
+    const bool x_special = px >= 0 || (mode && (i == d.i0 - 1 || i == d.i1));
+    bool valid[2], col_special[2];
+    int py[2];
+    int64_t n0[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-      const int xo = lane + 32 * c;
-      const int i = x0 + xo;
-      if (i < I - 1 && j < J - 1 && !timeout) {
+      const int j = y0 + r0 + 4 * c;
+      valid[c] = i < I - 1 && j < J - 1;
+      py[c] = PML ? slab_h(j, J, p) : -1;
+      col_special[c] = x_special || py[c] >= 0 || (mode && (j == d.j0 - 1 || j == d.j1));
+      n0[c] = valid[c] ? i + (int64_t)j * d.Ip + (int64_t)kb * d.plane : 0;
+    }
+    int prev = s;
+    ++q;
+    for (int t = 0; t < np; ++t, ++q) {
+      s = q % NSH;
+      if (!mbar_wait(&full[s], (uint32_t)((q / NSH) & 1))) {
+        if (d.err) atomicExch(d.err, 2);
+        return;
+      }
+      const int k = kb + t;
+      const unsigned char *st0 = smem + prev * H_STAGE;
+      const unsigned char *st1 = smem + s * H_STAGE;
+      const float *sEx = reinterpret_cast<const float *>(st0);
+      const float *sEy = sEx + HALO_SLOT / 4;
+      const float *sEz = sEy + HALO_SLOT / 4;
+      const float *sEx1 = reinterpret_cast<const float *>(st1);
+      const float *sEy1 = sEx1 + HALO_SLOT / 4;
+      const float *sHx = reinterpret_cast<const float *>(st0 + H_OFF_H);
+      const float *sHy = sHx + BX * BY;
+      const float *sHz = sHy + BX * BY;
+      const int pz = PML ? slab_h(k, K, p) : -1;
+      const bool plane_special = pz >= 0 || (mode && (k == d.k0 - 1 || k == d.k1));
+      const int64_t off = (int64_t)t * d.plane;
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int ty = r0 + 4 * c;
+        const bool act = valid[c];
         const int eb = ty * HW + xo;  // own cell in the halo tile
         const int hb = ty * BX + xo;  // own cell in the plain tile
         const float ex = sEx[eb], ey = sEy[eb], ez = sEz[eb];
+        const float dEz_y = sEz[eb + HW] - ez, dEx_y = sEx[eb + HW] - ex;
+        const float dEz_x = sEz[eb + 1] - ez, dEy_x = sEy[eb + 1] - ey;
+        const float dEy_z = sEy1[eb] - ey, dEx_z = sEx1[eb] - ex;
         float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
-        const int px = PML ? slab_h(i, I, p) : -1;
-        update_h_cell<true, PML>(d, mode, inc, i, j, k, px, py, pz, hx, hy, hz,
-                                 sEz[eb + HW] - ez, sEx[eb + HW] - ex, sEz[eb + 1] - ez,
-                                 sEy[eb + 1] - ey, sEy1[eb] - ey, sEx1[eb] - ex);
-        const int64_t n = i + (int64_t)j * d.Ip + (int64_t)k * d.plane;
-        d.f[3][n] = hx;
-        d.f[4][n] = hy;
-        d.f[5][n] = hz;
+        if (__any_sync(0xffffffffu, act && (col_special[c] || plane_special))) {
+          if (act)
+            update_h_cell<true, PML>(d, mode, inc, i, y0 + ty, k, px, py[c], pz, hx, hy, hz,
+                                     dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z);
+        } else {
+          hx = Chh * hx + Che * (-dEz_y + dEy_z);
+          hy = Chh * hy + Che * (-dEx_z + dEz_x);
+          hz = Chh * hz + Che * (-dEy_x + dEx_y);
+        }
+        if (act) {
+          d.f[3][n0[c] + off] = hx;
+          d.f[4][n0[c] + off] = hy;
+          d.f[5][n0[c] + off] = hz;
+        }
       }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[prev]);
+      prev = s;
     }
-    if (__syncthreads_or(timeout)) {
-      if (tid == 0) drain_and_flag(bars, t, issued, d.err, 2);
-      return;
-    }
-    if (tid == 0 && issued < nl) issue(issued++);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[prev]);  // the item's extra plane
   }
 }
 
-// z-chunk height: ~4 resident waves of 3 blocks per SM on 152 SMs.
-inline int pick_zchunk(int bx, int by, int nk) {
+// Item height: >= 4 items per resident block (dynamic balance), <= 32 planes.
+inline int pick_zchunk(int tiles, int nk, int blocks) {
   static int forced = -1;
   if (forced < 0) {
     const char *e = getenv("FDTD_TMA_ZCHUNK");
     forced = e ? atoi(e) : 0;
   }
   if (forced > 0) return forced;
-  const long long xy = (long long)bx * by;
-  const long long want = 152LL * 3 * 4;
-  long long chunks = (want + xy - 1) / xy;
+  const long long want = 4LL * blocks;
+  long long chunks = (want + tiles - 1) / tiles;
   if (chunks < 1) chunks = 1;
   if (chunks > nk) chunks = nk;
   int z = (int)((nk + chunks - 1) / chunks);
-  if (z < 4) z = 4;
-  if (z > 64) z = 64;
+  if (z < 2) z = 2;
+  if (z > 32) z = 32;
   return z;
 }
 
 template <class KH>
-int launch(KH kern, int smem, const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op,
-           cudaStream_t s, int ni, int nj, int nk) {
+int launch(KH kern, int smem, int *cached_blocks, const fdtd_dev *d, const fdtd_maps *m,
+           const fdtd_op *op, cudaStream_t s, int ni, int nj, int nk) {
   static_assert(sizeof(Maps) == sizeof(((fdtd_maps *)0)->bytes), "map layout");
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return (int)e;
+  if (!d->work) return (int)cudaErrorInvalidValue;
+  if (*cached_blocks <= 0) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return (int)e;
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    if (e != cudaSuccess) return (int)e;
+    *cached_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  }
   Maps mp;
   memcpy(&mp, m->bytes, sizeof(Maps));
-  const int bx = (ni + BX - 1) / BX, by = (nj + BY - 1) / BY;
-  const int zc = pick_zchunk(bx, by, nk);
-  dim3 grid(bx, by, (nk + zc - 1) / zc);
-  kern<<<grid, NT, smem, s>>>(*d, *op, mp, zc);
+  Items it;
+  it.tiles_x = (ni + BX - 1) / BX;
+  it.tiles_y = (nj + BY - 1) / BY;
+  it.nk = nk;
+  it.zchunk = pick_zchunk(it.tiles_x * it.tiles_y, nk, *cached_blocks);
+  it.n_items = it.tiles_x * it.tiles_y * ((nk + it.zchunk - 1) / it.zchunk);
+  const int blocks = it.n_items < *cached_blocks ? it.n_items : *cached_blocks;
+  kern<<<blocks, NT, smem, s>>>(*d, *op, mp, it);
   fdtdk_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -366,6 +538,8 @@ int encode(CUtensorMap *out, void *base, CUtensorMapDataType dt, int esize, cons
   return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
 }
 
+int g_blocks_e[2] = {0, 0}, g_blocks_h[2] = {0, 0};
+
 }  // namespace
 
 extern "C" {
@@ -395,13 +569,17 @@ int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) {
 }
 
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
-  if (op->pml) return launch(k_half_e_tma<true>, E_SMEM, d, m, op, s, d->I, d->J, d->K);
-  return launch(k_half_e_tma<false>, E_SMEM, d, m, op, s, d->I, d->J, d->K);
+  if (op->pml)
+    return launch(k_half_e_tma<true>, E_SMEM, &g_blocks_e[1], d, m, op, s, d->I, d->J, d->K);
+  return launch(k_half_e_tma<false>, E_SMEM, &g_blocks_e[0], d, m, op, s, d->I, d->J, d->K);
 }
 
 int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
-  if (op->pml) return launch(k_half_h_tma<true>, H_SMEM, d, m, op, s, d->I - 1, d->J - 1, d->K - 1);
-  return launch(k_half_h_tma<false>, H_SMEM, d, m, op, s, d->I - 1, d->J - 1, d->K - 1);
+  if (op->pml)
+    return launch(k_half_h_tma<true>, H_SMEM, &g_blocks_h[1], d, m, op, s, d->I - 1, d->J - 1,
+                  d->K - 1);
+  return launch(k_half_h_tma<false>, H_SMEM, &g_blocks_h[0], d, m, op, s, d->I - 1, d->J - 1,
+                d->K - 1);
 }
 
 }  // extern "C"
