@@ -180,8 +180,10 @@ typedef struct {
 } fdtd_info;
 int fdtd_get_info(fdtd_handle h, fdtd_info *out);
 
-/* Copies one of the CPML tables (0 b_E, 1 c_E, 2 b_H, 3 c_H: 2*pml floats)
- * or the x-only stretch denominators (4 den_ex, 5 den_hx: Imax floats). */
+/* Copies one of the CPML tables (0 b_E, 1 c_E, 2 b_H, 3 c_H: 2*pml floats),
+ * the x-only stretch denominators (4 den_ex, 5 den_hx: Imax floats), or
+ * the material-indexed coefficient table (6: num_materials x 6 floats,
+ * Cexe Ceye Ceze Cexh Ceyh Cezh per id; coef_mode 1 only). */
 int fdtd_get_table(fdtd_handle h, int32_t which, float *out, size_t n);
 
 /* Timing on the handle's stream (CUDA events).  slot 0..15. */
@@ -198,6 +200,32 @@ int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t tfsf
 /* Selects the CUDA device used by handles created afterwards on the calling
  * thread (one process per GPU: pass the local rank). */
 int fdtd_set_device(int32_t device);
+
+/* Allocation-free coefficient indexing.  No counterpart in the reference:
+ * it serves callers that cannot allocate device memory -- hosts whose
+ * device memory all comes from their own pool or a fixed budget, and loops
+ * that must not stall other streams with the device-wide synchronisation
+ * cudaMalloc / cudaFree imply.
+ *
+ * Replaces six per-cell E-coefficient arrays (ce[0..5] = Cexe Ceye Ceze
+ * Cexh Ceyh Cezh, device pointers, cell (i,j,k) at i + j*pitch +
+ * k*pitch*J) by a 2-byte id per cell (ids, device, pitch*J*K entries) and
+ * a table of the distinct tuples (table, device, max_ids*6 floats, row id =
+ * the six coefficients); *n_ids (host) receives the number of ids.  The
+ * result is the one ReadySimulation builds internally (fdtd_get_table 6).
+ *
+ * Allocates nothing: the hash-table scratch is a file-scope device array of
+ * 1.25 MiB that every GPU loading the library holds until the process
+ * exits.  Limit: max_ids <= 32768; larger values are rejected with
+ * FDTD_ERR_INVALID_ARG, and inputs with more distinct tuples than max_ids
+ * fail with FDTD_ERR_UNSUPPORTED.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * All calls share the one array, so calls that overlap on the GPU (on
+ * different streams or host threads) race; serialise them.  stream is a
+ * cudaStream_t (NULL: the legacy default stream); the call waits for it. */
+int fdtd_index_coefficients_static(const float *const ce[6], int32_t I, int32_t J, int32_t K,
+                                   int32_t pitch, uint16_t *ids, float *table, int32_t max_ids,
+                                   int32_t *n_ids, void *stream);
 
 /* Number of kernels this library has launched (all handles). */
 uint64_t fdtd_launch_count(void);

@@ -74,6 +74,8 @@ SIGNATURES = {
     "fdtd_profile_steps": (ctypes.c_int, [U64, I32, I32, I32, ctypes.POINTER(FdtdCurrent),
                                           ctypes.POINTER(ctypes.c_float * 3)]),
     "fdtd_set_device": (ctypes.c_int, [I32]),
+    "fdtd_index_coefficients_static": (ctypes.c_int, [ctypes.POINTER(P), I32, I32, I32, I32, P,
+                                                      P, I32, ctypes.POINTER(I32), P]),
     "fdtd_launch_count": (ctypes.c_uint64, []),
     "fdtd_last_error": (ctypes.c_char_p, []),
     "fdtd_create_signal": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double,

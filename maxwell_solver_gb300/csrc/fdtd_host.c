@@ -53,6 +53,10 @@ static int fail(int code, const char *fmt, ...) {
 
 const char *fdtd_last_error(void) { return g_err; }
 
+/* Sets the thread's error message for entry points implemented in the
+ * CUDA files (fdtd_internal.h). */
+int fdtd_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
+
 #define CU(call)                                                           \
   do {                                                                     \
     cudaError_t e_ = (call);                                               \
@@ -1163,6 +1167,16 @@ int fdtd_get_info(fdtd_handle h, fdtd_info *o) {
 int fdtd_get_table(fdtd_handle h, int32_t which, float *out, size_t n) {
   GET(h);
   if (!s->init_ready) return fail(FDTD_ERR_STATE, "tables exist after ReadySimulation");
+  if (which == 6) { /* material-indexed coefficient table: num_materials x 6 */
+    if (s->coef_mode != 1) return fail(FDTD_ERR_STATE, "coefficients are not material-indexed");
+    const size_t cnt = (size_t)s->num_mat * 6;
+    if (!out || n < cnt) return fail(FDTD_ERR_INVALID_ARG, "table needs %zu values", cnt);
+    int rc = flush(s);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(out, s->d_tab, cnt * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CU(cudaStreamSynchronize(s->stream));
+    return FDTD_OK;
+  }
   const float *src = NULL;
   size_t cnt = 0;
   switch (which) {

@@ -120,6 +120,9 @@ int fdtdk_compute_mu(float *out, const float *mu, const float *den_hx,
                      int64_t IJK, int32_t I, float delT, float sigma_m,
                      cudaStream_t s);
 unsigned long long fdtdk_launch_count(void);
+/* Records an error message for the calling thread (fdtd_last_error) and
+ * returns code. */
+int fdtd_internal_fail(int code, const char *msg);
 
 #ifdef __cplusplus
 }

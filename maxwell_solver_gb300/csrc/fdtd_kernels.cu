@@ -554,3 +554,116 @@ void fdtdk_count_launches(unsigned long long n) { g_launches += n; }
 unsigned long long fdtdk_launch_count(void) { return g_launches; }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Allocation-free coefficient indexing.
+//
+// Some callers cannot call cudaMalloc: hosts that own all device memory
+// through their own pool or a fixed budget (an embedding application's
+// allocator, a serving loop that admits work against an exact HBM budget)
+// and loops that must not stall other streams with the device-wide
+// synchronisation cudaMalloc/cudaFree imply.  fdtd_index_coefficients_static
+// serves them: the same indexing kernels as ReadySimulation's, with their
+// hash-table scratch in the file-scope array below instead of allocated
+// memory.  Every GPU that loads the library holds this array (1.25 MiB)
+// until the process exits.
+// ------------------------------------------------------------------------
+
+#include <mutex>
+
+namespace {
+
+constexpr int kStaticHashCap = 65536;   // slots (fixed: ids ride in a u16)
+constexpr int kStaticMaxIds = 32768;    // largest max_ids accepted
+constexpr size_t kStaticKeysOff = 0;
+constexpr size_t kStaticRepOff = kStaticKeysOff + kStaticHashCap * sizeof(unsigned long long);
+constexpr size_t kStaticIdsOff = kStaticRepOff + kStaticHashCap * sizeof(int64_t);
+constexpr size_t kStaticCntOff = kStaticIdsOff + kStaticHashCap * sizeof(int32_t);
+constexpr size_t kStaticScratchBytes = kStaticCntOff + 256;
+
+static __device__ __align__(256) unsigned char g_index_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_lock;
+unsigned char *g_static_ptr[kMaxDevices];  // device address of g_index_scratch, per device
+
+// Device address of the scratch array for the current device.  The first
+// call on a device looks it up (cudaGetSymbolAddress), so that first call
+// should come before any stream capture on that device.
+int static_scratch(unsigned char **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  if (dev < 0 || dev >= kMaxDevices) return (int)cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> guard(g_static_lock);
+  if (!g_static_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_index_scratch);
+    if (e != cudaSuccess) return (int)e;
+    g_static_ptr[dev] = static_cast<unsigned char *>(p);
+  }
+  *out = g_static_ptr[dev];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int fdtd_index_coefficients_static(const float *const ce[6], int32_t I, int32_t J,
+                                              int32_t K, int32_t pitch, uint16_t *ids,
+                                              float *table, int32_t max_ids, int32_t *n_ids,
+                                              void *stream) {
+  if (n_ids) *n_ids = 0;
+  if (!ce || !ids || !table || !n_ids)
+    return fdtd_internal_fail(2, "fdtd_index_coefficients_static: null pointer argument");
+  for (int a = 0; a < 6; ++a)
+    if (!ce[a]) return fdtd_internal_fail(2, "fdtd_index_coefficients_static: null ce array");
+  if (I < 1 || J < 1 || K < 1 || pitch < I)
+    return fdtd_internal_fail(2, "fdtd_index_coefficients_static: need I, J, K >= 1 and "
+                                 "pitch >= I");
+  if (max_ids < 1 || max_ids > kStaticMaxIds)
+    return fdtd_internal_fail(2, "fdtd_index_coefficients_static: max_ids must be in "
+                                 "[1, 32768], the capacity of the static scratch table");
+  unsigned char *base = nullptr;
+  int e = static_scratch(&base);
+  if (e) return fdtd_internal_fail(5, cudaGetErrorString((cudaError_t)e));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned long long *keys = reinterpret_cast<unsigned long long *>(base + kStaticKeysOff);
+  int64_t *rep = reinterpret_cast<int64_t *>(base + kStaticRepOff);
+  int32_t *sid = reinterpret_cast<int32_t *>(base + kStaticIdsOff);
+  int32_t *cnt = reinterpret_cast<int32_t *>(base + kStaticCntOff);
+
+  fdtd_dev d;
+  memset(&d, 0, sizeof(d));
+  d.I = I;
+  d.J = J;
+  d.K = K;
+  d.Ip = pitch;
+  d.plane = (int64_t)pitch * J;
+  d.cells = d.plane * K;
+  // the array keeps the previous call's contents: clear what starts at zero
+  cudaError_t ce_ = cudaMemsetAsync(keys, 0, kStaticHashCap * sizeof(unsigned long long), s);
+  if (ce_ == cudaSuccess) ce_ = cudaMemsetAsync(sid, 0xFF, kStaticHashCap * sizeof(int32_t), s);
+  if (ce_ == cudaSuccess) ce_ = cudaMemsetAsync(cnt, 0, 4 * sizeof(int32_t), s);
+  if (ce_ != cudaSuccess) return fdtd_internal_fail(5, cudaGetErrorString(ce_));
+  k_hash_insert<<<152 * 8, 256, 0, s>>>(d, ce[0], ce[1], ce[2], ce[3], ce[4], ce[5], ids, keys,
+                                         rep, kStaticHashCap, max_ids, cnt);
+  k_hash_compact<<<1, 1024, 0, s>>>(ce[0], ce[1], ce[2], ce[3], ce[4], ce[5], keys, rep, sid,
+                                     kStaticHashCap, table, max_ids, cnt);
+  k_hash_remap<<<152 * 8, 256, 0, s>>>(d, ce[0], ce[1], ce[2], ce[3], ce[4], ce[5], ids, sid,
+                                        table, max_ids, cnt);
+  g_launches += 3;
+  int32_t h_cnt[4] = {0, 0, 0, 0};
+  ce_ = cudaGetLastError();
+  if (ce_ == cudaSuccess)
+    ce_ = cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, s);
+  if (ce_ == cudaSuccess) ce_ = cudaStreamSynchronize(s);
+  if (ce_ != cudaSuccess) return fdtd_internal_fail(5, cudaGetErrorString(ce_));
+  if (h_cnt[1] || h_cnt[0] > max_ids)
+    return fdtd_internal_fail(7, "fdtd_index_coefficients_static: more distinct coefficient "
+                                 "tuples than max_ids");
+  if (h_cnt[2])
+    return fdtd_internal_fail(7, "fdtd_index_coefficients_static: hash collision between "
+                                 "distinct coefficient tuples");
+  *n_ids = h_cnt[0];
+  return 0;
+}

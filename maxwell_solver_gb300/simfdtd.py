@@ -205,9 +205,9 @@ def info(P) -> dict:
 
 def get_table(P, which: str) -> np.ndarray:
     lib = _native.load()
-    idx = ("b_E", "c_E", "b_H", "c_H", "den_ex", "den_hx").index(which)
+    idx = ("b_E", "c_E", "b_H", "c_H", "den_ex", "den_hx", "materials").index(which)
     inf = info(P)
-    n = 2 * inf["pml"] if idx < 4 else inf["I"]
+    n = 2 * inf["pml"] if idx < 4 else (inf["I"] if idx < 6 else 6 * inf["num_materials"])
     out = np.zeros(n, dtype=np.float32)
     _check(lib.fdtd_get_table(_handle(P), idx, _ptr(out), n))
     return out
