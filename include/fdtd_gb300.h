@@ -177,6 +177,8 @@ typedef struct {
   int32_t num_materials;   /* distinct coefficient tuples (coef_mode 1) */
   uint64_t device_bytes;   /* device memory held by the handle */
   float Chh, Che;
+  int32_t zchunk_h, zchunk_e; /* z-planes per work item of the TMA half-steps
+                                 (autotuned; 0 = built-in heuristic) */
 } fdtd_info;
 int fdtd_get_info(fdtd_handle h, fdtd_info *out);
 

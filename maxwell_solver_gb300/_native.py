@@ -36,7 +36,8 @@ class FdtdInfo(ctypes.Structure):
                 ("pml", I32), ("size_1d", I32), ("i0", I32), ("i1", I32), ("j0", I32),
                 ("j1", I32), ("k0", I32), ("k1", I32), ("coef_mode", I32),
                 ("num_materials", I32), ("device_bytes", ctypes.c_uint64),
-                ("Chh", ctypes.c_float), ("Che", ctypes.c_float)]
+                ("Chh", ctypes.c_float), ("Che", ctypes.c_float),
+                ("zchunk_h", I32), ("zchunk_e", I32)]
 
 
 # name -> (restype, argtypes)

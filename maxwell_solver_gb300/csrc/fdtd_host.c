@@ -22,6 +22,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/stat.h>
 
 #include <cuda_runtime_api.h>
 
@@ -116,6 +117,7 @@ typedef struct sim {
   int32_t coef_mode, num_mat;
   int use_tma, allow_compress;
   fdtd_maps maps;
+  int32_t zc_h, zc_e; /* tuned z-planes per TMA work item (0: heuristic) */
   uint64_t device_bytes;
   fdtd_dev dev;
   pending_t pend;
@@ -345,6 +347,7 @@ int fdtd_set_source(fdtd_handle h, const float *src, size_t n) {
 }
 
 static int flush(sim *s);
+static int issue(sim *s, int hfam, const fdtd_op *op);
 
 /* src/simulation.h:1084-1095 */
 int fdtd_update_source(fdtd_handle h, const float *src, size_t n) {
@@ -492,6 +495,8 @@ static void fill_dev_struct(sim *s) {
   d->mat_tab = s->d_tab;
   d->n_mat = s->num_mat;
   d->err = s->d_err;
+  d->zc_h = s->zc_h;
+  d->zc_e = s->zc_e;
   for (int a = 0; a < FDTD_NUM_PSI; ++a) d->psi[a] = s->d_psi[a];
   for (int a = 0; a < 4; ++a) d->inc[a] = s->d_inc[a];
   d->src = s->d_src;
@@ -548,6 +553,142 @@ static int zero_state(sim *s) {
   const size_t psi_total = (size_t)(4 * 2 * (s->size_x + s->size_y + s->size_z)) * sizeof(float);
   CU(cudaMemsetAsync(s->d_psi_pool, 0, psi_total, s->stream));
   CU(cudaMemsetAsync(s->d_ctr, 0, 4 * sizeof(int32_t), s->stream));
+  return FDTD_OK;
+}
+
+/* ------------------------------------------------------------ autotune
+ *
+ * The TMA half-steps split the grid into work items of one tile and a run of
+ * z-planes; the best run length depends on the grid (how many items keep
+ * the GPU busy, how wide a band of planes the blocks sweep together).  It is
+ * measured once per grid shape, at the end of ReadySimulation, while every
+ * field and psi value is still exactly zero: a source-free step maps zero to
+ * zero exactly, so the trial steps leave the state bit-identical and need no
+ * snapshot.  Results are kept per process and in a text file
+ * (FDTD_TUNE_CACHE, default $HOME/.cache/fdtd_gb300/autotune.txt);
+ * FDTD_AUTOTUNE=0 disables it. */
+
+#define TUNE_MAX 128
+typedef struct {
+  int32_t I, J, K, p, coef_mode, zh, ze;
+} tune_entry;
+static tune_entry g_tune[TUNE_MAX];
+static int g_tune_n = 0, g_tune_loaded = 0;
+static pthread_mutex_t g_tune_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static void tune_cache_path(char *buf, size_t n) {
+  const char *e = getenv("FDTD_TUNE_CACHE");
+  const char *home = getenv("HOME");
+  if (e) snprintf(buf, n, "%s", e);
+  else if (home) snprintf(buf, n, "%s/.cache/fdtd_gb300/autotune.txt", home);
+  else buf[0] = '\0';
+}
+
+static void tune_load(void) {
+  if (g_tune_loaded) return;
+  g_tune_loaded = 1;
+  char path[512];
+  tune_cache_path(path, sizeof(path));
+  if (!path[0]) return;
+  FILE *f = fopen(path, "r");
+  if (!f) return;
+  tune_entry t;
+  while (g_tune_n < TUNE_MAX && fscanf(f, "%d %d %d %d %d %d %d", &t.I, &t.J, &t.K, &t.p,
+                                       &t.coef_mode, &t.zh, &t.ze) == 7)
+    g_tune[g_tune_n++] = t;
+  fclose(f);
+}
+
+static void tune_store(const tune_entry *t) {
+  if (g_tune_n < TUNE_MAX) g_tune[g_tune_n++] = *t;
+  char path[512];
+  tune_cache_path(path, sizeof(path));
+  if (!path[0]) return;
+  char dir[512];
+  snprintf(dir, sizeof(dir), "%s", path);
+  char *slash = strrchr(dir, '/');
+  if (slash) { /* best effort: create the two last directory levels */
+    *slash = '\0';
+    char *up = strrchr(dir, '/');
+    if (up) {
+      *up = '\0';
+      mkdir(dir, 0755);
+      *up = '/';
+    }
+    mkdir(dir, 0755);
+  }
+  FILE *f = fopen(path, "a");
+  if (!f) return;
+  fprintf(f, "%d %d %d %d %d %d %d\n", t->I, t->J, t->K, t->p, t->coef_mode, t->zh, t->ze);
+  fclose(f);
+}
+
+/* Mean device time of the H and E half-steps over `steps` source-free steps
+ * with z-run length z (after one untimed step). */
+static int tune_measure(sim *s, int z, int steps, float *th, float *te) {
+  fdtd_op op;
+  memset(&op, 0, sizeof(op));
+  op.curl = 1;
+  op.pml = 1;
+  s->dev.zc_h = s->dev.zc_e = z;
+  float sh = 0, se = 0;
+  for (int c = -1; c < steps; ++c) {
+    CU(cudaEventRecord(s->ev[12], s->stream));
+    int rc = issue(s, 1, &op);
+    if (rc) return rc;
+    CU(cudaEventRecord(s->ev[13], s->stream));
+    if ((rc = issue(s, 0, &op))) return rc;
+    CU(cudaEventRecord(s->ev[14], s->stream));
+    CU(cudaEventSynchronize(s->ev[14]));
+    float a = 0, b = 0;
+    CU(cudaEventElapsedTime(&a, s->ev[12], s->ev[13]));
+    CU(cudaEventElapsedTime(&b, s->ev[13], s->ev[14]));
+    if (c >= 0) {
+      sh += a;
+      se += b;
+    }
+  }
+  *th = sh / steps;
+  *te = se / steps;
+  return FDTD_OK;
+}
+
+static int autotune_zero_state(sim *s) {
+  const char *e = getenv("FDTD_AUTOTUNE");
+  if ((e && strcmp(e, "0") == 0) || !s->use_tma || !s->maps.valid) return FDTD_OK;
+  if (s->cells < (int64_t)1 << 21) return FDTD_OK; /* small grids: heuristic */
+  pthread_mutex_lock(&g_tune_lock);
+  tune_load();
+  for (int i = 0; i < g_tune_n; ++i) {
+    const tune_entry *t = &g_tune[i];
+    if (t->I == s->I && t->J == s->J && t->K == s->K && t->p == s->p &&
+        t->coef_mode == s->coef_mode) {
+      s->zc_h = t->zh;
+      s->zc_e = t->ze;
+      pthread_mutex_unlock(&g_tune_lock);
+      fill_dev_struct(s);
+      return FDTD_OK;
+    }
+  }
+  pthread_mutex_unlock(&g_tune_lock);
+  static const int cand[] = {2, 4, 8, 16, 32};
+  float best_h = 1e30f, best_e = 1e30f;
+  int zh = 0, ze = 0;
+  for (size_t c = 0; c < sizeof(cand) / sizeof(cand[0]); ++c) {
+    if (cand[c] > s->K) break;
+    float th = 0, te = 0;
+    int rc = tune_measure(s, cand[c], 3, &th, &te);
+    if (rc) return rc;
+    if (th < best_h) { best_h = th; zh = cand[c]; }
+    if (te < best_e) { best_e = te; ze = cand[c]; }
+  }
+  s->zc_h = zh;
+  s->zc_e = ze;
+  fill_dev_struct(s);
+  tune_entry t = {s->I, s->J, s->K, s->p, s->coef_mode, zh, ze};
+  pthread_mutex_lock(&g_tune_lock);
+  tune_store(&t);
+  pthread_mutex_unlock(&g_tune_lock);
   return FDTD_OK;
 }
 
@@ -650,6 +791,7 @@ int fdtd_ready_simulation(fdtd_handle h) {
     int e = fdtdk_make_maps(&s->dev, &s->maps);
     if (e) s->maps.valid = 0; /* the direct kernels take over */
   }
+  if ((rc = autotune_zero_state(s))) return rc;
   CU(cudaStreamSynchronize(s->stream));
   s->init_ready = 1;
   return FDTD_OK;
@@ -1161,6 +1303,8 @@ int fdtd_get_info(fdtd_handle h, fdtd_info *o) {
   o->device_bytes = s->device_bytes;
   o->Chh = s->Chh;
   o->Che = s->Che;
+  o->zchunk_h = s->zc_h;
+  o->zchunk_e = s->zc_e;
   return FDTD_OK;
 }
 

@@ -57,6 +57,7 @@ typedef struct {
   const int64_t *probe_idx; /* [num_ant] pitched cell index, -1 if outside */
   int32_t num_ant;
   int32_t *err;             /* device error word (bounded-wait timeouts) */
+  int32_t zc_h, zc_e;       /* z-planes per TMA work item (0: heuristic) */
 } fdtd_dev;
 
 /* TMA descriptors (CUtensorMap, 128 B each) of one grid: 0..5 = Ex Ey Ez Hx

@@ -484,7 +484,7 @@ inline int pick_zchunk(int tiles, int nk, int blocks) {
 
 template <class KH>
 int launch(KH kern, int smem, int *cached_blocks, const fdtd_dev *d, const fdtd_maps *m,
-           const fdtd_op *op, cudaStream_t s, int ni, int nj, int nk) {
+           const fdtd_op *op, cudaStream_t s, int ni, int nj, int nk, int zc_tuned) {
   static_assert(sizeof(Maps) == sizeof(((fdtd_maps *)0)->bytes), "map layout");
   if (!d->work) return (int)cudaErrorInvalidValue;
   if (*cached_blocks <= 0) {
@@ -504,6 +504,7 @@ int launch(KH kern, int smem, int *cached_blocks, const fdtd_dev *d, const fdtd_
   it.tiles_y = (nj + BY - 1) / BY;
   it.nk = nk;
   it.zchunk = pick_zchunk(it.tiles_x * it.tiles_y, nk, *cached_blocks);
+  if (zc_tuned > 0 && !getenv("FDTD_TMA_ZCHUNK")) it.zchunk = zc_tuned < nk ? zc_tuned : nk;
   it.n_items = it.tiles_x * it.tiles_y * ((nk + it.zchunk - 1) / it.zchunk);
   const int blocks = it.n_items < *cached_blocks ? it.n_items : *cached_blocks;
   kern<<<blocks, NT, smem, s>>>(*d, *op, mp, it);
@@ -570,16 +571,18 @@ int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) {
 
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
   if (op->pml)
-    return launch(k_half_e_tma<true>, E_SMEM, &g_blocks_e[1], d, m, op, s, d->I, d->J, d->K);
-  return launch(k_half_e_tma<false>, E_SMEM, &g_blocks_e[0], d, m, op, s, d->I, d->J, d->K);
+    return launch(k_half_e_tma<true>, E_SMEM, &g_blocks_e[1], d, m, op, s, d->I, d->J, d->K,
+                  d->zc_e);
+  return launch(k_half_e_tma<false>, E_SMEM, &g_blocks_e[0], d, m, op, s, d->I, d->J, d->K,
+                d->zc_e);
 }
 
 int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
   if (op->pml)
     return launch(k_half_h_tma<true>, H_SMEM, &g_blocks_h[1], d, m, op, s, d->I - 1, d->J - 1,
-                  d->K - 1);
+                  d->K - 1, d->zc_h);
   return launch(k_half_h_tma<false>, H_SMEM, &g_blocks_h[0], d, m, op, s, d->I - 1, d->J - 1,
-                d->K - 1);
+                d->K - 1, d->zc_h);
 }
 
 }  // extern "C"

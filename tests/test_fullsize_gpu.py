@@ -121,3 +121,32 @@ def test_tfsf_leakage_vacuum(mode):
     ratio = np.sqrt(e2[shell].mean() / inside.mean())
     assert inside.mean() > 0
     assert ratio < 1e-4, ratio
+
+
+def test_autotune_keeps_state_zero_and_results_exact(tmp_path, monkeypatch):
+    """ReadySimulation tunes the TMA work-item height on grids of >= 2M cells
+    by running source-free trial steps on the all-zero state: afterwards the
+    fields are still exactly zero, the choice is cached on disk, and a run
+    with the tuned kernels matches the oracle bit for bit."""
+    from maxwell_solver_gb300 import info, simFDTD
+    from maxwell_solver_gb300.workloads import WORKLOADS, setup
+
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("FDTD_TUNE_CACHE", str(cache))
+    w = WORKLOADS["c2"]
+    T = 20
+    P = setup(simFDTD, w, steps=T)
+    inf = info(P)
+    assert inf["zchunk_h"] > 0 and inf["zchunk_e"] > 0
+    if cache.exists():  # absent when this process had tuned the shape already
+        assert cache.read_text().split()[:3] == ["256", "256", "256"]
+    for f in range(1, 7):
+        assert not simFDTD("OutputVis", P, np.uint32(w.cells), np.int32(f)).any()
+    simFDTD("StepN", P, np.int32([0, 4, w.mode]))
+    o = oracle_for(w, T)
+    for n in range(4):
+        o.step(n, w.mode)
+    for f, n in zip(range(1, 7), FIELDS):
+        np.testing.assert_array_equal(simFDTD("OutputVis", P, np.uint32(w.cells), np.int32(f)),
+                                      o.field(n), err_msg=n)
+    simFDTD("DeleteSimulation", P)
