@@ -203,6 +203,32 @@ int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t tfsf
  * thread (one process per GPU: pass the local rank). */
 int fdtd_set_device(int32_t device);
 
+/* ---------------------------------------------------------------------
+ * Batched execution (extension, no reference counterpart): many ready
+ * simulation handles of different sizes, materials and sources advance
+ * together, one H and one E launch per step for all of them (persistent
+ * TMA kernels over the work items of every member).  The arithmetic per
+ * cell is unchanged: each member ends bit-identical to running it alone.
+ * --------------------------------------------------------------------- */
+typedef uint64_t fdtd_batch;
+int fdtd_batch_create(fdtd_batch *out);
+int fdtd_batch_destroy(fdtd_batch b);
+/* Adds handle h to run steps first..first+count-1 (TF/SF mode 0..4, current
+ * source cur or NULL).  h must be ready and keeps its own state; calls on h
+ * issued after the batch finishes it see the batch's results. */
+int fdtd_batch_add(fdtd_batch b, fdtd_handle h, int32_t first, int32_t count,
+                   int32_t tfsf_mode, const fdtd_current *cur);
+/* Advances every active member by the same number of steps: the fewest
+ * remaining of any active member, at most max_steps.  *active_left (may be
+ * NULL) receives the number of members still running. */
+int fdtd_batch_step(fdtd_batch b, int32_t max_steps, int32_t *active_left);
+/* Runs every member to its last step and waits. */
+int fdtd_batch_run(fdtd_batch b);
+/* Drops all members. */
+int fdtd_batch_clear(fdtd_batch b);
+/* Steps member h has completed (-1 when h is not a member). */
+int fdtd_batch_progress(fdtd_batch b, fdtd_handle h, int32_t *done);
+
 /* Allocation-free coefficient indexing.  No counterpart in the reference:
  * it serves callers that cannot allocate device memory -- hosts whose
  * device memory all comes from their own pool or a fixed budget, and loops

@@ -77,6 +77,13 @@ SIGNATURES = {
     "fdtd_set_device": (ctypes.c_int, [I32]),
     "fdtd_index_coefficients_static": (ctypes.c_int, [ctypes.POINTER(P), I32, I32, I32, I32, P,
                                                       P, I32, ctypes.POINTER(I32), P]),
+    "fdtd_batch_create": (ctypes.c_int, [ctypes.POINTER(U64)]),
+    "fdtd_batch_destroy": (ctypes.c_int, [U64]),
+    "fdtd_batch_add": (ctypes.c_int, [U64, U64, I32, I32, I32, ctypes.POINTER(FdtdCurrent)]),
+    "fdtd_batch_step": (ctypes.c_int, [U64, I32, ctypes.POINTER(I32)]),
+    "fdtd_batch_run": (ctypes.c_int, [U64]),
+    "fdtd_batch_clear": (ctypes.c_int, [U64]),
+    "fdtd_batch_progress": (ctypes.c_int, [U64, U64, ctypes.POINTER(I32)]),
     "fdtd_launch_count": (ctypes.c_uint64, []),
     "fdtd_last_error": (ctypes.c_char_p, []),
     "fdtd_create_signal": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double,

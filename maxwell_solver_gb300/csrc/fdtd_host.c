@@ -1376,3 +1376,418 @@ int fdtd_create_signal(double fctr, double delT, double percentage_bw, double nu
   }
   return FDTD_OK;
 }
+
+/* ==================================================================== batch
+ *
+ * A batch advances many simulation handles of different sizes together:
+ * every batched step is one H and one E launch of the persistent TMA kernels
+ * over the work items of all active members (plus a probe gather and a step
+ * counter update), so small grids fill the GPU together instead of each
+ * leaving most of it idle.  The per-cell arithmetic is the single-grid
+ * kernels', so every member ends bit-identical to running it alone.
+ */
+
+#define MAX_BATCHES 256
+#define BATCH_ZRUN 8
+
+typedef struct {
+  fdtd_handle h;
+  int32_t first, count, done, mode, has_cur;
+  fdtd_current cur;
+} bmember;
+
+typedef struct batch {
+  bmember *m;
+  int n, cap;
+  cudaStream_t stream;
+  cudaEvent_t ev;
+  /* device mirrors of the active members, rebuilt when the set changes */
+  fdtd_dev *d_devs;
+  unsigned char *d_maps;
+  fdtd_op *d_ops;
+  int32_t *d_steps, *d_tab_h, *d_tab_e, *d_work, *d_err;
+  int dev_cap, cap_h, cap_e;
+  /* host staging */
+  fdtd_dev *h_devs;
+  unsigned char *h_maps;
+  fdtd_op *h_ops;
+  int32_t *h_steps, *h_tab_h, *h_tab_e;
+  int *act;  /* member index of each active slot */
+  int n_act, n_h, n_e, any_probes, dirty;
+} batch;
+
+static batch *g_batches[MAX_BATCHES];
+static uint32_t g_bgen[MAX_BATCHES];
+
+static batch *blookup(fdtd_batch b) {
+  uint32_t slot = (uint32_t)(b & 0xffffffffu), gen = (uint32_t)(b >> 32);
+  if (slot == 0 || slot > MAX_BATCHES) return NULL;
+  pthread_mutex_lock(&g_reg_lock);
+  batch *p = g_bgen[slot - 1] == gen ? g_batches[slot - 1] : NULL;
+  pthread_mutex_unlock(&g_reg_lock);
+  return p;
+}
+
+int fdtd_batch_create(fdtd_batch *out) {
+  if (!out) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  batch *b = (batch *)calloc(1, sizeof(batch));
+  if (!b) return fail(FDTD_ERR_OOM, "out of host memory");
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_work, 4 * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_err, sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_work, 0, 4 * sizeof(int32_t), b->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), b->stream);
+  if (e != cudaSuccess) {
+    free(b);
+    return fail(FDTD_ERR_CUDA, "batch create: %s", cudaGetErrorString(e));
+  }
+  pthread_mutex_lock(&g_reg_lock);
+  int slot = -1;
+  for (int i = 0; i < MAX_BATCHES; ++i)
+    if (!g_batches[i]) {
+      slot = i;
+      break;
+    }
+  if (slot < 0) {
+    pthread_mutex_unlock(&g_reg_lock);
+    cudaFree(b->d_work);
+    cudaFree(b->d_err);
+    cudaStreamDestroy(b->stream);
+    free(b);
+    return fail(FDTD_ERR_OOM, "too many batches");
+  }
+  g_batches[slot] = b;
+  g_bgen[slot] += 1;
+  *out = ((uint64_t)g_bgen[slot] << 32) | (uint64_t)(slot + 1);
+  pthread_mutex_unlock(&g_reg_lock);
+  return FDTD_OK;
+}
+
+static void batch_free_mirrors(batch *b) {
+  dfree(b->d_devs);
+  dfree(b->d_maps);
+  dfree(b->d_ops);
+  dfree(b->d_steps);
+  dfree(b->d_tab_h);
+  dfree(b->d_tab_e);
+  b->d_devs = NULL;
+  b->d_maps = NULL;
+  b->d_ops = NULL;
+  b->d_steps = b->d_tab_h = b->d_tab_e = NULL;
+  free(b->h_devs);
+  free(b->h_maps);
+  free(b->h_ops);
+  free(b->h_steps);
+  free(b->h_tab_h);
+  free(b->h_tab_e);
+  free(b->act);
+  b->h_devs = NULL;
+  b->h_maps = NULL;
+  b->h_ops = NULL;
+  b->h_steps = b->h_tab_h = b->h_tab_e = NULL;
+  b->act = NULL;
+  b->dev_cap = b->cap_h = b->cap_e = 0;
+}
+
+int fdtd_batch_destroy(fdtd_batch h) {
+  uint32_t slot = (uint32_t)(h & 0xffffffffu);
+  batch *b = blookup(h);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  pthread_mutex_lock(&g_reg_lock);
+  g_batches[slot - 1] = NULL;
+  pthread_mutex_unlock(&g_reg_lock);
+  cudaStreamSynchronize(b->stream);
+  batch_free_mirrors(b);
+  dfree(b->d_work);
+  dfree(b->d_err);
+  cudaEventDestroy(b->ev);
+  cudaStreamDestroy(b->stream);
+  free(b->m);
+  free(b);
+  return FDTD_OK;
+}
+
+int fdtd_batch_add(fdtd_batch bh, fdtd_handle h, int32_t first, int32_t count, int32_t mode,
+                   const fdtd_current *cur) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  sim *s = lookup(h);
+  if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "invalid simulation handle");
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "batch members need ReadySimulation");
+  if (!s->maps.valid) return fail(FDTD_ERR_UNSUPPORTED, "batch members need the TMA kernels");
+  if (first < 0 || count < 0) return fail(FDTD_ERR_INVALID_ARG, "negative step range");
+  if (mode < 1 || mode > 4) mode = 0;
+  const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
+  if ((mode || use_cur) && (int64_t)first + count > s->T)
+    return fail(FDTD_ERR_INVALID_ARG, "steps [%d, %d) exceed T=%d", first, first + count, s->T);
+  if (mode) {
+    int rc = tfsf_check(s, first, mode);
+    if (rc) return rc;
+  }
+  if (use_cur && !s->init_src) return fail(FDTD_ERR_STATE, "current source requires SetSource");
+  for (int i = 0; i < b->n; ++i)
+    if (b->m[i].h == h && b->m[i].done < b->m[i].count)
+      return fail(FDTD_ERR_STATE, "handle is already an active member of this batch");
+  if (b->n == b->cap) {
+    int nc = b->cap ? 2 * b->cap : 64;
+    bmember *nm = (bmember *)realloc(b->m, (size_t)nc * sizeof(bmember));
+    if (!nm) return fail(FDTD_ERR_OOM, "out of host memory");
+    b->m = nm;
+    b->cap = nc;
+  }
+  bmember *m = &b->m[b->n++];
+  memset(m, 0, sizeof(*m));
+  m->h = h;
+  m->first = first;
+  m->count = count;
+  m->mode = mode;
+  m->has_cur = 0;
+  if (use_cur) {
+    int ok = 1;
+    for (int a = 0; a < 6; ++a) ok &= cur->box[a] >= 0;
+    ok &= cur->box[1] >= cur->box[0] && cur->box[3] >= cur->box[2] && cur->box[5] >= cur->box[4];
+    if (ok) {
+      m->has_cur = 1;
+      m->cur = *cur;
+    }
+  }
+  b->dirty = 1;
+  return FDTD_OK;
+}
+
+static int ensure_cap(void **d, void **hbuf, int *cap, int need, size_t elem) {
+  if (need <= *cap) return FDTD_OK;
+  int nc = *cap ? *cap : 256;
+  while (nc < need) nc *= 2;
+  if (*d) cudaFree(*d);
+  free(*hbuf);
+  *d = NULL;
+  *hbuf = malloc((size_t)nc * elem);
+  if (!*hbuf) return fail(FDTD_ERR_OOM, "out of host memory");
+  cudaError_t e = cudaMalloc(d, (size_t)nc * elem);
+  if (e != cudaSuccess) return fail(FDTD_ERR_OOM, "cudaMalloc: %s", cudaGetErrorString(e));
+  *cap = nc;
+  return FDTD_OK;
+}
+
+static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk) {
+  for (int kb = 0; kb < nk; kb += BATCH_ZRUN) {
+    const int np = nk - kb < BATCH_ZRUN ? nk - kb : BATCH_ZRUN;
+    for (int y0 = 0; y0 < nj; y0 += FDTD_TILE_Y)
+      for (int x0 = 0; x0 < ni; x0 += FDTD_TILE_X) {
+        int32_t *e = tab + 4 * (size_t)n;
+        e[0] = g;
+        e[1] = x0;
+        e[2] = y0;
+        e[3] = kb | (np << 16);
+        ++n;
+      }
+  }
+  return n;
+}
+
+static int count_items(int ni, int nj, int nk) {
+  return ((ni + FDTD_TILE_X - 1) / FDTD_TILE_X) * ((nj + FDTD_TILE_Y - 1) / FDTD_TILE_Y) *
+         ((nk + BATCH_ZRUN - 1) / BATCH_ZRUN);
+}
+
+/* Builds and uploads the device mirrors of the active members. */
+static int batch_rebuild(batch *b) {
+  int na = 0, nh = 0, ne = 0;
+  for (int i = 0; i < b->n; ++i) {
+    const bmember *m = &b->m[i];
+    if (m->done >= m->count) continue;
+    sim *s = lookup(m->h);
+    if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "a batch member was deleted");
+    ++na;
+    nh += count_items(s->I - 1, s->J - 1, s->K - 1);
+    ne += count_items(s->I, s->J, s->K);
+  }
+  int rc;
+  if (na > b->dev_cap) { /* per-member mirrors share one capacity */
+    int cap = b->dev_cap ? b->dev_cap : 64;
+    while (cap < na) cap *= 2;
+    int c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    dfree(b->d_devs);
+    dfree(b->d_maps);
+    dfree(b->d_ops);
+    dfree(b->d_steps);
+    b->d_devs = NULL;
+    b->d_maps = NULL;
+    b->d_ops = NULL;
+    b->d_steps = NULL;
+    free(b->act);
+    b->act = (int *)malloc((size_t)cap * sizeof(int));
+    if (!b->act) return fail(FDTD_ERR_OOM, "out of host memory");
+    if ((rc = ensure_cap((void **)&b->d_devs, (void **)&b->h_devs, &c0, cap, sizeof(fdtd_dev))))
+      return rc;
+    if ((rc = ensure_cap((void **)&b->d_maps, (void **)&b->h_maps, &c1, cap,
+                         sizeof(((fdtd_maps *)0)->bytes))))
+      return rc;
+    if ((rc = ensure_cap((void **)&b->d_ops, (void **)&b->h_ops, &c2, cap, sizeof(fdtd_op))))
+      return rc;
+    if ((rc = ensure_cap((void **)&b->d_steps, (void **)&b->h_steps, &c3, cap, sizeof(int32_t))))
+      return rc;
+    b->dev_cap = cap;
+  }
+  if ((rc = ensure_cap((void **)&b->d_tab_h, (void **)&b->h_tab_h, &b->cap_h, nh,
+                       4 * sizeof(int32_t))))
+    return rc;
+  if ((rc = ensure_cap((void **)&b->d_tab_e, (void **)&b->h_tab_e, &b->cap_e, ne,
+                       4 * sizeof(int32_t))))
+    return rc;
+  int g = 0;
+  nh = ne = 0;
+  b->any_probes = 0;
+  const size_t mapsz = sizeof(((fdtd_maps *)0)->bytes);
+  for (int i = 0; i < b->n; ++i) {
+    const bmember *m = &b->m[i];
+    if (m->done >= m->count) continue;
+    sim *s = lookup(m->h);
+    b->act[g] = i;
+    b->h_devs[g] = s->dev;
+    memcpy(b->h_maps + (size_t)g * mapsz, s->maps.bytes, mapsz);
+    fdtd_op *op = &b->h_ops[g];
+    memset(op, 0, sizeof(*op));
+    op->curl = 1;
+    op->pml = 1;
+    op->tfsf_mode = m->mode;
+    if (m->has_cur) {
+      op->cur_mode = m->cur.mode;
+      memcpy(op->cur_box, m->cur.box, sizeof(op->cur_box));
+    }
+    b->h_steps[g] = m->first + m->done;
+    if (s->dev.num_ant > 0) b->any_probes = 1;
+    nh = add_items(b->h_tab_h, nh, g, s->I - 1, s->J - 1, s->K - 1);
+    ne = add_items(b->h_tab_e, ne, g, s->I, s->J, s->K);
+    ++g;
+  }
+  b->n_act = na;
+  b->n_h = nh;
+  b->n_e = ne;
+  if (na) {
+    CU(cudaMemcpyAsync(b->d_devs, b->h_devs, (size_t)na * sizeof(fdtd_dev),
+                       cudaMemcpyHostToDevice, b->stream));
+    CU(cudaMemcpyAsync(b->d_maps, b->h_maps, (size_t)na * mapsz, cudaMemcpyHostToDevice,
+                       b->stream));
+    CU(cudaMemcpyAsync(b->d_ops, b->h_ops, (size_t)na * sizeof(fdtd_op), cudaMemcpyHostToDevice,
+                       b->stream));
+    CU(cudaMemcpyAsync(b->d_steps, b->h_steps, (size_t)na * sizeof(int32_t),
+                       cudaMemcpyHostToDevice, b->stream));
+    CU(cudaMemcpyAsync(b->d_tab_h, b->h_tab_h, (size_t)nh * 4 * sizeof(int32_t),
+                       cudaMemcpyHostToDevice, b->stream));
+    CU(cudaMemcpyAsync(b->d_tab_e, b->h_tab_e, (size_t)ne * 4 * sizeof(int32_t),
+                       cudaMemcpyHostToDevice, b->stream));
+    /* the staging buffers are reused by the next rebuild: wait for the copies */
+    CU(cudaStreamSynchronize(b->stream));
+  }
+  b->dirty = 0;
+  return FDTD_OK;
+}
+
+/* Advances every active member by up to max_steps steps (all by the same
+ * number: the fewest remaining steps of any active member, capped by
+ * max_steps).  *active_left receives the number of members still running. */
+int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  int rc;
+  int32_t left = 0;
+  for (int i = 0; i < b->n; ++i) left += b->m[i].done < b->m[i].count;
+  if (active_left) *active_left = left;
+  if (!left || max_steps <= 0) return FDTD_OK;
+  if (b->dirty) {
+    /* new members: their own queued work must be on the device first */
+    for (int i = 0; i < b->n; ++i) {
+      if (b->m[i].done >= b->m[i].count) continue;
+      sim *s = lookup(b->m[i].h);
+      if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "a batch member was deleted");
+      if ((rc = flush(s))) return rc;
+      CU(cudaEventRecord(s->ev[15], s->stream));
+      CU(cudaStreamWaitEvent(b->stream, s->ev[15], 0));
+    }
+    if ((rc = batch_rebuild(b))) return rc;
+  }
+  int32_t nsteps = max_steps;
+  for (int g = 0; g < b->n_act; ++g) {
+    const bmember *m = &b->m[b->act[g]];
+    if (m->count - m->done < nsteps) nsteps = m->count - m->done;
+  }
+  for (int32_t t = 0; t < nsteps; ++t) {
+    if (b->any_probes) KL(fdtdk_batch_probes(b->d_devs, b->n_act, b->stream));
+    KL(fdtdk_batch_half(1, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_h, b->n_h,
+                        b->d_work, b->d_err, b->stream));
+    KL(fdtdk_batch_half(0, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_e, b->n_e,
+                        b->d_work + 2, b->d_err, b->stream));
+    KL(fdtdk_batch_advance(b->d_steps, b->n_act, b->stream));
+  }
+  int finished = 0;
+  for (int g = 0; g < b->n_act; ++g) {
+    bmember *m = &b->m[b->act[g]];
+    m->done += nsteps;
+    if (m->done >= m->count) finished = 1;
+  }
+  if (finished) {
+    /* finished members: later calls on their handles follow the batch */
+    CU(cudaEventRecord(b->ev, b->stream));
+    for (int g = 0; g < b->n_act; ++g) {
+      bmember *m = &b->m[b->act[g]];
+      if (m->done < m->count) continue;
+      sim *s = lookup(m->h);
+      if (s) CU(cudaStreamWaitEvent(s->stream, b->ev, 0));
+    }
+    b->dirty = 1;
+  }
+  left = 0;
+  for (int i = 0; i < b->n; ++i) left += b->m[i].done < b->m[i].count;
+  if (active_left) *active_left = left;
+  return FDTD_OK;
+}
+
+/* Runs every member to its last step. */
+int fdtd_batch_run(fdtd_batch bh) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  int32_t left = 1;
+  while (left) {
+    int rc = fdtd_batch_step(bh, 1 << 30, &left);
+    if (rc) return rc;
+  }
+  CU(cudaStreamSynchronize(b->stream));
+  int32_t e = 0;
+  CU(cudaMemcpy(&e, b->d_err, sizeof(e), cudaMemcpyDeviceToHost));
+  if (e) {
+    cudaMemset(b->d_err, 0, sizeof(int32_t));
+    return fail(FDTD_ERR_CUDA, "a TMA pipeline wait timed out in a batched half-step "
+                               "(device error word %d); member fields are not valid", e);
+  }
+  return FDTD_OK;
+}
+
+/* Drops the members (finished or not); device buffers are kept. */
+int fdtd_batch_clear(fdtd_batch bh) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  CU(cudaStreamSynchronize(b->stream));
+  CU(cudaEventRecord(b->ev, b->stream));
+  for (int i = 0; i < b->n; ++i) {
+    sim *s = lookup(b->m[i].h);
+    if (s) CU(cudaStreamWaitEvent(s->stream, b->ev, 0));
+  }
+  b->n = 0;
+  b->n_act = 0;
+  b->dirty = 1;
+  return FDTD_OK;
+}
+
+/* Steps a member has completed in its batch (-1 if not a member). */
+int fdtd_batch_progress(fdtd_batch bh, fdtd_handle h, int32_t *done) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  if (!done) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  *done = -1;
+  for (int i = 0; i < b->n; ++i)
+    if (b->m[i].h == h) *done = b->m[i].done;
+  return FDTD_OK;
+}

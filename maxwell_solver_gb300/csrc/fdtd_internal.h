@@ -116,6 +116,22 @@ int fdtdk_compute_ce(const fdtd_dev *d, float *const ce[6],
 int fdtdk_init_1d(const fdtd_dev *d, float *tab[4], const float *pw,
                   float Ceh, float *scratch, cudaStream_t s);
 size_t fdtdk_init_1d_smem_limit(void);
+/* Batched half-step over many grids (fdtd_tma.cu): table holds n_items
+ * int4 {grid, x0, y0, kb | np << 16}; devs / maps (FDTD_NUM_MAPS x 128 B per
+ * grid, 64-byte aligned) / ops / steps are per-grid device arrays; work is
+ * a zeroed counter pair.  Every grid runs curl + CPML (+ its TF/SF mode and
+ * current source) at step steps[g] + ops[g].step. */
+int fdtdk_batch_half(int hfam, const fdtd_dev *devs, const void *maps, const fdtd_op *ops,
+                     const int32_t *steps, const int32_t *table, int32_t n_items, int32_t *work,
+                     int32_t *err, cudaStream_t s);
+/* Probe rows of every grid of a batch, then +1 on each grid's probe row
+ * and step (fdtd_kernels.cu). */
+int fdtdk_batch_probes(const fdtd_dev *devs, int32_t n, cudaStream_t s);
+int fdtdk_batch_advance(int32_t *steps, int32_t n, cudaStream_t s);
+/* Batched-tile geometry of the TMA kernels. */
+#define FDTD_TILE_X 64
+#define FDTD_TILE_Y 8
+
 /* Per-cell mu coefficients (src/simulation.h:43-63). */
 int fdtdk_compute_mu(float *out, const float *mu, const float *den_hx,
                      int64_t IJK, int32_t I, float delT, float sigma_m,

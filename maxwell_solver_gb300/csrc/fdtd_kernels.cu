@@ -161,6 +161,30 @@ __global__ void k_probe_gather(const fdtd_dev d) {
   }
 }
 
+// Batched probe gather: block g records grid g's probes into its current
+// row, then advances the row.
+__global__ void k_batch_probes(const fdtd_dev *devs, int n) {
+  const int g = blockIdx.x;
+  if (g >= n) return;
+  const fdtd_dev &d = devs[g];
+  if (d.num_ant <= 0 || !d.probes) return;
+  const int row = *d.probe_row;
+  if (row < d.T) {
+    for (int t = threadIdx.x; t < d.num_ant * 6; t += blockDim.x) {
+      const int a = t / 6, c = t - a * 6;
+      const int64_t id = d.probe_idx[a];
+      d.probes[((int64_t)row * d.num_ant + a) * 6 + c] = id >= 0 ? d.f[c][id] : 0.f;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *d.probe_row = row + 1;
+}
+
+__global__ void k_batch_advance(int32_t *steps, int n) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n) steps[g] += 1;
+}
+
 __global__ void k_add_i32(int32_t *p, int32_t v) { *p += v; }
 __global__ void k_set_i32(int32_t *p, int32_t v) { *p = v; }
 
@@ -545,6 +569,20 @@ int fdtdk_init_1d(const fdtd_dev *d, float *tab[4], const float *pw, float Ceh, 
   if (threads < 64) threads = 64;
   k_init_1d<<<2, threads, use_smem ? smem : 0, s>>>(*d, tab[0], tab[1], tab[2], tab[3], pw, Ceh,
                                                     scratch, use_smem);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_batch_probes(const fdtd_dev *devs, int32_t n, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_batch_probes<<<n, 256, 0, s>>>(devs, n);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_batch_advance(int32_t *steps, int32_t n, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_batch_advance<<<(n + 255) / 256, 256, 0, s>>>(steps, n);
   ++g_launches;
   return (int)cudaGetLastError();
 }

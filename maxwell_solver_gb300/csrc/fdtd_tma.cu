@@ -75,9 +75,19 @@ struct Maps {
   CUtensorMap m[FDTD_NUM_MAPS];
 };
 
-// Per-launch geometry of the work items.
+// Work items of one launch.  Single grid: a regular decomposition of the
+// grid (tiles_x * tiles_y tiles x z-runs of zchunk planes).  Batch: an
+// explicit table over many grids, each with its descriptor, TMA maps, op
+// and current step in device memory.
 struct Items {
   int tiles_x, tiles_y, zchunk, nk, n_items;
+  int32_t *work;             // [0] next item, [1] finished producers
+  int32_t *err;              // device error word
+  const int4 *table;         // batch: {grid, x0, y0, kb | np << 16} per item
+  const fdtd_dev *devs;      // batch: per grid
+  const CUtensorMap *maps;   // batch: FDTD_NUM_MAPS per grid
+  const fdtd_op *ops;        // batch: per grid (step from steps[])
+  const int32_t *steps;      // batch: step each grid is on
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -127,42 +137,53 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, u
       : "memory");
 }
 
-__device__ __forceinline__ void decode_item(const Items &it, int w, int &x0, int &y0, int &kb,
-                                            int &np) {
-  const int nt = it.tiles_x * it.tiles_y;
-  const int chunk = w / nt, tile = w - chunk * nt;
-  x0 = (tile % it.tiles_x) * BX;
-  y0 = (tile / it.tiles_x) * BY;
-  kb = chunk * it.zchunk;
-  np = min(it.zchunk, it.nk - kb);
+template <bool BATCH>
+__device__ __forceinline__ void decode_item(const Items &it, int w, int &g, int &x0, int &y0,
+                                            int &kb, int &np) {
+  if (BATCH) {
+    const int4 e = it.table[w];
+    g = e.x;
+    x0 = e.y;
+    y0 = e.z;
+    kb = e.w & 0xFFFF;
+    np = e.w >> 16;
+  } else {
+    const int nt = it.tiles_x * it.tiles_y;
+    const int chunk = w / nt, tile = w - chunk * nt;
+    g = 0;
+    x0 = (tile % it.tiles_x) * BX;
+    y0 = (tile / it.tiles_x) * BY;
+    kb = chunk * it.zchunk;
+    np = min(it.zchunk, it.nk - kb);
+  }
 }
 
 // Producer side of one launch (lane 0 of the producer warp).  `extra` more
 // loads follow each item's np planes (the H half-step reads plane k+1).
 // Ends with a sentinel stage, rewinds the work counter when it is the last
 // producer, and waits for its own copies before returning.
-template <int NS, class IssueFn>
-__device__ void produce(const fdtd_dev &d, const Items &it, int extra, uint64_t *full,
-                        uint64_t *empty, int4 *meta, IssueFn issue) {
+template <int NS, bool BATCH, class IssueFn>
+__device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *empty, int4 *meta,
+                        IssueFn issue) {
   int q = 0;
   bool ok = true;
   for (;;) {
-    const int w = atomicAdd(&d.work[0], 1);
+    const int w = atomicAdd(&it.work[0], 1);
     if (w >= it.n_items) break;
-    int x0, y0, kb, np;
-    decode_item(it, w, x0, y0, kb, np);
+    int g, x0, y0, kb, np;
+    decode_item<BATCH>(it, w, g, x0, y0, kb, np);
     for (int t = 0; t < np + extra && ok; ++t, ++q) {
       const int s = q % NS;
       if (q >= NS) ok = mbar_wait(&empty[s], (uint32_t)(((q / NS) - 1) & 1));
       if (!ok) break;
       meta[s] = make_int4(w, t, np, kb);
-      issue(s, x0, y0, kb + t);
+      issue(s, g, x0, y0, kb + t);
     }
     if (!ok) break;
   }
-  if (atomicAdd(&d.work[1], 1) == (int)gridDim.x - 1) {  // last producer: rewind
-    atomicExch(&d.work[0], 0);
-    atomicExch(&d.work[1], 0);
+  if (atomicAdd(&it.work[1], 1) == (int)gridDim.x - 1) {  // last producer: rewind
+    atomicExch(&it.work[0], 0);
+    atomicExch(&it.work[1], 0);
   }
   if (ok) {  // sentinel: tells the consumers there is no more work
     const int s = q % NS;
@@ -173,7 +194,7 @@ __device__ void produce(const fdtd_dev &d, const Items &it, int extra, uint64_t 
       ++q;
     }
   }
-  if (!ok && d.err) atomicExch(d.err, 3);
+  if (!ok && it.err) atomicExch(it.err, 3);
   // drain: every copy issued by this block has landed before it retires
   for (int r = (q > NS ? q - NS : 0); r < q; ++r) mbar_wait(&full[r % NS], (uint32_t)((r / NS) & 1));
 }
@@ -189,18 +210,18 @@ __device__ __forceinline__ void cell_map(int tid, int &xo, int &r0) {
 
 // ----------------------------------------------------------------- E half
 
-template <bool PML>
+template <bool PML, bool BATCH>
 __global__ void __launch_bounds__(NT, 3)
-    k_half_e_tma(const fdtd_dev d, const fdtd_op op, const __grid_constant__ Maps mp,
-                 const Items it) {
+    k_half_e_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
+                 const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSE * E_STAGE);
   uint64_t *empty = full + NSE;
   int4 *meta = reinterpret_cast<int4 *>(empty + NSE);
   float *stab = reinterpret_cast<float *>(smem + NSE * E_STAGE + CTRL_B);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const bool use_mat = d.coef_mode == 1;
-  const bool tab_in_smem = use_mat && d.n_mat <= kSmemTabMax;
+  // single grid: the coefficient table (if small) lives in shared memory
+  const bool tab_in_smem = !BATCH && d0.coef_mode == 1 && d0.n_mat <= kSmemTabMax;
 
   if (tid == 0) {
     for (int s = 0; s < NSE; ++s) {
@@ -210,36 +231,34 @@ __global__ void __launch_bounds__(NT, 3)
     mbar_init_fence();
   }
   if (tab_in_smem)
-    for (int t = tid; t < d.n_mat * 6; t += NT) stab[t] = __ldg(d.mat_tab + t);
+    for (int t = tid; t < d0.n_mat * 6; t += NT) stab[t] = __ldg(d0.mat_tab + t);
   __syncthreads();
 
   if (warp == NCW) {  // ------------------------------------- producer
     if (lane == 0) {
-      const uint32_t tx_bytes = 3 * TILE_B + 3 * HALO_B + (use_mat ? MAT_B : 0);
-      produce<NSE>(d, it, 0, full, empty, meta, [&](int s, int x0, int y0, int k) {
+      produce<NSE, BATCH>(it, 0, full, empty, meta, [&](int s, int g, int x0, int y0, int k) {
+        const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
+        const bool um = (BATCH ? it.devs[g].coef_mode : d0.coef_mode) == 1;
         unsigned char *st = smem + s * E_STAGE;
         proxy_fence();
-        mbar_expect_tx(&full[s], tx_bytes);
-        for (int c = 0; c < 3; ++c) tma_load_3d(st + c * TILE_B, &mp.m[c], &full[s], x0, y0, k);
+        mbar_expect_tx(&full[s], 3 * TILE_B + 3 * HALO_B + (um ? MAT_B : 0));
+        for (int c = 0; c < 3; ++c) tma_load_3d(st + c * TILE_B, &mm[c], &full[s], x0, y0, k);
         for (int c = 0; c < 3; ++c)
-          tma_load_3d(st + E_OFF_H + c * HALO_SLOT, &mp.m[3 + c], &full[s], x0 - 4, y0 - 1, k);
-        if (use_mat) tma_load_3d(st + E_OFF_M, &mp.m[12], &full[s], x0, y0, k);
+          tma_load_3d(st + E_OFF_H + c * HALO_SLOT, &mm[3 + c], &full[s], x0 - 4, y0 - 1, k);
+        if (um) tma_load_3d(st + E_OFF_M, &mm[12], &full[s], x0, y0, k);
       });
     }
     return;
   }
 
   // ------------------------------------------------------------ consumers
-  const int I = d.I, J = d.J, K = d.K;
   int xo, r0;
   cell_map(tid, xo, r0);
-  const int mode = op.tfsf_mode;
-  const int cm = op.cur_mode;
-  const int step = (mode || cm) ? op_step(d, op) : 0;
-  const float *inc = mode ? inc_e_row(d, mode, step) : nullptr;
-  const float cur_src = cm ? d.src[step] : 0.f;
-
-  int i = 0, y0 = 0, kb = 0;
+  // per-item state
+  int g = 0, x0i = 0, i = 0, y0 = 0, kb = 0, mode = 0, cm = 0;
+  bool use_mat = false;
+  const float *inc = nullptr;
+  float cur_src = 0.f;
   bool valid[2] = {false, false}, col_special[2] = {false, false}, cur_col[2] = {false, false};
   float hx_km[2] = {0.f, 0.f}, hy_km[2] = {0.f, 0.f};
   int64_t n0[2] = {0, 0};
@@ -247,15 +266,26 @@ __global__ void __launch_bounds__(NT, 3)
   for (int q = 0;; ++q) {
     const int s = q % NSE;
     if (!mbar_wait(&full[s], (uint32_t)((q / NSE) & 1))) {
-      if (d.err) atomicExch(d.err, 1);
+      if (it.err) atomicExch(it.err, 1);
       return;
     }
     const int4 m = meta[s];
     if (m.x < 0) return;  // sentinel
-    if (m.y == 0) {       // first plane of a new item: column constants
-      int x0, np;
-      decode_item(it, m.x, x0, y0, kb, np);
-      i = x0 + xo;
+    if (m.y == 0) {       // first plane of a new item
+      int np;
+      decode_item<BATCH>(it, m.x, g, x0i, y0, kb, np);
+    }
+    const fdtd_dev &d = BATCH ? it.devs[g] : d0;
+    const fdtd_op &op = BATCH ? it.ops[g] : op0;
+    const int I = d.I, J = d.J, K = d.K;
+    if (m.y == 0) {  // column constants of the item
+      i = x0i + xo;
+      mode = op.tfsf_mode;
+      cm = op.cur_mode;
+      use_mat = d.coef_mode == 1;
+      const int step = (mode || cm) ? (BATCH ? it.steps[g] + op.step : op_step(d, op)) : 0;
+      inc = mode ? inc_e_row(d, mode, step) : nullptr;
+      cur_src = cm ? d.src[step] : 0.f;
       const bool cur_x = cm && in_range(i, op.cur_box[0], op.cur_box[1]);
       const bool x_special =
           (PML && slab_e(i, I, d.p) >= 0) || (mode && (i == d.i0 || i == d.i1)) || i == 0;
@@ -339,10 +369,10 @@ __global__ void __launch_bounds__(NT, 3)
 
 // ----------------------------------------------------------------- H half
 
-template <bool PML>
+template <bool PML, bool BATCH>
 __global__ void __launch_bounds__(NT, 3)
-    k_half_h_tma(const fdtd_dev d, const fdtd_op op, const __grid_constant__ Maps mp,
-                 const Items it) {
+    k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
+                 const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSH * H_STAGE);
   uint64_t *empty = full + NSH;
@@ -361,38 +391,42 @@ __global__ void __launch_bounds__(NT, 3)
   if (warp == NCW) {  // ------------------------------------- producer
     if (lane == 0) {
       const uint32_t tx_bytes = 3 * HALO_B + 3 * TILE_B;
-      produce<NSH>(d, it, 1, full, empty, meta, [&](int s, int x0, int y0, int k) {
+      produce<NSH, BATCH>(it, 1, full, empty, meta, [&](int s, int g, int x0, int y0, int k) {
+        const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
         unsigned char *st = smem + s * H_STAGE;
         proxy_fence();
         mbar_expect_tx(&full[s], tx_bytes);
         for (int c = 0; c < 3; ++c)
-          tma_load_3d(st + c * HALO_SLOT, &mp.m[6 + c], &full[s], x0, y0, k);
+          tma_load_3d(st + c * HALO_SLOT, &mm[6 + c], &full[s], x0, y0, k);
         for (int c = 0; c < 3; ++c)
-          tma_load_3d(st + H_OFF_H + c * TILE_B, &mp.m[9 + c], &full[s], x0, y0, k);
+          tma_load_3d(st + H_OFF_H + c * TILE_B, &mm[9 + c], &full[s], x0, y0, k);
       });
     }
     return;
   }
 
   // ------------------------------------------------------------ consumers
-  const int I = d.I, J = d.J, K = d.K, p = d.p;
   int xo, r0;
   cell_map(tid, xo, r0);
-  const int mode = op.tfsf_mode;
-  const float *inc = mode ? inc_h_row(d, mode, op_step(d, op)) : nullptr;
-  const float Chh = d.Chh, Che = d.Che;
 
   int q = 0;
   for (;;) {
     int s = q % NSH;
     if (!mbar_wait(&full[s], (uint32_t)((q / NSH) & 1))) {
-      if (d.err) atomicExch(d.err, 2);
+      if (it.err) atomicExch(it.err, 2);
       return;
     }
     const int4 m = meta[s];
     if (m.x < 0) return;  // sentinel
-    int x0, y0, kb, np;
-    decode_item(it, m.x, x0, y0, kb, np);
+    int g, x0, y0, kb, np;
+    decode_item<BATCH>(it, m.x, g, x0, y0, kb, np);
+    const fdtd_dev &d = BATCH ? it.devs[g] : d0;
+    const fdtd_op &op = BATCH ? it.ops[g] : op0;
+    const int I = d.I, J = d.J, K = d.K, p = d.p;
+    const int mode = op.tfsf_mode;
+    const float *inc =
+        mode ? inc_h_row(d, mode, BATCH ? it.steps[g] + op.step : op_step(d, op)) : nullptr;
+    const float Chh = d.Chh, Che = d.Che;
     const int i = x0 + xo;
     const int px = PML ? slab_h(i, I, p) : -1;
     const bool x_special = px >= 0 || (mode && (i == d.i0 - 1 || i == d.i1));
@@ -412,7 +446,7 @@ __global__ void __launch_bounds__(NT, 3)
     for (int t = 0; t < np; ++t, ++q) {
       s = q % NSH;
       if (!mbar_wait(&full[s], (uint32_t)((q / NSH) & 1))) {
-        if (d.err) atomicExch(d.err, 2);
+        if (it.err) atomicExch(it.err, 2);
         return;
       }
       const int k = kb + t;
@@ -500,6 +534,9 @@ int launch(KH kern, int smem, int *cached_blocks, const fdtd_dev *d, const fdtd_
   Maps mp;
   memcpy(&mp, m->bytes, sizeof(Maps));
   Items it;
+  memset(&it, 0, sizeof(it));
+  it.work = d->work;
+  it.err = d->err;
   it.tiles_x = (ni + BX - 1) / BX;
   it.tiles_y = (nj + BY - 1) / BY;
   it.nk = nk;
@@ -539,7 +576,22 @@ int encode(CUtensorMap *out, void *base, CUtensorMapDataType dt, int esize, cons
   return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
 }
 
-int g_blocks_e[2] = {0, 0}, g_blocks_h[2] = {0, 0};
+int g_blocks_e[2] = {0, 0}, g_blocks_h[2] = {0, 0}, g_blocks_b[2] = {0, 0};
+
+// Resident blocks of a kernel on the current device (cached per kernel).
+template <class KH>
+int resident_blocks(KH kern, int smem, int *cached) {
+  if (*cached > 0) return 0;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return (int)e;
+  int per_sm = 0, sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+  if (e != cudaSuccess) return (int)e;
+  *cached = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  return 0;
+}
 
 }  // namespace
 
@@ -571,18 +623,52 @@ int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) {
 
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
   if (op->pml)
-    return launch(k_half_e_tma<true>, E_SMEM, &g_blocks_e[1], d, m, op, s, d->I, d->J, d->K,
-                  d->zc_e);
-  return launch(k_half_e_tma<false>, E_SMEM, &g_blocks_e[0], d, m, op, s, d->I, d->J, d->K,
-                d->zc_e);
+    return launch(k_half_e_tma<true, false>, E_SMEM, &g_blocks_e[1], d, m, op, s, d->I, d->J,
+                  d->K, d->zc_e);
+  return launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, op, s, d->I, d->J,
+                d->K, d->zc_e);
 }
 
 int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
   if (op->pml)
-    return launch(k_half_h_tma<true>, H_SMEM, &g_blocks_h[1], d, m, op, s, d->I - 1, d->J - 1,
-                  d->K - 1, d->zc_h);
-  return launch(k_half_h_tma<false>, H_SMEM, &g_blocks_h[0], d, m, op, s, d->I - 1, d->J - 1,
-                d->K - 1, d->zc_h);
+    return launch(k_half_h_tma<true, false>, H_SMEM, &g_blocks_h[1], d, m, op, s, d->I - 1,
+                  d->J - 1, d->K - 1, d->zc_h);
+  return launch(k_half_h_tma<false, false>, H_SMEM, &g_blocks_h[0], d, m, op, s, d->I - 1,
+                d->J - 1, d->K - 1, d->zc_h);
+}
+
+int fdtdk_batch_half(int hfam, const fdtd_dev *devs, const void *maps, const fdtd_op *ops,
+                     const int32_t *steps, const int32_t *table, int32_t n_items, int32_t *work,
+                     int32_t *err, cudaStream_t s) {
+  if (n_items <= 0) return 0;
+  Items it;
+  memset(&it, 0, sizeof(it));
+  it.n_items = n_items;
+  it.work = work;
+  it.err = err;
+  it.table = reinterpret_cast<const int4 *>(table);
+  it.devs = devs;
+  it.maps = static_cast<const CUtensorMap *>(maps);
+  it.ops = ops;
+  it.steps = steps;
+  // the single-grid parameters are unused in batch mode
+  static fdtd_dev d0;
+  static fdtd_op op0;
+  static Maps mp0;
+  int e;
+  if (hfam) {
+    e = resident_blocks(k_half_h_tma<true, true>, H_SMEM, &g_blocks_b[0]);
+    if (e) return e;
+    const int blocks = n_items < g_blocks_b[0] ? n_items : g_blocks_b[0];
+    k_half_h_tma<true, true><<<blocks, NT, H_SMEM, s>>>(d0, op0, mp0, it);
+  } else {
+    e = resident_blocks(k_half_e_tma<true, true>, E_SMEM, &g_blocks_b[1]);
+    if (e) return e;
+    const int blocks = n_items < g_blocks_b[1] ? n_items : g_blocks_b[1];
+    k_half_e_tma<true, true><<<blocks, NT, E_SMEM, s>>>(d0, op0, mp0, it);
+  }
+  fdtdk_count_launches(1);
+  return (int)cudaGetLastError();
 }
 
 }  // extern "C"

@@ -1,0 +1,106 @@
+"""Batched execution: heterogeneous grids advanced together by the batched
+persistent kernels end bit-identical to each grid run alone (and to the
+oracle), whatever the mix, the step counts, or when members join."""
+import numpy as np
+import pytest
+
+from scenarios import SCENARIOS, run_mex, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+
+
+def _ready(sc, inp):
+    """A handle set up like run_mex but with no step taken."""
+    from maxwell_solver_gb300 import simFDTD
+
+    return run_mex(simFDTD, type(sc)(**{**sc.__dict__, "steps": 0}), inp)
+
+
+def _fields(P, sc):
+    from maxwell_solver_gb300 import simFDTD
+
+    n = int(np.prod(sc.dims))
+    return [simFDTD("OutputVis", P, np.uint32(n), np.int32(f)) for f in range(1, 7)]
+
+
+def _current(sc):
+    return (sc.cur_mode, sc.cur_box) if sc.cur_mode else None
+
+
+def _alone(sc, inp, steps):
+    from maxwell_solver_gb300 import simFDTD
+
+    P = _ready(sc, inp)
+    cur = [np.int32([sc.cur_mode, *sc.cur_box])] if sc.cur_mode else []
+    simFDTD("StepN", P, np.int32([0, steps, sc.mode]), *cur)
+    out = _fields(P, sc)
+    probes = (simFDTD("OutputProbes", P, np.uint32(sc.steps * sc.n_probes * 6))
+              if sc.n_probes else None)
+    simFDTD("DeleteSimulation", P)
+    return out, probes
+
+
+def test_batch_equals_alone_heterogeneous():
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.batch import Batch
+
+    members = []
+    with Batch() as b:
+        for idx, sc in enumerate(SCENARIOS):
+            inp = sc.inputs()
+            steps = sc.steps - 7 * idx  # different step counts
+            P = _ready(sc, inp)
+            b.add(P, 0, steps, sc.mode, _current(sc))
+            members.append((sc, inp, steps, P))
+        b.run()
+        for sc, inp, steps, P in members:
+            got = _fields(P, sc)
+            want, want_probes = _alone(sc, inp, steps)
+            for a, w, n in zip(got, want, FIELDS):
+                np.testing.assert_array_equal(a, w, err_msg=f"{sc.name} {n}")
+            if sc.n_probes:
+                rec = simFDTD("OutputProbes", P, np.uint32(sc.steps * sc.n_probes * 6))
+                np.testing.assert_array_equal(rec, want_probes)
+            if steps == sc.steps:  # full runs also match the oracle
+                o = run_oracle(sc, "f32", inp=inp)
+                for a, n in zip(got, FIELDS):
+                    np.testing.assert_array_equal(a, o.field(n), err_msg=n)
+            simFDTD("DeleteSimulation", P)
+
+
+def test_members_joining_mid_run():
+    """A member added while others are half done (as the serving loop does)
+    still ends bit-identical to running alone."""
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.batch import Batch
+
+    a, c = SCENARIOS[0], SCENARIOS[3]
+    ia, ic = a.inputs(), c.inputs()
+    Pa, Pc = _ready(a, ia), _ready(c, ic)
+    with Batch() as b:
+        b.add(Pa, 0, a.steps, a.mode)
+        left = b.step(25)
+        assert left == 1 and b.progress(Pa) == 25
+        b.add(Pc, 0, c.steps, c.mode)
+        while b.step(13):
+            pass
+        assert b.progress(Pa) == a.steps and b.progress(Pc) == c.steps
+    for P, sc, inp in ((Pa, a, ia), (Pc, c, ic)):
+        want, _ = _alone(sc, inp, sc.steps)
+        for x, w, n in zip(_fields(P, sc), want, FIELDS):
+            np.testing.assert_array_equal(x, w, err_msg=f"{sc.name} {n}")
+        simFDTD("DeleteSimulation", P)
+
+
+def test_batch_rejects_unready_members():
+    from maxwell_solver_gb300 import SimFDTDError, simFDTD
+    from maxwell_solver_gb300.batch import Batch
+
+    P = simFDTD("CreateSimulation")
+    with Batch() as b:
+        with pytest.raises(SimFDTDError) as e:
+            b.add(P, 0, 10, 0)
+        assert e.value.identifier == "simFDTD:InvalidState"
+    simFDTD("DeleteSimulation", P)
