@@ -276,6 +276,10 @@ def run_ours(args, ranks):
     if ranks.rank == 0 and not args.no_e2e:
         e2e = run_e2e(w, K, simFDTD, materials, probe_locations, sources)
 
+    batched = None
+    if ranks.rank == 0 and not args.no_batch:
+        batched = run_batched(args.batch_grids)
+
     cpu = None
     if ranks.rank == 0 and not args.no_cpu:
         rate, done, secs = cpu_oracle_rate(w, target_s=args.cpu_seconds, max_steps=200)
@@ -306,6 +310,7 @@ def run_ours(args, ranks):
                               "alg_bytes_per_cell_step": ALG_BYTES_STEP}},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "batched": batched,
         "clocks": clk,
         "gpu_launches": int(launches),
     }
@@ -359,6 +364,87 @@ def run_e2e(w, K, simFDTD, materials, probe_locations, sources):
                     "material/source upload, probe + Ez readout"}
 
 
+def run_batched(n_grids: int, batched_only: bool = False):
+    """Batched configuration c4: the same heterogeneous solves run one at a
+    time through the plain solver (fdtd_step_n per grid) and together in one
+    batch (one H + one E launch per step for all of them); solves/s of both,
+    on the same handles (reset in between), and a bitwise identity check of
+    members between the two runs."""
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.batch import Batch
+    from maxwell_solver_gb300.workloads import batch_mix, setup_grid
+
+    mix = batch_mix(n_grids)
+    t0 = time.perf_counter()
+    handles = [setup_grid(simFDTD, s) for s in mix]
+    for P in handles:
+        simFDTD("Synchronize", P)
+    t_setup = time.perf_counter() - t0
+    check = list(range(0, len(mix), max(1, len(mix) // 8)))
+
+    t_one = t_ops = None
+    ref = {}
+    if not batched_only:
+        # one at a time through fdtd_step_n (graph-replayed fused steps)
+        t0 = time.perf_counter()
+        for P, s in zip(handles, mix):
+            simFDTD("StepN", P, np.int32([0, s.steps, s.mode]))
+            simFDTD("Synchronize", P)
+        t_one = time.perf_counter() - t0
+        ref = {g: simFDTD("OutputVis", handles[g], np.uint32(mix[g].cells), np.int32(3))
+               for g in check}
+        # one at a time through the per-op calls (6 per step, as highfrequency.m)
+        for P in handles:
+            simFDTD("ResetFieldAll", P)
+        t0 = time.perf_counter()
+        for P, s in zip(handles, mix):
+            for n in range(s.steps):
+                tm = np.array([n, s.mode], dtype=np.int32)
+                simFDTD("UpdateH_All", P)
+                simFDTD("UpdateH_PlaneWave", P, tm)
+                simFDTD("UpdateH_PML", P)
+                simFDTD("UpdateE_All", P)
+                simFDTD("UpdateE_PlaneWave", P, tm)
+                simFDTD("UpdateE_PML", P)
+            simFDTD("Synchronize", P)
+        t_ops = time.perf_counter() - t0
+
+    for P in handles:
+        simFDTD("ResetFieldAll", P)
+        simFDTD("Synchronize", P)
+    b = Batch()
+    t0 = time.perf_counter()
+    for P, s in zip(handles, mix):
+        b.add(P, 0, s.steps, s.mode)
+    b.run()
+    t_batch = time.perf_counter() - t0
+    b.close()
+    same = all(np.array_equal(ref[g], simFDTD("OutputVis", handles[g], np.uint32(mix[g].cells),
+                                              np.int32(3))) for g in ref)
+    for P in handles:
+        simFDTD("DeleteSimulation", P)
+    cell_steps = sum(s.cells * s.steps for s in mix)
+    rate = lambda t: None if t is None else round(len(mix) / t, 3)  # noqa: E731
+    return {
+        "workload": f"c4: {len(mix)} grids, axes U{{32..128}}, 8-cell CPML, 0-10 spheres, "
+                    "TF/SF axis mode U{1..4}, f0 U[10,60] GHz, steps U[300,1500] (seed 3)",
+        "solves": len(mix),
+        "batched_solves_per_s": rate(t_batch),
+        "one_at_a_time_solves_per_s": rate(t_one),
+        "one_at_a_time_per_op_solves_per_s": rate(t_ops),
+        "speedup": None if t_one is None else round(t_one / t_batch, 2),
+        "speedup_vs_per_op": None if t_ops is None else round(t_ops / t_batch, 2),
+        "batched_Mcell_steps_per_s": round(cell_steps / t_batch / 1e6, 1),
+        "seconds": {"batched": round(t_batch, 3),
+                    "one_at_a_time": None if t_one is None else round(t_one, 3),
+                    "one_at_a_time_per_op": None if t_ops is None else round(t_ops, 3),
+                    "setup": round(t_setup, 2)},
+        "identical_results": bool(same), "members_compared": len(ref),
+        "timing": "wall clock, fields resident, setup excluded; one at a time = fdtd_step_n "
+                  "per grid (graph-replayed fused steps) and, separately, the per-op calls",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -369,10 +455,17 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched (c4) leg")
+    ap.add_argument("--batch-grids", type=int, default=256)
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batched leg, without its one-at-a-time baselines")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     ranks = Ranks()
+    if args.batch_only:
+        print(json.dumps({"batched": run_batched(args.batch_grids, batched_only=True)}), flush=True)
+        return
     if args.impl == "reference":
         out = run_reference(args, ranks)
         ranks.close()

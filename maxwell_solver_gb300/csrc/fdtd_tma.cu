@@ -63,8 +63,30 @@ constexpr int H_OFF_H = 3 * HALO_SLOT;
 constexpr int H_STAGE = H_OFF_H + 3 * TILE_B;  // 13824 B
 constexpr int kSmemTabMax = 512;             // coefficient ids staged in shared memory
 constexpr int CTRL_B = 256;                  // barriers + stage metadata
-constexpr int E_SMEM = NSE * E_STAGE + CTRL_B + kSmemTabMax * 6 * 4;
-constexpr int H_SMEM = NSH * H_STAGE + CTRL_B;
+// Batch mode: every stage also carries its grid's descriptor and op (bulk
+// copies completing on the stage's barrier), so the per-cell code reads
+// them from shared memory instead of global memory.
+constexpr int DESC_B = 1536;                 // >= sizeof(fdtd_dev), 128-aligned
+constexpr int OPSLOT_B = 128;                // >= sizeof(fdtd_op)
+static_assert(sizeof(fdtd_dev) <= DESC_B && sizeof(fdtd_dev) % 16 == 0, "descriptor slot");
+static_assert(sizeof(fdtd_op) <= OPSLOT_B && sizeof(fdtd_op) % 16 == 0, "op slot");
+template <bool BATCH>
+struct EG {
+  static constexpr int NS = NSE;
+  static constexpr int STAGE = BATCH ? E_STAGE + DESC_B + OPSLOT_B : E_STAGE;
+  static constexpr int SMEM = NS * STAGE + CTRL_B + (BATCH ? 0 : kSmemTabMax * 6 * 4);
+};
+template <bool BATCH>
+struct HG {
+  static constexpr int NS = BATCH ? 4 : NSH;
+  static constexpr int STAGE = BATCH ? H_STAGE + DESC_B + OPSLOT_B : H_STAGE;
+  static constexpr int SMEM = NS * STAGE + CTRL_B;
+};
+constexpr int E_SMEM = EG<false>::SMEM;
+constexpr int H_SMEM = HG<false>::SMEM;
+static_assert(EG<true>::STAGE % 128 == 0 && HG<true>::STAGE % 128 == 0, "batch stage alignment");
+static_assert(3 * (EG<true>::SMEM + 1024) <= 228 * 1024 && 3 * (HG<true>::SMEM + 1024) <= 228 * 1024,
+              "three batch blocks per SM");
 constexpr unsigned kSpinLimit = 1u << 22;    // bounded mbarrier waits
 static_assert(E_STAGE % 128 == 0 && H_STAGE % 128 == 0, "stage alignment");
 static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
@@ -128,6 +150,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// Plain bulk copy global -> shared (16-byte aligned, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar,
                                             int x, int y, int z) {
   asm volatile(
@@ -215,10 +246,11 @@ __global__ void __launch_bounds__(NT, 3)
     k_half_e_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSE * E_STAGE);
+  constexpr int ST = EG<BATCH>::STAGE;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSE * ST);
   uint64_t *empty = full + NSE;
   int4 *meta = reinterpret_cast<int4 *>(empty + NSE);
-  float *stab = reinterpret_cast<float *>(smem + NSE * E_STAGE + CTRL_B);
+  float *stab = reinterpret_cast<float *>(smem + NSE * ST + CTRL_B);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // single grid: the coefficient table (if small) lives in shared memory
   const bool tab_in_smem = !BATCH && d0.coef_mode == 1 && d0.n_mat <= kSmemTabMax;
@@ -239,9 +271,14 @@ __global__ void __launch_bounds__(NT, 3)
       produce<NSE, BATCH>(it, 0, full, empty, meta, [&](int s, int g, int x0, int y0, int k) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
         const bool um = (BATCH ? it.devs[g].coef_mode : d0.coef_mode) == 1;
-        unsigned char *st = smem + s * E_STAGE;
+        unsigned char *st = smem + s * ST;
         proxy_fence();
-        mbar_expect_tx(&full[s], 3 * TILE_B + 3 * HALO_B + (um ? MAT_B : 0));
+        mbar_expect_tx(&full[s], 3 * TILE_B + 3 * HALO_B + (um ? MAT_B : 0) +
+                                     (BATCH ? (uint32_t)(sizeof(fdtd_dev) + sizeof(fdtd_op)) : 0u));
+        if (BATCH) {
+          bulk_g2s(st + E_STAGE, &it.devs[g], sizeof(fdtd_dev), &full[s]);
+          bulk_g2s(st + E_STAGE + DESC_B, &it.ops[g], sizeof(fdtd_op), &full[s]);
+        }
         for (int c = 0; c < 3; ++c) tma_load_3d(st + c * TILE_B, &mm[c], &full[s], x0, y0, k);
         for (int c = 0; c < 3; ++c)
           tma_load_3d(st + E_OFF_H + c * HALO_SLOT, &mm[3 + c], &full[s], x0 - 4, y0 - 1, k);
@@ -275,8 +312,9 @@ __global__ void __launch_bounds__(NT, 3)
       int np;
       decode_item<BATCH>(it, m.x, g, x0i, y0, kb, np);
     }
-    const fdtd_dev &d = BATCH ? it.devs[g] : d0;
-    const fdtd_op &op = BATCH ? it.ops[g] : op0;
+    const unsigned char *st = smem + s * ST;
+    const fdtd_dev &d = BATCH ? *reinterpret_cast<const fdtd_dev *>(st + E_STAGE) : d0;
+    const fdtd_op &op = BATCH ? *reinterpret_cast<const fdtd_op *>(st + E_STAGE + DESC_B) : op0;
     const int I = d.I, J = d.J, K = d.K;
     if (m.y == 0) {  // column constants of the item
       i = x0i + xo;
@@ -305,7 +343,6 @@ __global__ void __launch_bounds__(NT, 3)
       }
     }
     const int k = kb + m.y;
-    const unsigned char *st = smem + s * E_STAGE;
     const float *sEx = reinterpret_cast<const float *>(st);
     const float *sEy = sEx + BX * BY;
     const float *sEz = sEy + BX * BY;
@@ -374,13 +411,15 @@ __global__ void __launch_bounds__(NT, 3)
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSH * H_STAGE);
-  uint64_t *empty = full + NSH;
-  int4 *meta = reinterpret_cast<int4 *>(empty + NSH);
+  constexpr int ST = HG<BATCH>::STAGE;
+  constexpr int NS = HG<BATCH>::NS;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * ST);
+  uint64_t *empty = full + NS;
+  int4 *meta = reinterpret_cast<int4 *>(empty + NS);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
-    for (int s = 0; s < NSH; ++s) {
+    for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], NCW);
     }
@@ -391,11 +430,16 @@ __global__ void __launch_bounds__(NT, 3)
   if (warp == NCW) {  // ------------------------------------- producer
     if (lane == 0) {
       const uint32_t tx_bytes = 3 * HALO_B + 3 * TILE_B;
-      produce<NSH, BATCH>(it, 1, full, empty, meta, [&](int s, int g, int x0, int y0, int k) {
+      produce<NS, BATCH>(it, 1, full, empty, meta, [&](int s, int g, int x0, int y0, int k) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
-        unsigned char *st = smem + s * H_STAGE;
+        unsigned char *st = smem + s * ST;
         proxy_fence();
-        mbar_expect_tx(&full[s], tx_bytes);
+        mbar_expect_tx(&full[s], tx_bytes + (BATCH ? (uint32_t)(sizeof(fdtd_dev) +
+                                                                sizeof(fdtd_op)) : 0u));
+        if (BATCH) {
+          bulk_g2s(st + H_STAGE, &it.devs[g], sizeof(fdtd_dev), &full[s]);
+          bulk_g2s(st + H_STAGE + DESC_B, &it.ops[g], sizeof(fdtd_op), &full[s]);
+        }
         for (int c = 0; c < 3; ++c)
           tma_load_3d(st + c * HALO_SLOT, &mm[6 + c], &full[s], x0, y0, k);
         for (int c = 0; c < 3; ++c)
@@ -411,8 +455,8 @@ __global__ void __launch_bounds__(NT, 3)
 
   int q = 0;
   for (;;) {
-    int s = q % NSH;
-    if (!mbar_wait(&full[s], (uint32_t)((q / NSH) & 1))) {
+    int s = q % NS;
+    if (!mbar_wait(&full[s], (uint32_t)((q / NS) & 1))) {
       if (it.err) atomicExch(it.err, 2);
       return;
     }
@@ -420,8 +464,12 @@ __global__ void __launch_bounds__(NT, 3)
     if (m.x < 0) return;  // sentinel
     int g, x0, y0, kb, np;
     decode_item<BATCH>(it, m.x, g, x0, y0, kb, np);
-    const fdtd_dev &d = BATCH ? it.devs[g] : d0;
-    const fdtd_op &op = BATCH ? it.ops[g] : op0;
+    // the item's descriptor and op: the first load's copies (every load of
+    // the item carries the same ones)
+    const unsigned char *st_item = smem + s * ST;
+    const fdtd_dev &d = BATCH ? *reinterpret_cast<const fdtd_dev *>(st_item + H_STAGE) : d0;
+    const fdtd_op &op =
+        BATCH ? *reinterpret_cast<const fdtd_op *>(st_item + H_STAGE + DESC_B) : op0;
     const int I = d.I, J = d.J, K = d.K, p = d.p;
     const int mode = op.tfsf_mode;
     const float *inc =
@@ -444,14 +492,17 @@ __global__ void __launch_bounds__(NT, 3)
     int prev = s;
     ++q;
     for (int t = 0; t < np; ++t, ++q) {
-      s = q % NSH;
-      if (!mbar_wait(&full[s], (uint32_t)((q / NSH) & 1))) {
+      s = q % NS;
+      if (!mbar_wait(&full[s], (uint32_t)((q / NS) & 1))) {
         if (it.err) atomicExch(it.err, 2);
         return;
       }
       const int k = kb + t;
-      const unsigned char *st0 = smem + prev * H_STAGE;
-      const unsigned char *st1 = smem + s * H_STAGE;
+      const unsigned char *st0 = smem + prev * ST;
+      // descriptor of the stage in use (the item's first stage may already
+      // have been handed back to the producer)
+      const fdtd_dev &dp = BATCH ? *reinterpret_cast<const fdtd_dev *>(st0 + H_STAGE) : d0;
+      const unsigned char *st1 = smem + s * ST;
       const float *sEx = reinterpret_cast<const float *>(st0);
       const float *sEy = sEx + HALO_SLOT / 4;
       const float *sEz = sEy + HALO_SLOT / 4;
@@ -461,8 +512,8 @@ __global__ void __launch_bounds__(NT, 3)
       const float *sHy = sHx + BX * BY;
       const float *sHz = sHy + BX * BY;
       const int pz = PML ? slab_h(k, K, p) : -1;
-      const bool plane_special = pz >= 0 || (mode && (k == d.k0 - 1 || k == d.k1));
-      const int64_t off = (int64_t)t * d.plane;
+      const bool plane_special = pz >= 0 || (mode && (k == dp.k0 - 1 || k == dp.k1));
+      const int64_t off = (int64_t)t * dp.plane;
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         const int ty = r0 + 4 * c;
@@ -476,7 +527,7 @@ __global__ void __launch_bounds__(NT, 3)
         float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
         if (__any_sync(0xffffffffu, act && (col_special[c] || plane_special))) {
           if (act)
-            update_h_cell<true, PML>(d, mode, inc, i, y0 + ty, k, px, py[c], pz, hx, hy, hz,
+            update_h_cell<true, PML>(dp, mode, inc, i, y0 + ty, k, px, py[c], pz, hx, hy, hz,
                                      dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z);
         } else {
           hx = Chh * hx + Che * (-dEz_y + dEy_z);
@@ -484,9 +535,9 @@ __global__ void __launch_bounds__(NT, 3)
           hz = Chh * hz + Che * (-dEy_x + dEx_y);
         }
         if (act) {
-          d.f[3][n0[c] + off] = hx;
-          d.f[4][n0[c] + off] = hy;
-          d.f[5][n0[c] + off] = hz;
+          dp.f[3][n0[c] + off] = hx;
+          dp.f[4][n0[c] + off] = hy;
+          dp.f[5][n0[c] + off] = hz;
         }
       }
       __syncwarp();
@@ -657,15 +708,15 @@ int fdtdk_batch_half(int hfam, const fdtd_dev *devs, const void *maps, const fdt
   static Maps mp0;
   int e;
   if (hfam) {
-    e = resident_blocks(k_half_h_tma<true, true>, H_SMEM, &g_blocks_b[0]);
+    e = resident_blocks(k_half_h_tma<true, true>, HG<true>::SMEM, &g_blocks_b[0]);
     if (e) return e;
     const int blocks = n_items < g_blocks_b[0] ? n_items : g_blocks_b[0];
-    k_half_h_tma<true, true><<<blocks, NT, H_SMEM, s>>>(d0, op0, mp0, it);
+    k_half_h_tma<true, true><<<blocks, NT, HG<true>::SMEM, s>>>(d0, op0, mp0, it);
   } else {
-    e = resident_blocks(k_half_e_tma<true, true>, E_SMEM, &g_blocks_b[1]);
+    e = resident_blocks(k_half_e_tma<true, true>, EG<true>::SMEM, &g_blocks_b[1]);
     if (e) return e;
     const int blocks = n_items < g_blocks_b[1] ? n_items : g_blocks_b[1];
-    k_half_e_tma<true, true><<<blocks, NT, E_SMEM, s>>>(d0, op0, mp0, it);
+    k_half_e_tma<true, true><<<blocks, NT, EG<true>::SMEM, s>>>(d0, op0, mp0, it);
   }
   fdtdk_count_launches(1);
   return (int)cudaGetLastError();

@@ -163,3 +163,91 @@ def setup(api, w: Workload, steps: int | None = None, params=None):
     api("ReadySimulation", P)
     api("Init1D", P, np.float32(1.0), pw)
     return P
+
+
+# ------------------------------------------------------------------ batches
+
+@dataclass(frozen=True)
+class GridSpec:
+    """One solve of a heterogeneous mix (batched configuration c4 / served c5)."""
+    dims: tuple
+    steps: int
+    pml: int
+    mode: int
+    n_spheres: int
+    fctr: float
+    seed: int
+    delX: float = 1e-3
+
+    @property
+    def delT(self) -> float:
+        return 0.99 * self.delX / (math.sqrt(3.0) * C0)
+
+    @property
+    def cells(self) -> int:
+        return int(np.prod(self.dims))
+
+
+def batch_mix(n: int = 256, seed: int = 3):
+    """c4: axes uniform-integer 32..128, 8-cell CPML, 0..10 spheres, TF/SF with
+    a random axis-aligned incidence (modes 1..4) and f0 uniform 10..60 GHz,
+    steps uniform 300..1500."""
+    r = rng(seed)
+    out = []
+    for g in range(n):
+        dims = tuple(int(x) for x in r.integers(32, 129, 3))
+        out.append(GridSpec(dims, int(r.integers(300, 1501)), 8, int(r.integers(1, 5)),
+                            int(r.integers(0, 11)), float(r.uniform(10e9, 60e9)), seed * 1000 + g))
+    return out
+
+
+def grid_materials(spec: GridSpec):
+    """eps, sigma (float32, F-order flat) with the spec's random spheres."""
+    I, J, K = spec.dims
+    r = rng(spec.seed)
+    eps = np.ones((I, J, K), dtype=np.float32, order="F")
+    sig = np.zeros((I, J, K), dtype=np.float32, order="F")
+    lo = spec.pml + 2
+    room = min(I, J, K) - 2 * lo
+    for _ in range(spec.n_spheres):
+        rad = min(r.uniform(4, 20), max(room / 2 - 1, 1.0))
+        c = [r.uniform(lo + rad, n - lo - rad) for n in (I, J, K)]
+        e = np.float32(r.uniform(1.5, 10.0))
+        s = np.float32(10.0 ** r.uniform(-4, 0))
+        b0 = [max(0, int(math.floor(c[a] - rad))) for a in range(3)]
+        b1 = [min(n, int(math.ceil(c[a] + rad)) + 1) for a, n in enumerate((I, J, K))]
+        x = np.arange(b0[0], b1[0]) + 0.5 - c[0]
+        y = np.arange(b0[1], b1[1]) + 0.5 - c[1]
+        z = np.arange(b0[2], b1[2]) + 0.5 - c[2]
+        inside = (x[:, None, None] ** 2 + y[None, :, None] ** 2 + z[None, None, :] ** 2) <= rad * rad
+        sl = (slice(b0[0], b1[0]), slice(b0[1], b1[1]), slice(b0[2], b1[2]))
+        eps[sl][inside] = e
+        sig[sl][inside] = s
+    return eps.ravel(order="F"), sig.ravel(order="F")
+
+
+def grid_source(spec: GridSpec):
+    """Gaussian-modulated sine at the spec's f0 (10 ps spread), float32 [steps]."""
+    n = np.arange(spec.steps, dtype=np.float64)
+    t = n * float(np.float32(spec.delT))
+    spread = 10e-12
+    t0 = 4 * spread
+    return (np.sin(2 * math.pi * spec.fctr * (t - t0)) *
+            np.exp(-((t - t0) / spread) ** 2)).astype(np.float32)
+
+
+def setup_grid(api, spec: GridSpec):
+    """Creates and readies one grid of a mix; returns its handle."""
+    I, J, K = spec.dims
+    P = api("CreateSimulation")
+    api("SetParams", P, np.float64([spec.pml, spec.pml + 5, 3, 1, 0.08, 1, 0.8, 0]))
+    api("SetConst", P, np.float32([spec.fctr, spec.delX, spec.delT]),
+        np.int32([spec.steps, I, J, K, 0]))
+    eps, sig = grid_materials(spec)
+    for flag in (1, 2, 3):
+        api("UpdateMaterial", P, np.int32(flag), sig)
+    for flag in (4, 5, 6):
+        api("UpdateMaterial", P, np.int32(flag), eps)
+    api("ReadySimulation", P)
+    api("Init1D", P, np.float32(1.0), grid_source(spec))
+    return P
