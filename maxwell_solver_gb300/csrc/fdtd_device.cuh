@@ -215,41 +215,50 @@ __device__ __forceinline__ void update_h_cell(const fdtd_dev &d, int mode, const
   }
   if (mode) tfsf_h(d, mode, inc, i, j, k, hx, hy, hz);
   if (PML) {
+    // Each psi entry belongs to one cell, so all of the cell's psi loads are
+    // issued before its first psi store: one memory round trip, not six.
     const int64_t I = d.I, J = d.J, pj = 2 * (int64_t)d.p;
+    const int64_t ty = i + py * I + k * pj * I;
+    const int64_t tx = px + j * pj + k * pj * J;
+    const int64_t tz = i + j * I + pz * d.IJ;
+    float y0 = 0.f, y1 = 0.f, x0 = 0.f, x1 = 0.f, z0 = 0.f, z1 = 0.f;
     if (py >= 0) {
-      const int64_t t = i + py * I + k * pj * I;
+      y0 = d.psi[PSI_HXY][ty];
+      y1 = d.psi[PSI_HZY][ty];
+    }
+    if (px >= 0) {
+      x0 = d.psi[PSI_HYX][tx];
+      x1 = d.psi[PSI_HZX][tx];
+    }
+    if (pz >= 0) {
+      z0 = d.psi[PSI_HXZ][tz];
+      z1 = d.psi[PSI_HYZ][tz];
+    }
+    if (py >= 0) {
       const float b = d.bH[py], c = d.cH[py];
-      float *ps = d.psi[PSI_HXY] + t;
-      float v = b * *ps + c * dEz_y / dx;
-      *ps = v;
+      float v = b * y0 + c * dEz_y / dx;
+      d.psi[PSI_HXY][ty] = v;
       hx = hx - Che * v * dx;
-      ps = d.psi[PSI_HZY] + t;
-      v = b * *ps + c * dEx_y / dx;
-      *ps = v;
+      v = b * y1 + c * dEx_y / dx;
+      d.psi[PSI_HZY][ty] = v;
       hz = hz + Che * v * dx;
     }
     if (px >= 0) {
-      const int64_t t = px + j * pj + k * pj * J;
       const float b = d.bH[px], c = d.cH[px];
-      float *ps = d.psi[PSI_HYX] + t;
-      float v = b * *ps + c * dEz_x / dx;
-      *ps = v;
+      float v = b * x0 + c * dEz_x / dx;
+      d.psi[PSI_HYX][tx] = v;
       hy = hy + Che * v * dx;
-      ps = d.psi[PSI_HZX] + t;
-      v = b * *ps + c * dEy_x / dx;
-      *ps = v;
+      v = b * x1 + c * dEy_x / dx;
+      d.psi[PSI_HZX][tx] = v;
       hz = hz - Che * v * dx;
     }
     if (pz >= 0) {
-      const int64_t t = i + j * I + pz * d.IJ;
       const float b = d.bH[pz], c = d.cH[pz];
-      float *ps = d.psi[PSI_HXZ] + t;
-      float v = b * *ps + c * dEy_z / dx;
-      *ps = v;
+      float v = b * z0 + c * dEy_z / dx;
+      d.psi[PSI_HXZ][tz] = v;
       hx = hx + Che * v * dx;
-      ps = d.psi[PSI_HYZ] + t;
-      v = b * *ps + c * dEx_z / dx;
-      *ps = v;
+      v = b * z1 + c * dEx_z / dx;
+      d.psi[PSI_HYZ][tz] = v;
       hy = hy - Che * v * dx;
     }
   }
@@ -286,41 +295,49 @@ __device__ __forceinline__ void update_e_cell(const fdtd_dev &d, int mode, const
   }
   if (mode) tfsf_e(d, mode, inc, i, j, k, C.exh, C.eyh, C.ezh, ex, ey, ez);
   if (PML) {
+    // all psi loads of the cell first (see update_h_cell)
     const int64_t I = d.I, J = d.J, pj = 2 * (int64_t)d.p;
+    const int64_t ty = i + py * I + k * pj * I;
+    const int64_t tz = i + j * I + pz * d.IJ;
+    const int64_t tx = px + j * pj + k * pj * J;
+    float y0 = 0.f, y1 = 0.f, z0 = 0.f, z1 = 0.f, x0 = 0.f, x1 = 0.f;
     if (py >= 0) {
-      const int64_t t = i + py * I + k * pj * I;
+      y0 = d.psi[PSI_EXY][ty];
+      y1 = d.psi[PSI_EZY][ty];
+    }
+    if (pz >= 0) {
+      z0 = d.psi[PSI_EXZ][tz];
+      z1 = d.psi[PSI_EYZ][tz];
+    }
+    if (px >= 0) {
+      x0 = d.psi[PSI_EYX][tx];
+      x1 = d.psi[PSI_EZX][tx];
+    }
+    if (py >= 0) {
       const float b = d.bE[py], c = d.cE[py];
-      float *ps = d.psi[PSI_EXY] + t;
-      float v = b * *ps + c * (hz - hz_jm) / dx;
-      *ps = v;
+      float v = b * y0 + c * (hz - hz_jm) / dx;
+      d.psi[PSI_EXY][ty] = v;
       ex = ex + C.exh * v * dx;
-      ps = d.psi[PSI_EZY] + t;
-      v = b * *ps + c * (hx - hx_jm) / dx;
-      *ps = v;
+      v = b * y1 + c * (hx - hx_jm) / dx;
+      d.psi[PSI_EZY][ty] = v;
       ez = ez - C.ezh * v * dx;
     }
     if (pz >= 0) {
-      const int64_t t = i + j * I + pz * d.IJ;
       const float b = d.bE[pz], c = d.cE[pz];
-      float *ps = d.psi[PSI_EXZ] + t;
-      float v = b * *ps + c * (hy - hy_km) / dx;
-      *ps = v;
+      float v = b * z0 + c * (hy - hy_km) / dx;
+      d.psi[PSI_EXZ][tz] = v;
       ex = ex - C.exh * v * dx;
-      ps = d.psi[PSI_EYZ] + t;
-      v = b * *ps + c * (hx - hx_km) / dx;
-      *ps = v;
+      v = b * z1 + c * (hx - hx_km) / dx;
+      d.psi[PSI_EYZ][tz] = v;
       ey = ey + C.eyh * v * dx;
     }
     if (px >= 0) {
-      const int64_t t = px + j * pj + k * pj * J;
       const float b = d.bE[px], c = d.cE[px];
-      float *ps = d.psi[PSI_EYX] + t;
-      float v = b * *ps + c * (hz - hz_im) / dx;
-      *ps = v;
+      float v = b * x0 + c * (hz - hz_im) / dx;
+      d.psi[PSI_EYX][tx] = v;
       ey = ey - C.eyh * v * dx;
-      ps = d.psi[PSI_EZX] + t;
-      v = b * *ps + c * (hy - hy_im) / dx;
-      *ps = v;
+      v = b * x1 + c * (hy - hy_im) / dx;
+      d.psi[PSI_EZX][tx] = v;
       ez = ez + C.ezh * v * dx;
     }
   }

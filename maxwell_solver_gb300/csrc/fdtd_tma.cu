@@ -65,15 +65,18 @@ constexpr int kSmemTabMax = 512;             // coefficient ids staged in shared
 constexpr int CTRL_B = 256;                  // barriers + stage metadata
 // Batch mode: every stage also carries its grid's descriptor and op (bulk
 // copies completing on the stage's barrier), so the per-cell code reads
-// them from shared memory instead of global memory.
+// them from shared memory instead of global memory; E stages also carry
+// the grid's coefficient table when it has at most kStageTabMax ids.
 constexpr int DESC_B = 1536;                 // >= sizeof(fdtd_dev), 128-aligned
 constexpr int OPSLOT_B = 128;                // >= sizeof(fdtd_op)
+constexpr int kStageTabMax = 64;
+constexpr int TAB_B = kStageTabMax * 6 * 4;  // 1536 B
 static_assert(sizeof(fdtd_dev) <= DESC_B && sizeof(fdtd_dev) % 16 == 0, "descriptor slot");
 static_assert(sizeof(fdtd_op) <= OPSLOT_B && sizeof(fdtd_op) % 16 == 0, "op slot");
 template <bool BATCH>
 struct EG {
   static constexpr int NS = NSE;
-  static constexpr int STAGE = BATCH ? E_STAGE + DESC_B + OPSLOT_B : E_STAGE;
+  static constexpr int STAGE = BATCH ? E_STAGE + DESC_B + OPSLOT_B + TAB_B : E_STAGE;
   static constexpr int SMEM = NS * STAGE + CTRL_B + (BATCH ? 0 : kSmemTabMax * 6 * 4);
 };
 template <bool BATCH>
@@ -91,7 +94,7 @@ constexpr unsigned kSpinLimit = 1u << 22;    // bounded mbarrier waits
 static_assert(E_STAGE % 128 == 0 && H_STAGE % 128 == 0, "stage alignment");
 static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
               "TMA inner box extents must be multiples of 16 bytes");
-static_assert(NSH * (8 + 8 + 16) <= CTRL_B && NSE * (8 + 8 + 16) <= CTRL_B, "control block");
+static_assert(NSH * (8 + 8 + 32) <= CTRL_B && NSE * (8 + 8 + 32) <= CTRL_B, "control block");
 
 struct Maps {
   CUtensorMap m[FDTD_NUM_MAPS];
@@ -189,13 +192,16 @@ __device__ __forceinline__ void decode_item(const Items &it, int w, int &g, int 
   }
 }
 
+// Stage metadata, written by the producer before it arms the stage:
+// meta[2s] = {item, plane of the item, planes, first plane},
+// meta[2s+1] = {grid, x0, y0, absolute step of the grid's op}.
 // Producer side of one launch (lane 0 of the producer warp).  `extra` more
 // loads follow each item's np planes (the H half-step reads plane k+1).
 // Ends with a sentinel stage, rewinds the work counter when it is the last
 // producer, and waits for its own copies before returning.
-template <int NS, bool BATCH, class IssueFn>
+template <int NS, bool BATCH, class StepFn, class IssueFn>
 __device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *empty, int4 *meta,
-                        IssueFn issue) {
+                        StepFn step_of, IssueFn issue) {
   int q = 0;
   bool ok = true;
   for (;;) {
@@ -203,11 +209,13 @@ __device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *em
     if (w >= it.n_items) break;
     int g, x0, y0, kb, np;
     decode_item<BATCH>(it, w, g, x0, y0, kb, np);
+    const int step = step_of(g);
     for (int t = 0; t < np + extra && ok; ++t, ++q) {
       const int s = q % NS;
       if (q >= NS) ok = mbar_wait(&empty[s], (uint32_t)(((q / NS) - 1) & 1));
       if (!ok) break;
-      meta[s] = make_int4(w, t, np, kb);
+      meta[2 * s] = make_int4(w, t, np, kb);
+      meta[2 * s + 1] = make_int4(g, x0, y0, step);
       issue(s, g, x0, y0, kb + t);
     }
     if (!ok) break;
@@ -220,7 +228,7 @@ __device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *em
     const int s = q % NS;
     if (q >= NS) ok = mbar_wait(&empty[s], (uint32_t)(((q / NS) - 1) & 1));
     if (ok) {
-      meta[s] = make_int4(-1, 0, 0, 0);
+      meta[2 * s] = make_int4(-1, 0, 0, 0);
       mbar_arrive(&full[s]);
       ++q;
     }
@@ -268,16 +276,34 @@ __global__ void __launch_bounds__(NT, 3)
 
   if (warp == NCW) {  // ------------------------------------- producer
     if (lane == 0) {
-      produce<NSE, BATCH>(it, 0, full, empty, meta, [&](int s, int g, int x0, int y0, int k) {
+      // per item (batch): the grid's coefficient mode and table size
+      int g_um = -1;
+      bool um = d0.coef_mode == 1;
+      uint32_t tab_b = 0;
+      const auto step_of = [&](int g) {
+        return (BATCH ? it.steps[g] + it.ops[g].step : op_step(d0, op0));
+      };
+      produce<NSE, BATCH>(it, 0, full, empty, meta, step_of, [&](int s, int g, int x0, int y0,
+                                                                  int k) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
-        const bool um = (BATCH ? it.devs[g].coef_mode : d0.coef_mode) == 1;
+        if (BATCH && g != g_um) {
+          g_um = g;
+          um = it.devs[g].coef_mode == 1;
+          const int nm = it.devs[g].n_mat;
+          // whole 16-byte units; the table allocation holds 32768 ids
+          tab_b = (um && nm <= kStageTabMax) ? (uint32_t)((nm * 24 + 15) & ~15) : 0u;
+        }
         unsigned char *st = smem + s * ST;
+        const uint32_t desc_b = BATCH ? (uint32_t)(sizeof(fdtd_dev) + sizeof(fdtd_op)) : 0u;
         proxy_fence();
-        mbar_expect_tx(&full[s], 3 * TILE_B + 3 * HALO_B + (um ? MAT_B : 0) +
-                                     (BATCH ? (uint32_t)(sizeof(fdtd_dev) + sizeof(fdtd_op)) : 0u));
+        // one arrive per phase: the stage's whole byte count at once
+        mbar_expect_tx(&full[s], desc_b + 3 * TILE_B + 3 * HALO_B + (um ? MAT_B : 0) +
+                                     (BATCH ? tab_b : 0u));
         if (BATCH) {
           bulk_g2s(st + E_STAGE, &it.devs[g], sizeof(fdtd_dev), &full[s]);
           bulk_g2s(st + E_STAGE + DESC_B, &it.ops[g], sizeof(fdtd_op), &full[s]);
+          if (tab_b)
+            bulk_g2s(st + E_STAGE + DESC_B + OPSLOT_B, it.devs[g].mat_tab, tab_b, &full[s]);
         }
         for (int c = 0; c < 3; ++c) tma_load_3d(st + c * TILE_B, &mm[c], &full[s], x0, y0, k);
         for (int c = 0; c < 3; ++c)
@@ -292,8 +318,8 @@ __global__ void __launch_bounds__(NT, 3)
   int xo, r0;
   cell_map(tid, xo, r0);
   // per-item state
-  int g = 0, x0i = 0, i = 0, y0 = 0, kb = 0, mode = 0, cm = 0;
-  bool use_mat = false;
+  int i = 0, y0 = 0, kb = 0, mode = 0, cm = 0;
+  bool use_mat = false, tab_local = false;
   const float *inc = nullptr;
   float cur_src = 0.f;
   bool valid[2] = {false, false}, col_special[2] = {false, false}, cur_col[2] = {false, false};
@@ -306,22 +332,27 @@ __global__ void __launch_bounds__(NT, 3)
       if (it.err) atomicExch(it.err, 1);
       return;
     }
-    const int4 m = meta[s];
+    const int4 m = meta[2 * s];
     if (m.x < 0) return;  // sentinel
-    if (m.y == 0) {       // first plane of a new item
-      int np;
-      decode_item<BATCH>(it, m.x, g, x0i, y0, kb, np);
-    }
     const unsigned char *st = smem + s * ST;
     const fdtd_dev &d = BATCH ? *reinterpret_cast<const fdtd_dev *>(st + E_STAGE) : d0;
     const fdtd_op &op = BATCH ? *reinterpret_cast<const fdtd_op *>(st + E_STAGE + DESC_B) : op0;
+    const float *ttab = BATCH ? reinterpret_cast<const float *>(st + E_STAGE + DESC_B + OPSLOT_B)
+                              : stab;
     const int I = d.I, J = d.J, K = d.K;
-    if (m.y == 0) {  // column constants of the item
-      i = x0i + xo;
+    const float *sHx = reinterpret_cast<const float *>(st + E_OFF_H);
+    const float *sHy = sHx + HALO_SLOT / 4;
+    const float *sHz = sHy + HALO_SLOT / 4;
+    if (m.y == 0) {  // first plane of a new item: column constants
+      const int4 m1 = meta[2 * s + 1];
+      kb = m.w;
+      y0 = m1.z;
+      i = m1.y + xo;
       mode = op.tfsf_mode;
       cm = op.cur_mode;
       use_mat = d.coef_mode == 1;
-      const int step = (mode || cm) ? (BATCH ? it.steps[g] + op.step : op_step(d, op)) : 0;
+      tab_local = BATCH ? (use_mat && d.n_mat <= kStageTabMax) : tab_in_smem;
+      const int step = m1.w;
       inc = mode ? inc_e_row(d, mode, step) : nullptr;
       cur_src = cm ? d.src[step] : 0.f;
       const bool cur_x = cm && in_range(i, op.cur_box[0], op.cur_box[1]);
@@ -346,9 +377,6 @@ __global__ void __launch_bounds__(NT, 3)
     const float *sEx = reinterpret_cast<const float *>(st);
     const float *sEy = sEx + BX * BY;
     const float *sEz = sEy + BX * BY;
-    const float *sHx = reinterpret_cast<const float *>(st + E_OFF_H);
-    const float *sHy = sHx + HALO_SLOT / 4;
-    const float *sHz = sHy + HALO_SLOT / 4;
     const uint16_t *sM = reinterpret_cast<const uint16_t *>(st + E_OFF_M);
     const bool plane_special = (PML && slab_e(k, K, d.p) >= 0) ||
                                (mode && (k == d.k0 || k == d.k1)) || k == 0 ||
@@ -363,8 +391,8 @@ __global__ void __launch_bounds__(NT, 3)
       Coef6 C = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       if (use_mat) {
         const int mi = sM[eb];
-        if (tab_in_smem) {
-          const float *r = stab + mi * 6;
+        if (tab_local) {
+          const float *r = ttab + mi * 6;
           C.exe = r[0]; C.eye = r[1]; C.eze = r[2]; C.exh = r[3]; C.eyh = r[4]; C.ezh = r[5];
         } else {
           C = coef_from_table(d, mi);
@@ -430,7 +458,11 @@ __global__ void __launch_bounds__(NT, 3)
   if (warp == NCW) {  // ------------------------------------- producer
     if (lane == 0) {
       const uint32_t tx_bytes = 3 * HALO_B + 3 * TILE_B;
-      produce<NS, BATCH>(it, 1, full, empty, meta, [&](int s, int g, int x0, int y0, int k) {
+      const auto step_of = [&](int g) {
+        return (BATCH ? it.steps[g] + it.ops[g].step : op_step(d0, op0));
+      };
+      produce<NS, BATCH>(it, 1, full, empty, meta, step_of, [&](int s, int g, int x0, int y0,
+                                                                 int k) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
         unsigned char *st = smem + s * ST;
         proxy_fence();
@@ -460,10 +492,10 @@ __global__ void __launch_bounds__(NT, 3)
       if (it.err) atomicExch(it.err, 2);
       return;
     }
-    const int4 m = meta[s];
+    const int4 m = meta[2 * s];
     if (m.x < 0) return;  // sentinel
-    int g, x0, y0, kb, np;
-    decode_item<BATCH>(it, m.x, g, x0, y0, kb, np);
+    const int4 m1 = meta[2 * s + 1];
+    const int x0 = m1.y, y0 = m1.z, kb = m.w, np = m.z;
     // the item's descriptor and op: the first load's copies (every load of
     // the item carries the same ones)
     const unsigned char *st_item = smem + s * ST;
@@ -472,8 +504,7 @@ __global__ void __launch_bounds__(NT, 3)
         BATCH ? *reinterpret_cast<const fdtd_op *>(st_item + H_STAGE + DESC_B) : op0;
     const int I = d.I, J = d.J, K = d.K, p = d.p;
     const int mode = op.tfsf_mode;
-    const float *inc =
-        mode ? inc_h_row(d, mode, BATCH ? it.steps[g] + op.step : op_step(d, op)) : nullptr;
+    const float *inc = mode ? inc_h_row(d, mode, m1.w) : nullptr;
     const float Chh = d.Chh, Che = d.Che;
     const int i = x0 + xo;
     const int px = PML ? slab_h(i, I, p) : -1;
