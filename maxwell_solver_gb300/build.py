@@ -63,7 +63,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(obj)
         jobs.append([nvcc, ARCH, "-lineinfo", "-O3", "--fmad=false", "-std=c++17",
                      "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",
-                     *inc, "-c", src, "-o", obj])
+                     *inc, *os.environ.get("FDTD_NVCC_DEFINES", "").split(),
+                     "-c", src, "-o", obj])
     for src in c:
         obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
         objs.append(obj)

@@ -19,6 +19,10 @@ namespace fdtd {
 
 __device__ __forceinline__ bool in_range(int v, int lo, int hi) { return v >= lo && v <= hi; }
 
+__device__ __forceinline__ float2 *psi_pairs(const fdtd_dev &d, int a) {
+  return reinterpret_cast<float2 *>(d.psi[a]);
+}
+
 // Slab position of index v in a CPML of thickness p on an axis of length n.
 // H cells: low side [0,p) -> v, high side [n-p, n-2] -> v-n+2p
 // (src/gpu.h:615-617, :654-656, :698-700).
@@ -215,51 +219,39 @@ __device__ __forceinline__ void update_h_cell(const fdtd_dev &d, int mode, const
   }
   if (mode) tfsf_h(d, mode, inc, i, j, k, hx, hy, hz);
   if (PML) {
-    // Each psi entry belongs to one cell, so all of the cell's psi loads are
-    // issued before its first psi store: one memory round trip, not six.
+    // Each psi pair belongs to one cell, so all of the cell's pairs are
+    // loaded before its first psi store: one memory round trip.
     const int64_t I = d.I, J = d.J, pj = 2 * (int64_t)d.p;
-    const int64_t ty = i + py * I + k * pj * I;
-    const int64_t tx = px + j * pj + k * pj * J;
-    const int64_t tz = i + j * I + pz * d.IJ;
-    float y0 = 0.f, y1 = 0.f, x0 = 0.f, x1 = 0.f, z0 = 0.f, z1 = 0.f;
-    if (py >= 0) {
-      y0 = d.psi[PSI_HXY][ty];
-      y1 = d.psi[PSI_HZY][ty];
-    }
-    if (px >= 0) {
-      x0 = d.psi[PSI_HYX][tx];
-      x1 = d.psi[PSI_HZX][tx];
-    }
-    if (pz >= 0) {
-      z0 = d.psi[PSI_HXZ][tz];
-      z1 = d.psi[PSI_HYZ][tz];
-    }
-    if (py >= 0) {
+    float2 *Y = psi_pairs(d, PSI_HY) + (i + py * I + k * pj * I);
+    float2 *X = psi_pairs(d, PSI_HX) + (px + j * pj + k * pj * J);
+    float2 *Z = psi_pairs(d, PSI_HZ) + (i + j * I + pz * d.IJ);
+    float2 y = make_float2(0.f, 0.f), x = y, z = y;
+    if (py >= 0) y = *Y;
+    if (px >= 0) x = *X;
+    if (pz >= 0) z = *Z;
+    if (py >= 0) {  // {psi_Hxy, psi_Hzy}
       const float b = d.bH[py], c = d.cH[py];
-      float v = b * y0 + c * dEz_y / dx;
-      d.psi[PSI_HXY][ty] = v;
-      hx = hx - Che * v * dx;
-      v = b * y1 + c * dEx_y / dx;
-      d.psi[PSI_HZY][ty] = v;
-      hz = hz + Che * v * dx;
+      const float v0 = b * y.x + c * dEz_y / dx;
+      hx = hx - Che * v0 * dx;
+      const float v1 = b * y.y + c * dEx_y / dx;
+      hz = hz + Che * v1 * dx;
+      *Y = make_float2(v0, v1);
     }
-    if (px >= 0) {
+    if (px >= 0) {  // {psi_Hyx, psi_Hzx}
       const float b = d.bH[px], c = d.cH[px];
-      float v = b * x0 + c * dEz_x / dx;
-      d.psi[PSI_HYX][tx] = v;
-      hy = hy + Che * v * dx;
-      v = b * x1 + c * dEy_x / dx;
-      d.psi[PSI_HZX][tx] = v;
-      hz = hz - Che * v * dx;
+      const float v0 = b * x.x + c * dEz_x / dx;
+      hy = hy + Che * v0 * dx;
+      const float v1 = b * x.y + c * dEy_x / dx;
+      hz = hz - Che * v1 * dx;
+      *X = make_float2(v0, v1);
     }
-    if (pz >= 0) {
+    if (pz >= 0) {  // {psi_Hxz, psi_Hyz}
       const float b = d.bH[pz], c = d.cH[pz];
-      float v = b * z0 + c * dEy_z / dx;
-      d.psi[PSI_HXZ][tz] = v;
-      hx = hx + Che * v * dx;
-      v = b * z1 + c * dEx_z / dx;
-      d.psi[PSI_HYZ][tz] = v;
-      hy = hy - Che * v * dx;
+      const float v0 = b * z.x + c * dEy_z / dx;
+      hx = hx + Che * v0 * dx;
+      const float v1 = b * z.y + c * dEx_z / dx;
+      hy = hy - Che * v1 * dx;
+      *Z = make_float2(v0, v1);
     }
   }
 }
@@ -295,50 +287,38 @@ __device__ __forceinline__ void update_e_cell(const fdtd_dev &d, int mode, const
   }
   if (mode) tfsf_e(d, mode, inc, i, j, k, C.exh, C.eyh, C.ezh, ex, ey, ez);
   if (PML) {
-    // all psi loads of the cell first (see update_h_cell)
+    // all psi pairs of the cell first (see update_h_cell)
     const int64_t I = d.I, J = d.J, pj = 2 * (int64_t)d.p;
-    const int64_t ty = i + py * I + k * pj * I;
-    const int64_t tz = i + j * I + pz * d.IJ;
-    const int64_t tx = px + j * pj + k * pj * J;
-    float y0 = 0.f, y1 = 0.f, z0 = 0.f, z1 = 0.f, x0 = 0.f, x1 = 0.f;
-    if (py >= 0) {
-      y0 = d.psi[PSI_EXY][ty];
-      y1 = d.psi[PSI_EZY][ty];
-    }
-    if (pz >= 0) {
-      z0 = d.psi[PSI_EXZ][tz];
-      z1 = d.psi[PSI_EYZ][tz];
-    }
-    if (px >= 0) {
-      x0 = d.psi[PSI_EYX][tx];
-      x1 = d.psi[PSI_EZX][tx];
-    }
-    if (py >= 0) {
+    float2 *Y = psi_pairs(d, PSI_EY) + (i + py * I + k * pj * I);
+    float2 *Z = psi_pairs(d, PSI_EZ) + (i + j * I + pz * d.IJ);
+    float2 *X = psi_pairs(d, PSI_EX) + (px + j * pj + k * pj * J);
+    float2 y = make_float2(0.f, 0.f), z = y, x = y;
+    if (py >= 0) y = *Y;
+    if (pz >= 0) z = *Z;
+    if (px >= 0) x = *X;
+    if (py >= 0) {  // {psi_Exy, psi_Ezy}
       const float b = d.bE[py], c = d.cE[py];
-      float v = b * y0 + c * (hz - hz_jm) / dx;
-      d.psi[PSI_EXY][ty] = v;
-      ex = ex + C.exh * v * dx;
-      v = b * y1 + c * (hx - hx_jm) / dx;
-      d.psi[PSI_EZY][ty] = v;
-      ez = ez - C.ezh * v * dx;
+      const float v0 = b * y.x + c * (hz - hz_jm) / dx;
+      ex = ex + C.exh * v0 * dx;
+      const float v1 = b * y.y + c * (hx - hx_jm) / dx;
+      ez = ez - C.ezh * v1 * dx;
+      *Y = make_float2(v0, v1);
     }
-    if (pz >= 0) {
+    if (pz >= 0) {  // {psi_Exz, psi_Eyz}
       const float b = d.bE[pz], c = d.cE[pz];
-      float v = b * z0 + c * (hy - hy_km) / dx;
-      d.psi[PSI_EXZ][tz] = v;
-      ex = ex - C.exh * v * dx;
-      v = b * z1 + c * (hx - hx_km) / dx;
-      d.psi[PSI_EYZ][tz] = v;
-      ey = ey + C.eyh * v * dx;
+      const float v0 = b * z.x + c * (hy - hy_km) / dx;
+      ex = ex - C.exh * v0 * dx;
+      const float v1 = b * z.y + c * (hx - hx_km) / dx;
+      ey = ey + C.eyh * v1 * dx;
+      *Z = make_float2(v0, v1);
     }
-    if (px >= 0) {
+    if (px >= 0) {  // {psi_Eyx, psi_Ezx}
       const float b = d.bE[px], c = d.cE[px];
-      float v = b * x0 + c * (hz - hz_im) / dx;
-      d.psi[PSI_EYX][tx] = v;
-      ey = ey - C.eyh * v * dx;
-      v = b * x1 + c * (hy - hy_im) / dx;
-      d.psi[PSI_EZX][tx] = v;
-      ez = ez + C.ezh * v * dx;
+      const float v0 = b * x.x + c * (hz - hz_im) / dx;
+      ey = ey - C.eyh * v0 * dx;
+      const float v1 = b * x.y + c * (hy - hy_im) / dx;
+      ez = ez + C.ezh * v1 * dx;
+      *X = make_float2(v0, v1);
     }
   }
   if (cur) {  // E -= Ce?h * source * dx / dx / dx

@@ -754,11 +754,10 @@ int fdtd_ready_simulation(fdtd_handle h) {
   }
   if ((rc = dalloc(s, (void **)&s->d_err, sizeof(int32_t)))) return rc;
   CU(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream));
+  /* floats per pair array: 2 slabs of size_* cells, 2 values per cell */
   const int64_t psi_n[FDTD_NUM_PSI] = {
-      [PSI_EXY] = 2 * s->size_y, [PSI_EZY] = 2 * s->size_y, [PSI_HXY] = 2 * s->size_y,
-      [PSI_HZY] = 2 * s->size_y, [PSI_EXZ] = 2 * s->size_z, [PSI_EYZ] = 2 * s->size_z,
-      [PSI_HXZ] = 2 * s->size_z, [PSI_HYZ] = 2 * s->size_z, [PSI_EYX] = 2 * s->size_x,
-      [PSI_EZX] = 2 * s->size_x, [PSI_HYX] = 2 * s->size_x, [PSI_HZX] = 2 * s->size_x};
+      [PSI_EY] = 4 * s->size_y, [PSI_HY] = 4 * s->size_y, [PSI_EZ] = 4 * s->size_z,
+      [PSI_HZ] = 4 * s->size_z, [PSI_EX] = 4 * s->size_x, [PSI_HX] = 4 * s->size_x};
   int64_t psi_total = 0;
   for (int a = 0; a < FDTD_NUM_PSI; ++a) psi_total += psi_n[a];
   if ((rc = dalloc(s, (void **)&s->d_psi_pool, (size_t)psi_total * sizeof(float)))) return rc;

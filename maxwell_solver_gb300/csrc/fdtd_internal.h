@@ -16,12 +16,20 @@ extern "C" {
 #endif
 
 #define FDTD_MAX_PML 32
-#define FDTD_NUM_PSI 12
+#define FDTD_NUM_PSI 6
 
-/* psi slots (one per field component x CPML axis) */
+/* CPML psi arrays: one per (field family, CPML axis), each storing the two
+ * recurrences that share a slab index as an interleaved pair {first,
+ * second}, so that a cell reads and writes both with one 8-byte access.
+ * The reference keeps them as twelve separate arrays (src/simulation.h);
+ * the values and their slab indexing are the same. */
 enum {
-  PSI_EXY = 0, PSI_EXZ, PSI_EYX, PSI_EYZ, PSI_EZX, PSI_EZY,
-  PSI_HXY, PSI_HXZ, PSI_HYX, PSI_HYZ, PSI_HZX, PSI_HZY
+  PSI_EY = 0, /* {psi_Exy, psi_Ezy}, index i + py*I + k*2p*I */
+  PSI_EZ,     /* {psi_Exz, psi_Eyz}, index i + j*I + pz*I*J   */
+  PSI_EX,     /* {psi_Eyx, psi_Ezx}, index px + j*2p + k*2p*J */
+  PSI_HY,     /* {psi_Hxy, psi_Hzy} */
+  PSI_HX,     /* {psi_Hyx, psi_Hzx} */
+  PSI_HZ      /* {psi_Hxz, psi_Hyz} */
 };
 
 /* Everything a kernel needs to know about one grid (by value).
@@ -46,7 +54,7 @@ typedef struct {
   const uint16_t *mat;      /* coef_mode 1: coefficient-tuple id per cell */
   const float *mat_tab;     /* coef_mode 1: [n][6] Cexe..Cezh per id */
   int32_t n_mat;            /* coef_mode 1: number of ids */
-  float *psi[FDTD_NUM_PSI];
+  float *psi[FDTD_NUM_PSI];  /* pairs: [slab cells][2] */
   const float *inc[4];      /* Ez_1D, Hy_1D, E_inv_1D, H_inv_1D: [T][size1d] */
   const float *src;         /* current-source waveform [T] */
   int32_t *step_base;       /* device step base for graph-replayed steps */

@@ -50,6 +50,16 @@ constexpr int BX = 64, BY = 8;
 constexpr int NCW = 8;                       // consumer warps
 constexpr int NT = (NCW + 1) * 32;           // + one producer warp
 constexpr int NSE = 4, NSH = 5;              // ring stages (E, H)
+// Batch kernels: resident blocks per SM the register budget is sized for,
+// and their ring depth (build-time tunables).
+#ifndef FDTD_BATCH_MIN_BLOCKS
+#define FDTD_BATCH_MIN_BLOCKS 3
+#endif
+#ifndef FDTD_BATCH_NS
+#define FDTD_BATCH_NS 4
+#endif
+constexpr int kBatchMinBlocks = FDTD_BATCH_MIN_BLOCKS;
+constexpr int kBatchNS = FDTD_BATCH_NS;
 constexpr int HW = BX + 4;                   // halo box row (floats)
 constexpr int HH = BY + 1;                   // halo box rows
 constexpr int TILE_B = BX * BY * 4;          // 2048 B
@@ -62,7 +72,7 @@ constexpr int E_STAGE = E_OFF_M + MAT_B;     // 14848 B
 constexpr int H_OFF_H = 3 * HALO_SLOT;
 constexpr int H_STAGE = H_OFF_H + 3 * TILE_B;  // 13824 B
 constexpr int kSmemTabMax = 512;             // coefficient ids staged in shared memory
-constexpr int CTRL_B = 256;                  // barriers + stage metadata
+constexpr int CTRL_B = 512;                  // barriers + stage metadata
 // Batch mode: every stage also carries its grid's descriptor and op (bulk
 // copies completing on the stage's barrier), so the per-cell code reads
 // them from shared memory instead of global memory; E stages also carry
@@ -75,26 +85,29 @@ static_assert(sizeof(fdtd_dev) <= DESC_B && sizeof(fdtd_dev) % 16 == 0, "descrip
 static_assert(sizeof(fdtd_op) <= OPSLOT_B && sizeof(fdtd_op) % 16 == 0, "op slot");
 template <bool BATCH>
 struct EG {
-  static constexpr int NS = NSE;
+  static constexpr int NS = BATCH ? kBatchNS : NSE;
   static constexpr int STAGE = BATCH ? E_STAGE + DESC_B + OPSLOT_B + TAB_B : E_STAGE;
   static constexpr int SMEM = NS * STAGE + CTRL_B + (BATCH ? 0 : kSmemTabMax * 6 * 4);
 };
 template <bool BATCH>
 struct HG {
-  static constexpr int NS = BATCH ? 4 : NSH;
+  static constexpr int NS = BATCH ? kBatchNS : NSH;
   static constexpr int STAGE = BATCH ? H_STAGE + DESC_B + OPSLOT_B : H_STAGE;
   static constexpr int SMEM = NS * STAGE + CTRL_B;
 };
 constexpr int E_SMEM = EG<false>::SMEM;
 constexpr int H_SMEM = HG<false>::SMEM;
 static_assert(EG<true>::STAGE % 128 == 0 && HG<true>::STAGE % 128 == 0, "batch stage alignment");
-static_assert(3 * (EG<true>::SMEM + 1024) <= 228 * 1024 && 3 * (HG<true>::SMEM + 1024) <= 228 * 1024,
-              "three batch blocks per SM");
+static_assert(kBatchMinBlocks * (EG<true>::SMEM + 1024) <= 228 * 1024 &&
+                  kBatchMinBlocks * (HG<true>::SMEM + 1024) <= 228 * 1024,
+              "batch blocks per SM");
 constexpr unsigned kSpinLimit = 1u << 22;    // bounded mbarrier waits
 static_assert(E_STAGE % 128 == 0 && H_STAGE % 128 == 0, "stage alignment");
 static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
               "TMA inner box extents must be multiples of 16 bytes");
-static_assert(NSH * (8 + 8 + 32) <= CTRL_B && NSE * (8 + 8 + 32) <= CTRL_B, "control block");
+static_assert(NSH * (8 + 8 + 32) <= CTRL_B && NSE * (8 + 8 + 32) <= CTRL_B &&
+                  kBatchNS * (8 + 8 + 32) <= CTRL_B,
+              "control block");
 
 struct Maps {
   CUtensorMap m[FDTD_NUM_MAPS];
@@ -250,21 +263,22 @@ __device__ __forceinline__ void cell_map(int tid, int &xo, int &r0) {
 // ----------------------------------------------------------------- E half
 
 template <bool PML, bool BATCH>
-__global__ void __launch_bounds__(NT, 3)
+__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
     k_half_e_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int ST = EG<BATCH>::STAGE;
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSE * ST);
-  uint64_t *empty = full + NSE;
-  int4 *meta = reinterpret_cast<int4 *>(empty + NSE);
-  float *stab = reinterpret_cast<float *>(smem + NSE * ST + CTRL_B);
+  constexpr int NS = EG<BATCH>::NS;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * ST);
+  uint64_t *empty = full + NS;
+  int4 *meta = reinterpret_cast<int4 *>(empty + NS);
+  float *stab = reinterpret_cast<float *>(smem + NS * ST + CTRL_B);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // single grid: the coefficient table (if small) lives in shared memory
   const bool tab_in_smem = !BATCH && d0.coef_mode == 1 && d0.n_mat <= kSmemTabMax;
 
   if (tid == 0) {
-    for (int s = 0; s < NSE; ++s) {
+    for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], NCW);
     }
@@ -283,7 +297,7 @@ __global__ void __launch_bounds__(NT, 3)
       const auto step_of = [&](int g) {
         return (BATCH ? it.steps[g] + it.ops[g].step : op_step(d0, op0));
       };
-      produce<NSE, BATCH>(it, 0, full, empty, meta, step_of, [&](int s, int g, int x0, int y0,
+      produce<NS, BATCH>(it, 0, full, empty, meta, step_of, [&](int s, int g, int x0, int y0,
                                                                   int k) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
         if (BATCH && g != g_um) {
@@ -327,8 +341,8 @@ __global__ void __launch_bounds__(NT, 3)
   int64_t n0[2] = {0, 0};
 
   for (int q = 0;; ++q) {
-    const int s = q % NSE;
-    if (!mbar_wait(&full[s], (uint32_t)((q / NSE) & 1))) {
+    const int s = q % NS;
+    if (!mbar_wait(&full[s], (uint32_t)((q / NS) & 1))) {
       if (it.err) atomicExch(it.err, 1);
       return;
     }
@@ -413,6 +427,7 @@ __global__ void __launch_bounds__(NT, 3)
           update_e_cell<true, PML>(d, mode, inc, cm, cur_src, cur, i, j, k, px, py, pz, C, ex,
                                    ey, ez, hx, hy, hz, hz_jm, hx_jm, hz_im, hy_im, hx_km[c],
                                    hy_km[c]);
+          // the next plane's psi pairs into L2 while this plane finishes
         }
       } else {  // interior warp: i, j, k >= 1, no CPML, TF/SF face or source
         ex = C.exe * ex + C.exh * (+(hz - hz_jm) - (hy - hy_km[c]));
@@ -435,7 +450,7 @@ __global__ void __launch_bounds__(NT, 3)
 // ----------------------------------------------------------------- H half
 
 template <bool PML, bool BATCH>
-__global__ void __launch_bounds__(NT, 3)
+__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -557,9 +572,10 @@ __global__ void __launch_bounds__(NT, 3)
         const float dEy_z = sEy1[eb] - ey, dEx_z = sEx1[eb] - ex;
         float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
         if (__any_sync(0xffffffffu, act && (col_special[c] || plane_special))) {
-          if (act)
+          if (act) {
             update_h_cell<true, PML>(dp, mode, inc, i, y0 + ty, k, px, py[c], pz, hx, hy, hz,
                                      dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z);
+          }
         } else {
           hx = Chh * hx + Che * (-dEz_y + dEy_z);
           hy = Chh * hy + Che * (-dEx_z + dEz_x);
