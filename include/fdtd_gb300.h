@@ -255,6 +255,21 @@ int fdtd_index_coefficients_static(const float *const ce[6], int32_t I, int32_t 
                                    int32_t pitch, uint16_t *ids, float *table, int32_t max_ids,
                                    int32_t *n_ids, void *stream);
 
+/* The plan the kernels use for the CPML recurrences' division by the cell
+ * size (no reference counterpart; the reference divides): out[0] =
+ * RN(1/dx); for numerators a with out[1] <= |a| < out[2] the quotient is
+ * RN(a*out[0]) corrected by one fused multiply-add step, which the library
+ * has checked to equal the IEEE quotient a/dx for every such a; for
+ * out[3] <= |a| < out[1] the same is done on a*2^64 and scaled back; zero
+ * and other numerators are exact or divided.  Host only. */
+int fdtd_division_plan(float dx, float out[4]);
+
+/* Evaluates that plan on the current GPU for every float bit pattern as a
+ * numerator (2^32 inputs, about a second) and stores in *mismatches the
+ * number whose quotient differs bitwise from the GPU's IEEE division a/dx
+ * (no reference counterpart: a self-check). */
+int fdtd_check_division(float dx, uint64_t *mismatches);
+
 /* Number of kernels this library has launched (all handles). */
 uint64_t fdtd_launch_count(void);
 

@@ -84,6 +84,8 @@ SIGNATURES = {
     "fdtd_batch_run": (ctypes.c_int, [U64]),
     "fdtd_batch_clear": (ctypes.c_int, [U64]),
     "fdtd_batch_progress": (ctypes.c_int, [U64, U64, ctypes.POINTER(I32)]),
+    "fdtd_division_plan": (ctypes.c_int, [ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
+    "fdtd_check_division": (ctypes.c_int, [ctypes.c_float, ctypes.POINTER(ctypes.c_uint64)]),
     "fdtd_launch_count": (ctypes.c_uint64, []),
     "fdtd_last_error": (ctypes.c_char_p, []),
     "fdtd_create_signal": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double,

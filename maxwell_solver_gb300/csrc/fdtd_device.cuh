@@ -19,6 +19,37 @@ namespace fdtd {
 
 __device__ __forceinline__ bool in_range(int v, int lo, int hi) { return v >= lo && v <= hi; }
 
+// IEEE quotient a / b, kept out of line of the fast paths below (an asm
+// statement is never evaluated speculatively).
+__device__ __forceinline__ float div_ieee(float a, float b) {
+  float q;
+  asm volatile("div.rn.f32 %0, %1, %2;" : "=f"(q) : "f"(a), "f"(b));
+  return q;
+}
+
+// RN(a / b) for a fixed divisor b with y = RN(1/b): one rounded product and
+// Markstein's correction step, q0 = RN(a*y), r = RN(a - b*q0),
+// q = RN(q0 + r*y), which the host has shown equal to the IEEE quotient
+// for lo <= |a| < hi (fdtd_make_div_plan).  For lo2 <= |a| < lo the same
+// is done on a*2^64 and the result scaled back by 2^-64: both scalings are
+// exact (the quotient is normal there).  A zero numerator gives a*y = +-0
+// = a/b; the rest (tiny, huge, inf, NaN) is divided.
+__device__ __forceinline__ float div_by(float a, float b, float y, float lo, float hi,
+                                        float lo2) {
+  const float aa = fabsf(a);
+  const bool small = aa < lo;
+  const float as = a * (small ? 0x1p64f : 1.0f);
+  const float q0 = as * y;
+  const float q = __fmaf_rn(__fmaf_rn(-q0, b, as), y, q0) * (small ? 0x1p-64f : 1.0f);
+  if (aa >= lo2 && aa < hi) return q;
+  if (aa == 0.f) return a * y;
+  return div_ieee(a, b);
+}
+// RN(a / dx): the CPML recurrences' c * difference / dx.
+__device__ __forceinline__ float div_dx(const fdtd_dev &d, float a) {
+  return div_by(a, d.dx, d.rdx, d.div_lo, d.div_hi, d.div_lo2);
+}
+
 __device__ __forceinline__ float2 *psi_pairs(const fdtd_dev &d, int a) {
   return reinterpret_cast<float2 *>(d.psi[a]);
 }
@@ -231,25 +262,25 @@ __device__ __forceinline__ void update_h_cell(const fdtd_dev &d, int mode, const
     if (pz >= 0) z = *Z;
     if (py >= 0) {  // {psi_Hxy, psi_Hzy}
       const float b = d.bH[py], c = d.cH[py];
-      const float v0 = b * y.x + c * dEz_y / dx;
+      const float v0 = b * y.x + div_dx(d, c * dEz_y);
       hx = hx - Che * v0 * dx;
-      const float v1 = b * y.y + c * dEx_y / dx;
+      const float v1 = b * y.y + div_dx(d, c * dEx_y);
       hz = hz + Che * v1 * dx;
       *Y = make_float2(v0, v1);
     }
     if (px >= 0) {  // {psi_Hyx, psi_Hzx}
       const float b = d.bH[px], c = d.cH[px];
-      const float v0 = b * x.x + c * dEz_x / dx;
+      const float v0 = b * x.x + div_dx(d, c * dEz_x);
       hy = hy + Che * v0 * dx;
-      const float v1 = b * x.y + c * dEy_x / dx;
+      const float v1 = b * x.y + div_dx(d, c * dEy_x);
       hz = hz - Che * v1 * dx;
       *X = make_float2(v0, v1);
     }
     if (pz >= 0) {  // {psi_Hxz, psi_Hyz}
       const float b = d.bH[pz], c = d.cH[pz];
-      const float v0 = b * z.x + c * dEy_z / dx;
+      const float v0 = b * z.x + div_dx(d, c * dEy_z);
       hx = hx + Che * v0 * dx;
-      const float v1 = b * z.y + c * dEx_z / dx;
+      const float v1 = b * z.y + div_dx(d, c * dEx_z);
       hy = hy - Che * v1 * dx;
       *Z = make_float2(v0, v1);
     }
@@ -298,25 +329,25 @@ __device__ __forceinline__ void update_e_cell(const fdtd_dev &d, int mode, const
     if (px >= 0) x = *X;
     if (py >= 0) {  // {psi_Exy, psi_Ezy}
       const float b = d.bE[py], c = d.cE[py];
-      const float v0 = b * y.x + c * (hz - hz_jm) / dx;
+      const float v0 = b * y.x + div_dx(d, c * (hz - hz_jm));
       ex = ex + C.exh * v0 * dx;
-      const float v1 = b * y.y + c * (hx - hx_jm) / dx;
+      const float v1 = b * y.y + div_dx(d, c * (hx - hx_jm));
       ez = ez - C.ezh * v1 * dx;
       *Y = make_float2(v0, v1);
     }
     if (pz >= 0) {  // {psi_Exz, psi_Eyz}
       const float b = d.bE[pz], c = d.cE[pz];
-      const float v0 = b * z.x + c * (hy - hy_km) / dx;
+      const float v0 = b * z.x + div_dx(d, c * (hy - hy_km));
       ex = ex - C.exh * v0 * dx;
-      const float v1 = b * z.y + c * (hx - hx_km) / dx;
+      const float v1 = b * z.y + div_dx(d, c * (hx - hx_km));
       ey = ey + C.eyh * v1 * dx;
       *Z = make_float2(v0, v1);
     }
     if (px >= 0) {  // {psi_Eyx, psi_Ezx}
       const float b = d.bE[px], c = d.cE[px];
-      const float v0 = b * x.x + c * (hz - hz_im) / dx;
+      const float v0 = b * x.x + div_dx(d, c * (hz - hz_im));
       ey = ey - C.eyh * v0 * dx;
-      const float v1 = b * x.y + c * (hy - hy_im) / dx;
+      const float v1 = b * x.y + div_dx(d, c * (hy - hy_im));
       ez = ez + C.ezh * v1 * dx;
       *X = make_float2(v0, v1);
     }

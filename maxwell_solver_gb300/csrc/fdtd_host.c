@@ -149,6 +149,97 @@ static sim *lookup(fdtd_handle h) {
   sim *s = lookup(h);                                                      \
   if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "invalid simulation handle")
 
+/* ------------------------------------------------------------------
+ * Division by the cell size.  The CPML recurrences divide by dx (12 times
+ * in a corner cell); the kernels do it as a multiplication by y = RN(1/dx)
+ * plus Markstein's correction step (P. Markstein, IBM J. Res. Dev. 34(1),
+ * 1990; P. Cornea, J. Harrison, P. Tang, ARITH 14, 1999):
+ * q0 = RN(a*y), r = RN(a - dx*q0), q = RN(q0 + r*y), one multiply and two
+ * fused multiply-adds.  The plan says where that equals the IEEE quotient
+ * RN(a/dx) bit for bit:
+ *   - every significand of a in [1, 2) (2^23 values) is checked here
+ *     against float division;
+ *   - multiplying a by 2^e multiplies q0, r and q by 2^e with the same
+ *     roundings as long as none of them (nor a/dx) leaves the normal
+ *     range, so the check holds for every |a| in [lo, hi), the range where
+ *     a*y and each nonzero r of the check, scaled, stay normal.
+ * If any significand fails, lo = inf and every nonzero quotient is an
+ * actual division.  Plans are cached per dx (grids share their cell size).
+ * ------------------------------------------------------------------ */
+static float f32_from_bits(uint32_t u) {
+  float f;
+  memcpy(&f, &u, sizeof(f));
+  return f;
+}
+
+static fdtd_div_plan div_plan_compute(float dx) {
+  fdtd_div_plan p = {dx, 1.0f / dx, INFINITY, 0.0f, INFINITY};
+  if (!isnormal(dx) || !(dx > 0.0f)) return p;
+  const float y = (float)(1.0 / (double)dx);
+  if (!isnormal(y)) return p;
+  float rmin = INFINITY; /* smallest nonzero |r| of the check */
+  for (uint32_t m = 0; m < (1u << 23); ++m) {
+    const float a = f32_from_bits(0x3F800000u | m);
+    const float q0 = a * y;
+    const float r = fmaf(-q0, dx, a);
+    const float q = fmaf(r, y, q0);
+    if (q != a / dx) return p;
+    const float ar = fabsf(r);
+    if (ar != 0.0f && ar < rmin) rmin = ar;
+  }
+  /* a = m * 2^e, m in [1, 2): need y*2^e >= 2^-126, rmin*2^e >= 2^-126 and
+   * 2y*2^e < 2^127 (q0, q and a/dx are within an ulp of a*y); one binade
+   * of margin on each side. */
+  int ey, er;
+  frexpf(y, &ey); /* y in [2^(ey-1), 2^ey) */
+  int e_min = -125 - ey + 1;
+  if (rmin != INFINITY) {
+    frexpf(rmin, &er);
+    if (-125 - er + 1 > e_min) e_min = -125 - er + 1;
+  }
+  int e_max = 126 - ey - 1;
+  if (e_max > 125) e_max = 125;
+  if (e_min < -125) e_min = -125;
+  if (e_min > e_max) return p;
+  p.rdx = y;
+  p.lo = ldexpf(1.0f, e_min);
+  p.hi = ldexpf(1.0f, e_max + 1);
+  /* below lo: scale by 2^64 into [lo, hi), which needs |a| >= lo*2^-64 and
+   * 2^64*lo <= hi; the scaled-back quotient is exact while it is normal,
+   * |a/dx| >= 2^-126: |a| >= 2^-125*dx with one binade of margin */
+  if (ldexpf(p.lo, 64) <= p.hi) {
+    const float l1 = ldexpf(p.lo, -64), l2 = ldexpf(dx, -125);
+    p.lo2 = l1 > l2 ? l1 : l2;
+    if (!(p.lo2 < p.lo)) p.lo2 = p.lo;
+  } else {
+    p.lo2 = p.lo;
+  }
+  return p;
+}
+
+#define DIV_CACHE 8
+static pthread_mutex_t g_div_lock = PTHREAD_MUTEX_INITIALIZER;
+static fdtd_div_plan g_div_cache[DIV_CACHE];
+static int g_div_used = 0, g_div_next = 0;
+
+fdtd_div_plan fdtd_make_div_plan(float dx) {
+  pthread_mutex_lock(&g_div_lock);
+  for (int i = 0; i < g_div_used; ++i)
+    if (memcmp(&g_div_cache[i].dx, &dx, sizeof(dx)) == 0) {
+      const fdtd_div_plan p = g_div_cache[i];
+      pthread_mutex_unlock(&g_div_lock);
+      return p;
+    }
+  pthread_mutex_unlock(&g_div_lock);
+  const fdtd_div_plan p = div_plan_compute(dx); /* ~50 ms, outside the lock */
+  pthread_mutex_lock(&g_div_lock);
+  g_div_cache[g_div_next] = p; /* round robin */
+  g_div_next = (g_div_next + 1) % DIV_CACHE;
+  if (g_div_used < DIV_CACHE) ++g_div_used;
+  pthread_mutex_unlock(&g_div_lock);
+  return p;
+}
+
 uint64_t fdtd_launch_count(void) {
   return (uint64_t)(fdtdk_launch_count() - g_captured_kernels + g_graph_kernels);
 }
@@ -482,6 +573,13 @@ static void fill_dev_struct(sim *s) {
   d->Chh = s->Chh;
   d->Che = s->Che;
   d->dx = s->delX;
+  {
+    const fdtd_div_plan dp = fdtd_make_div_plan(s->delX);
+    d->rdx = dp.rdx;
+    d->div_lo = dp.lo;
+    d->div_hi = dp.hi;
+    d->div_lo2 = dp.lo2;
+  }
   memcpy(d->bE, s->bE, sizeof(d->bE));
   memcpy(d->cE, s->cE, sizeof(d->cE));
   memcpy(d->bH, s->bH, sizeof(d->bH));
@@ -1208,6 +1306,31 @@ int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t mode
 int fdtd_set_device(int32_t device) {
   CU(cudaSetDevice(device));
   return FDTD_OK;
+}
+
+int fdtd_division_plan(float dx, float out[4]) {
+  if (!out) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  const fdtd_div_plan p = fdtd_make_div_plan(dx);
+  out[0] = p.rdx;
+  out[1] = p.lo;
+  out[2] = p.hi;
+  out[3] = p.lo2;
+  return FDTD_OK;
+}
+
+int fdtd_check_division(float dx, uint64_t *mismatches) {
+  if (!mismatches) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  const fdtd_div_plan p = fdtd_make_div_plan(dx);
+  unsigned long long *d_bad = NULL, bad = 0;
+  CU(cudaMalloc((void **)&d_bad, sizeof(*d_bad)));
+  int rc = FDTD_OK;
+  if (cudaMemset(d_bad, 0, sizeof(*d_bad)) != cudaSuccess ||
+      fdtdk_check_division(p, 0, 1ull << 32, d_bad, 0) != 0 ||
+      cudaMemcpy(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = fail(FDTD_ERR_CUDA, "division check: %s", cudaGetErrorString(cudaGetLastError()));
+  cudaFree(d_bad);
+  if (rc == FDTD_OK) *mismatches = (uint64_t)bad;
+  return rc;
 }
 
 /* ------------------------------------------------------------ outputs */

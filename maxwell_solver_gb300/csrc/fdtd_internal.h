@@ -46,6 +46,10 @@ typedef struct {
   int32_t i0, i1, j0, j1, k0, k1;   /* TF/SF box */
   int32_t size1d, T;
   float Chh, Che, dx;
+  /* quotient x/dx: see fdtd_make_div_plan (rdx = RN(1/dx); the corrected
+   * product is used for div_lo <= |x| < div_hi, and on x*2^64 for
+   * div_lo2 <= |x| < div_lo) */
+  float rdx, div_lo, div_hi, div_lo2;
   float bE[2 * FDTD_MAX_PML], cE[2 * FDTD_MAX_PML];
   float bH[2 * FDTD_MAX_PML], cH[2 * FDTD_MAX_PML];
   float *f[6];              /* Ex Ey Ez Hx Hy Hz, x-fastest IJK each */
@@ -148,6 +152,17 @@ unsigned long long fdtdk_launch_count(void);
 /* Records an error message for the calling thread (fdtd_last_error) and
  * returns code. */
 int fdtd_internal_fail(int code, const char *msg);
+
+/* Plan for dividing by a fixed cell size (fdtd_host.c). */
+typedef struct {
+  float dx, rdx, lo, hi, lo2;
+} fdtd_div_plan;
+fdtd_div_plan fdtd_make_div_plan(float dx);
+/* Adds to *out (device) the number of float bit patterns in
+ * [first, first + count) whose plan quotient differs bitwise from the IEEE
+ * division on the GPU. */
+int fdtdk_check_division(fdtd_div_plan p, uint64_t first, uint64_t count,
+                         unsigned long long *out, cudaStream_t s);
 
 #ifdef __cplusplus
 }

@@ -186,6 +186,23 @@ __global__ void k_batch_advance(int32_t *steps, int n) {
 }
 
 __global__ void k_add_i32(int32_t *p, int32_t v) { *p += v; }
+
+// Self-check of the division plan: over the float bit patterns
+// [first, first + count), counts inputs where fdtd::div_by differs bitwise
+// from the IEEE quotient a / dx computed by this GPU.
+__global__ void k_check_division(fdtd_div_plan p, uint64_t first, uint64_t count,
+                                 unsigned long long *out) {
+  unsigned long long bad = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < count; t += stride) {
+    const float a = __uint_as_float((uint32_t)(first + t));
+    const float q = div_by(a, p.dx, p.rdx, p.lo, p.hi, p.lo2);
+    const float r = a / p.dx;
+    bad += __float_as_uint(q) != __float_as_uint(r);
+  }
+  for (int o = 16; o > 0; o >>= 1) bad += __shfl_xor_sync(0xffffffffu, bad, o);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(out, bad);
+}
 __global__ void k_set_i32(int32_t *p, int32_t v) { *p = v; }
 
 // ------------------------------------------------------ coefficients (setup)
@@ -576,6 +593,16 @@ int fdtdk_init_1d(const fdtd_dev *d, float *tab[4], const float *pw, float Ceh, 
 int fdtdk_batch_probes(const fdtd_dev *devs, int32_t n, cudaStream_t s) {
   if (n <= 0) return 0;
   k_batch_probes<<<n, 256, 0, s>>>(devs, n);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_check_division(fdtd_div_plan p, uint64_t first, uint64_t count,
+                         unsigned long long *out, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_check_division<<<(sms > 0 ? sms : 1) * 8, 256, 0, s>>>(p, first, count, out);
   ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -112,3 +112,47 @@ def test_mex_dispatcher_errors(mex):
     with pytest.raises(MexError) as e:
         mex("UpdateH_All", bogus)
     assert e.value.identifier == "simFDTD:InvalidHandle"
+
+
+def _rn32(x):
+    """Round an exact rational to the nearest float32 (ties to even)."""
+    from fractions import Fraction
+
+    f = np.float32(float(x))  # within one float32 ulp of x
+    cands = [f, np.nextafter(f, np.float32(np.inf)), np.nextafter(f, np.float32(-np.inf))]
+    best = min(cands, key=lambda c: (abs(Fraction(float(c)) - x),
+                                     int(np.array(c).view(np.uint32)) & 1))
+    return best
+
+
+@pytest.mark.parametrize("dx", [1e-3, 3.7e-4, 1.0, 2.0 / 3.0, 12.5])
+def test_division_plan_equals_ieee_quotient(native_lib, dx):
+    """The CPML's division by dx is done as a corrected product inside the
+    plan's ranges; restated here in exact rational arithmetic, it must give
+    RN(a/dx) for numerators drawn across those ranges (the GPU test checks
+    every float)."""
+    from fractions import Fraction
+
+    out = (ctypes.c_float * 4)()
+    assert native_lib.fdtd_division_plan(ctypes.c_float(dx), out) == 0
+    y, lo, hi, lo2 = (np.float32(v) for v in out)
+    b = np.float32(dx)
+    assert y == np.float32(1.0 / float(b))
+    # corrected products cover the fields' range down to quotients near the
+    # smallest normal float
+    assert lo2 <= np.float32(max(1e-38, float(b) * 2.0 ** -123)) and lo <= np.float32(1e-20)
+    assert hi >= np.float32(1e30)
+    rng = np.random.default_rng(7)
+    ex = np.concatenate([rng.uniform(np.log2(float(lo)), np.log2(float(hi)), 300),
+                         rng.uniform(np.log2(float(lo2)), np.log2(float(lo)), 100)])
+    mags = [np.float32(2.0) ** np.float32(e) for e in ex]
+    for a in [np.float32(m * sgn) for m, sgn in zip(mags, rng.choice([-1, 1], len(mags)))]:
+        if not (lo2 <= abs(a) < hi):
+            continue
+        scale = Fraction(2) ** 64 if abs(a) < lo else Fraction(1)
+        A, B, Y = Fraction(float(a)) * scale, Fraction(float(b)), Fraction(float(y))
+        q0 = _rn32(A * Y)
+        r = _rn32(A - B * Fraction(float(q0)))
+        q = np.float32(float(Fraction(float(_rn32(Fraction(float(q0)) + Fraction(float(r)) * Y)))
+                             / scale))
+        assert q == a / b, (a, q, a / b)
