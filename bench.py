@@ -280,6 +280,11 @@ def run_ours(args, ranks):
     if ranks.rank == 0 and not args.no_batch:
         batched = run_batched(args.batch_grids)
 
+    served = None
+    if ranks.rank == 0 and not args.no_serve:
+        served = run_served(args.serve_requests,
+                            [float(x) for x in args.serve_loads.split(",") if x])
+
     cpu = None
     if ranks.rank == 0 and not args.no_cpu:
         rate, done, secs = cpu_oracle_rate(w, target_s=args.cpu_seconds, max_steps=200)
@@ -311,6 +316,7 @@ def run_ours(args, ranks):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "batched": batched,
+        "served": served,
         "clocks": clk,
         "gpu_launches": int(launches),
     }
@@ -445,6 +451,71 @@ def run_batched(n_grids: int, batched_only: bool = False):
     }
 
 
+def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4):
+    """Served configuration c5: a Poisson stream of requests (seeded serve
+    mix, axes log-uniform 48..384, steps 200..4000) through the C request
+    loop with continuous batching under an HBM budget, and the same arrival
+    trace through the one-at-a-time plain-solver queue.  Capacity = the
+    batched solves/s with every request queued at once; each load point
+    offers load x capacity requests per second.  Reports solves/s and
+    p50/p90/p99 latency (arrival to result) of both, and checks every
+    request's probe series is bit-identical in the two."""
+    from maxwell_solver_gb300.serve import Server
+    from maxwell_solver_gb300.workloads import serve_mix
+
+    specs = serve_mix(n_req, seed)
+    budget = int(budget_gb * (1 << 30))
+
+    def one_run(arrivals, one_at_a_time):
+        with Server(hbm_budget=budget, one_at_a_time=one_at_a_time) as srv:
+            t0 = time.perf_counter()
+            tickets = []
+            for spec, at in zip(specs, arrivals):
+                dt = at - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                tickets.append(srv.submit(spec, n_probes=8))
+            res = [srv.result(t) for t in tickets]
+            st = srv.stats()
+        summary = {"solves_per_s": round(st["solves_per_s"], 3),
+                   "p50_s": round(st["latency_p50_s"], 3), "p90_s": round(st["latency_p90_s"], 3),
+                   "p99_s": round(st["latency_p99_s"], 3), "mean_s": round(st["latency_mean_s"], 3),
+                   "Mcell_steps_per_s": round(st["cell_steps"] / st["elapsed_s"] / 1e6, 1),
+                   "peak_active": st["peak_active"],
+                   "peak_reserved_GB": round(st["peak_reserved_bytes"] / (1 << 30), 2),
+                   "completed": st["completed"], "failed": st["failed"],
+                   "seconds": round(st["elapsed_s"], 2)}
+        return summary, [r["probes"] for r in res]
+
+    cap, _ = one_run([0.0] * len(specs), False)
+    capacity = cap["solves_per_s"]
+    rng = np.random.default_rng(seed + 1)
+    gaps = rng.exponential(1.0, len(specs))
+    points, same = [], True
+    for load in loads:
+        rate = load * capacity
+        arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
+        served, p_s = one_run(arrivals, False)
+        plain, p_p = one_run(arrivals, True)
+        same &= all(np.array_equal(a, b) for a, b in zip(p_s, p_p))
+        points.append({"load": load, "rate_per_s": round(rate, 3), "served": served,
+                       "one_at_a_time": plain,
+                       "speedup_solves_per_s": round(served["solves_per_s"] /
+                                                     max(plain["solves_per_s"], 1e-9), 2),
+                       "p99_ratio_one_at_a_time_over_served": round(
+                           plain["p99_s"] / max(served["p99_s"], 1e-9), 2)})
+    return {
+        "workload": f"c5: {len(specs)} requests (seed {seed}), cubic-ish axes log-U[48,384], "
+                    "CPML 8..16, spheres or layers, steps U[200,4000], TF/SF mode 1..4, "
+                    "8 probes each; Poisson arrivals",
+        "hbm_budget_GB": budget_gb, "capacity_solves_per_s": capacity,
+        "saturated": cap, "loads": points, "identical_results": bool(same),
+        "timing": "wall clock from each request's submission to its result on the host "
+                  "(set-up on the device, all steps, probe readout); capacity = every request "
+                  "queued at t=0 through the batched server",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -459,12 +530,21 @@ def main():
     ap.add_argument("--batch-grids", type=int, default=256)
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the batched leg, without its one-at-a-time baselines")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served (c5) leg")
+    ap.add_argument("--serve-requests", type=int, default=20)
+    ap.add_argument("--serve-loads", default="0.5,1.0",
+                    help="offered loads, fractions of the measured batched capacity")
+    ap.add_argument("--serve-only", action="store_true", help="run only the served leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     ranks = Ranks()
     if args.batch_only:
         print(json.dumps({"batched": run_batched(args.batch_grids, batched_only=True)}), flush=True)
+        return
+    if args.serve_only:
+        loads = [float(x) for x in args.serve_loads.split(",") if x]
+        print(json.dumps({"served": run_served(args.serve_requests, loads)}), flush=True)
         return
     if args.impl == "reference":
         out = run_reference(args, ranks)

@@ -84,6 +84,28 @@ int fdtd_update_source(fdtd_handle h, const float *src, size_t n);
  * other flags are ignored.  Takes effect at ReadySimulation / UpdateCuda. */
 int fdtd_update_material(fdtd_handle h, int32_t flag, const float *values, size_t n);
 
+/* Media given as shapes, rasterised on the device at ReadySimulation (and
+ * UpdateCuda) into the same six per-cell arrays UpdateMaterial takes (no
+ * reference counterpart: the reference's scripts build those arrays in
+ * MATLAB, GICsimulation.m:59-94).  Every cell starts at (bg_eps_r,
+ * bg_sigma); shapes apply in order, later ones overwriting, with the same
+ * eps_r and sigma on all three components.  Indices cover the whole grid
+ * (CPML included), cell (i,j,k) centred at (i+0.5, j+0.5, k+0.5). */
+#define FDTD_MAX_SHAPES 4096
+enum { FDTD_SHAPE_SPHERE = 1, FDTD_SHAPE_LAYER_Z = 2, FDTD_SHAPE_BOX = 3 };
+typedef struct {
+  int32_t kind;
+  float eps_r, sigma; /* inside the shape: relative permittivity, S/m */
+  int32_t reserved;
+  /* sphere: centre x, y, z and radius r (cells); inside when
+   *   ((i+0.5-x)^2 + (j+0.5-y)^2) + (k+0.5-z)^2 <= r*r in double arithmetic
+   * layer: g[0] <= k < g[1]
+   * box: g[0] <= i < g[1], g[2] <= j < g[3], g[4] <= k < g[5] */
+  double g[6];
+} fdtd_shape;
+int fdtd_set_shapes(fdtd_handle h, float bg_eps_r, float bg_sigma, const fdtd_shape *shapes,
+                    int32_t n);
+
 /* 'CreateMu' -- src/simFDTD.cu:133-141, createMu src/simulation.h:28-68.
  * As in the reference, a call after ReadySimulation computes the
  * coefficients but leaves the H update unchanged; a call before it is
@@ -228,6 +250,89 @@ int fdtd_batch_run(fdtd_batch b);
 int fdtd_batch_clear(fdtd_batch b);
 /* Steps member h has completed (-1 when h is not a member). */
 int fdtd_batch_progress(fdtd_batch b, fdtd_handle h, int32_t *done);
+/* Drops member h (finished or not); calls on h issued afterwards follow the
+ * batch's queued work. */
+int fdtd_batch_remove(fdtd_batch b, fdtd_handle h);
+/* Waits for the batch's queued work and reports whether every pipelined
+ * half-step completed (FDTD_ERR_CUDA if a bounded wait timed out; the
+ * members' fields are then not valid). */
+int fdtd_batch_status(fdtd_batch b);
+
+/* ---------------------------------------------------------------------
+ * Serving (extension, no reference counterpart): a request loop in a
+ * server thread.  Solve requests of different sizes are admitted in
+ * arrival order while the device memory their handles will hold fits a
+ * budget; each is set up on the device (its fields, psi arrays and
+ * coefficients stay resident until it finishes), joins one batch that
+ * advances every active solve together, and is retired when it finishes,
+ * its outputs copied to the host and its memory returned -- continuous
+ * batching: requests arriving while others run start at the next round.
+ * A one-at-a-time mode runs the same requests as a plain FIFO queue
+ * through fdtd_step_n, one solve on the device at a time.
+ * --------------------------------------------------------------------- */
+typedef uint64_t fdtd_server;
+
+typedef struct {
+  int32_t I, J, K;        /* grid, CPML included (SetConst TimeDim[1..3]) */
+  int32_t steps;          /* time steps (TimeDim[0]) */
+  float fctr, delX, delT; /* SetConst freqRes */
+  fdtd_params params;     /* CPML and TF/SF settings (fdtd_default_params) */
+  int32_t tfsf_mode;      /* plane-wave mode 1..4 (0: none) */
+  float rate;             /* Init1D rate */
+  const float *waveform;  /* [steps] plane-wave source (Init1D PW_source) */
+  float bg_eps_r, bg_sigma;
+  const fdtd_shape *shapes; /* media (fdtd_set_shapes) */
+  int32_t n_shapes;
+  int32_t n_probes;       /* probes (SetAntennaLocations, n_probes x 3) */
+  const int32_t *probes;
+  int32_t out_field;      /* OutputVis flag 1..6 of a field returned at the end,
+                             0: none */
+} fdtd_request;           /* everything is copied at submission */
+
+typedef struct {
+  uint64_t hbm_budget;    /* device bytes the admitted solves may hold at their
+                             peak (fdtd_estimate_device_bytes) */
+  int32_t max_active;     /* solves on the device at once (0: no limit) */
+  int32_t round_steps;    /* most steps per batch round between admissions
+                             (0: 32) */
+  int32_t one_at_a_time;  /* 1: plain FIFO queue through fdtd_step_n */
+} fdtd_server_config;
+
+typedef struct {
+  double submit_s, admit_s, finish_s; /* server clock, seconds */
+  uint64_t device_bytes;  /* held while running */
+  int32_t status;         /* FDTD_OK, or the failing call's status */
+  int32_t steps;
+  char message[128];      /* why it failed */
+} fdtd_request_info;
+
+typedef struct {
+  uint64_t submitted, completed, failed;
+  uint64_t cell_steps;          /* of completed solves */
+  uint64_t peak_reserved_bytes; /* highest sum of admitted peaks */
+  int32_t peak_active;          /* most solves on the device at once */
+  int32_t queued;               /* waiting now */
+  int32_t active;               /* on the device now */
+  double elapsed_s;             /* first submission to last completion */
+  double latency_p50_s, latency_p90_s, latency_p99_s, latency_mean_s;
+  double solves_per_s;          /* completed / elapsed_s */
+} fdtd_server_stats;
+
+int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg);
+/* Waits for every submitted request to finish, then stops the loop. */
+int fdtd_server_destroy(fdtd_server srv);
+int fdtd_server_submit(fdtd_server srv, const fdtd_request *req, uint64_t *ticket);
+/* Blocks until the request finished (timeout_s < 0: no limit);
+ * FDTD_ERR_STATE on timeout. */
+int fdtd_server_wait(fdtd_server srv, uint64_t ticket, double timeout_s);
+/* Copies a finished request's outputs (probes: steps x n_probes x 6 floats
+ * as OutputProbes; field: I*J*K floats as OutputVis) and info, and releases
+ * the ticket.  Either buffer may be NULL. */
+int fdtd_server_result(fdtd_server srv, uint64_t ticket, float *probes, size_t n_probes,
+                       float *field, size_t n_field, fdtd_request_info *info);
+/* Blocks until nothing is queued or running. */
+int fdtd_server_drain(fdtd_server srv);
+int fdtd_server_get_stats(fdtd_server srv, fdtd_server_stats *out);
 
 /* Allocation-free coefficient indexing.  No counterpart in the reference:
  * it serves callers that cannot allocate device memory -- hosts whose
@@ -254,6 +359,12 @@ int fdtd_batch_progress(fdtd_batch b, fdtd_handle h, int32_t *done);
 int fdtd_index_coefficients_static(const float *const ce[6], int32_t I, int32_t J, int32_t K,
                                    int32_t pitch, uint16_t *ids, float *table, int32_t max_ids,
                                    int32_t *n_ids, void *stream);
+
+/* Upper bound of the device memory one handle of these dimensions takes
+ * at its peak (during ReadySimulation and Init1D), in bytes (no reference
+ * counterpart; used for admission by memory budget). */
+int fdtd_estimate_device_bytes(int32_t I, int32_t J, int32_t K, int32_t pml, int32_t T,
+                               int32_t num_ant, uint64_t *bytes);
 
 /* The plan the kernels use for the CPML recurrences' division by the cell
  * size (no reference counterpart; the reference divides): out[0] =

@@ -31,6 +31,52 @@ class FdtdCurrent(ctypes.Structure):
     _fields_ = [("mode", I32), ("box", I32 * 6)]
 
 
+class FdtdShape(ctypes.Structure):
+    _fields_ = [("kind", I32), ("eps_r", ctypes.c_float), ("sigma", ctypes.c_float),
+                ("reserved", I32), ("g", ctypes.c_double * 6)]
+
+
+def shapes_array(rows):
+    """ctypes array of FdtdShape from rows [kind, eps_r, sigma, g0..g5]."""
+    rows = [list(r) for r in rows]
+    arr = (FdtdShape * max(1, len(rows)))()
+    for n, r in enumerate(rows):
+        g = [float(x) for x in r[3:9]] + [0.0] * (9 - max(len(r), 3))
+        arr[n] = FdtdShape(int(r[0]), float(r[1]), float(r[2]), 0, (ctypes.c_double * 6)(*g[:6]))
+    return arr
+
+
+class FdtdRequest(ctypes.Structure):
+    _fields_ = [("I", I32), ("J", I32), ("K", I32), ("steps", I32),
+                ("fctr", ctypes.c_float), ("delX", ctypes.c_float), ("delT", ctypes.c_float),
+                ("params", FdtdParams), ("tfsf_mode", I32), ("rate", ctypes.c_float),
+                ("waveform", ctypes.POINTER(ctypes.c_float)),
+                ("bg_eps_r", ctypes.c_float), ("bg_sigma", ctypes.c_float),
+                ("shapes", ctypes.POINTER(FdtdShape)), ("n_shapes", I32),
+                ("n_probes", I32), ("probes", ctypes.POINTER(I32)), ("out_field", I32)]
+
+
+class FdtdServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_active", I32), ("round_steps", I32),
+                ("one_at_a_time", I32)]
+
+
+class FdtdRequestInfo(ctypes.Structure):
+    _fields_ = [("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double),
+                ("finish_s", ctypes.c_double), ("device_bytes", ctypes.c_uint64),
+                ("status", I32), ("steps", I32), ("message", ctypes.c_char * 128)]
+
+
+class FdtdServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("cell_steps", ctypes.c_uint64),
+                ("peak_reserved_bytes", ctypes.c_uint64), ("peak_active", I32),
+                ("queued", I32), ("active", I32), ("elapsed_s", ctypes.c_double),
+                ("latency_p50_s", ctypes.c_double), ("latency_p90_s", ctypes.c_double),
+                ("latency_p99_s", ctypes.c_double), ("latency_mean_s", ctypes.c_double),
+                ("solves_per_s", ctypes.c_double)]
+
+
 class FdtdInfo(ctypes.Structure):
     _fields_ = [("I", I32), ("J", I32), ("K", I32), ("T", I32), ("num_ant", I32),
                 ("pml", I32), ("size_1d", I32), ("i0", I32), ("i1", I32), ("j0", I32),
@@ -50,6 +96,8 @@ SIGNATURES = {
     "fdtd_set_source": (ctypes.c_int, [U64, P, SZ]),
     "fdtd_update_source": (ctypes.c_int, [U64, P, SZ]),
     "fdtd_update_material": (ctypes.c_int, [U64, I32, P, SZ]),
+    "fdtd_set_shapes": (ctypes.c_int, [U64, ctypes.c_float, ctypes.c_float,
+                                       ctypes.POINTER(FdtdShape), I32]),
     "fdtd_create_mu": (ctypes.c_int, [U64, P, P, P, SZ]),
     "fdtd_set_antenna_locations": (ctypes.c_int, [U64, P, SZ]),
     "fdtd_ready_simulation": (ctypes.c_int, [U64]),
@@ -84,6 +132,19 @@ SIGNATURES = {
     "fdtd_batch_run": (ctypes.c_int, [U64]),
     "fdtd_batch_clear": (ctypes.c_int, [U64]),
     "fdtd_batch_progress": (ctypes.c_int, [U64, U64, ctypes.POINTER(I32)]),
+    "fdtd_batch_remove": (ctypes.c_int, [U64, U64]),
+    "fdtd_batch_status": (ctypes.c_int, [U64]),
+    "fdtd_server_create": (ctypes.c_int, [ctypes.POINTER(U64), ctypes.POINTER(FdtdServerConfig)]),
+    "fdtd_server_destroy": (ctypes.c_int, [U64]),
+    "fdtd_server_submit": (ctypes.c_int, [U64, ctypes.POINTER(FdtdRequest),
+                                          ctypes.POINTER(ctypes.c_uint64)]),
+    "fdtd_server_wait": (ctypes.c_int, [U64, ctypes.c_uint64, ctypes.c_double]),
+    "fdtd_server_result": (ctypes.c_int, [U64, ctypes.c_uint64, P, SZ, P, SZ,
+                                          ctypes.POINTER(FdtdRequestInfo)]),
+    "fdtd_server_drain": (ctypes.c_int, [U64]),
+    "fdtd_server_get_stats": (ctypes.c_int, [U64, ctypes.POINTER(FdtdServerStats)]),
+    "fdtd_estimate_device_bytes": (ctypes.c_int, [I32, I32, I32, I32, I32, I32,
+                                                  ctypes.POINTER(ctypes.c_uint64)]),
     "fdtd_division_plan": (ctypes.c_int, [ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
     "fdtd_check_division": (ctypes.c_int, [ctypes.c_float, ctypes.POINTER(ctypes.c_uint64)]),
     "fdtd_launch_count": (ctypes.c_uint64, []),

@@ -94,7 +94,11 @@ typedef struct sim {
   int32_t i0, i1, j0, j1, k0, k1;
   int64_t size_x, size_y, size_z;
   /* host copies (reference: pinned arrays of setConst / setSource) */
-  float *h_mat[6];      /* sigma_x,y,z, eps_x,y,z */
+  float *h_mat[6];      /* sigma_x,y,z, eps_x,y,z; allocated on first use */
+  /* media as shapes (fdtd_set_shapes): rasterised on the device instead */
+  fdtd_shape *shapes;
+  int32_t n_shapes;
+  float bg_eps, bg_sigma;
   float *h_src;
   int64_t *h_probe_idx;
   float bE[2 * FDTD_MAX_PML], cE[2 * FDTD_MAX_PML];
@@ -257,6 +261,55 @@ fdtd_params fdtd_default_params(void) {
   return p;
 }
 
+/* Device memory comes from a pool owned by the library (one per device),
+ * in stream order on the handle's stream: creating and deleting handles
+ * while others run (as the serving loop does) never synchronises the
+ * device the way cudaMalloc / cudaFree do.  Freed blocks stay in the pool
+ * for the next handle; the pool gives them back when no handle is left. */
+#define MAX_DEVICES 64
+static pthread_mutex_t g_pool_lock = PTHREAD_MUTEX_INITIALIZER;
+static cudaMemPool_t g_pool[MAX_DEVICES];
+static int g_live_sims = 0;
+
+static cudaError_t device_pool(cudaMemPool_t *out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+  pthread_mutex_lock(&g_pool_lock);
+  if (!g_pool[dev]) {
+    struct cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    e = cudaMemPoolCreate(&g_pool[dev], &props);
+    if (e == cudaSuccess) {
+      uint64_t keep = UINT64_MAX; /* cache freed blocks across handles */
+      e = cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (e != cudaSuccess) g_pool[dev] = NULL;
+  }
+  *out = g_pool[dev];
+  pthread_mutex_unlock(&g_pool_lock);
+  return e;
+}
+
+static void dfree_on(cudaStream_t st, void *p) {
+  if (p) cudaFreeAsync(p, st);
+}
+#define dfree(p) dfree_on(s->stream, (p))
+
+/* Stream-ordered allocation from the library's pool (see dalloc). */
+static cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t st) {
+  cudaMemPool_t pool;
+  cudaError_t e = device_pool(&pool);
+  if (e == cudaSuccess) e = cudaMallocFromPoolAsync(p, bytes ? bytes : 4, pool, st);
+  if (e != cudaSuccess) *p = NULL;
+  return e;
+}
+
+
 int fdtd_create(fdtd_handle *out) {
   if (!out) return fail(FDTD_ERR_INVALID_ARG, "null output handle");
   sim *s = (sim *)calloc(1, sizeof(sim));
@@ -292,12 +345,12 @@ int fdtd_create(fdtd_handle *out) {
   g_gen[slot] += 1;
   *out = ((uint64_t)g_gen[slot] << 32) | (uint64_t)(slot + 1);
   pthread_mutex_unlock(&g_reg_lock);
+  pthread_mutex_lock(&g_pool_lock);
+  ++g_live_sims;
+  pthread_mutex_unlock(&g_pool_lock);
   return FDTD_OK;
 }
 
-static void dfree(void *p) {
-  if (p) cudaFree(p);
-}
 
 int fdtd_destroy(fdtd_handle h) {
   uint32_t slot = (uint32_t)(h & 0xffffffffu);
@@ -313,6 +366,7 @@ int fdtd_destroy(fdtd_handle h) {
     dfree(s->d_ce[a]);
     free(s->h_mat[a]);
   }
+  free(s->shapes);
   for (int a = 0; a < 4; ++a) dfree(s->d_inc[a]);
   for (int a = 0; a < 3; ++a) dfree(s->d_mu[a]);
   dfree(s->d_psi_pool);
@@ -334,15 +388,27 @@ int fdtd_destroy(fdtd_handle h) {
   free(s->h_den_ex);
   free(s->h_den_hx);
   for (int i = 0; i < MAX_EVENTS; ++i) cudaEventDestroy(s->ev[i]);
+  cudaStreamSynchronize(s->stream); /* the frees above have run */
   cudaStreamDestroy(s->stream);
   free(s);
+  pthread_mutex_lock(&g_pool_lock);
+  if (--g_live_sims == 0)
+    for (int d = 0; d < MAX_DEVICES; ++d)
+      if (g_pool[d]) cudaMemPoolTrimTo(g_pool[d], 0);
+  pthread_mutex_unlock(&g_pool_lock);
   return FDTD_OK;
 }
 
 static int dalloc(sim *s, void **p, size_t bytes) {
-  cudaError_t e = cudaMalloc(p, bytes ? bytes : 4);
-  if (e != cudaSuccess)
-    return fail(FDTD_ERR_OOM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  cudaMemPool_t pool;
+  cudaError_t e = device_pool(&pool);
+  if (e == cudaSuccess) e = cudaMallocFromPoolAsync(p, bytes ? bytes : 4, pool, s->stream);
+  if (e != cudaSuccess) {
+    *p = NULL;
+    cudaGetLastError();
+    return fail(FDTD_ERR_OOM, "device allocation of %zu bytes: %s", bytes,
+                cudaGetErrorString(e));
+  }
   s->device_bytes += bytes;
   return FDTD_OK;
 }
@@ -408,13 +474,20 @@ int fdtd_set_const(fdtd_handle h, const float freqRes[3], const int32_t timeDim[
   s->size_x = (int64_t)p * J * K;
   s->size_y = (int64_t)I * p * K;
   s->size_z = (int64_t)I * J * p;
+  s->init_const = 1;
+  return FDTD_OK;
+}
+
+/* The host material arrays (sigma 0, eps 1 until UpdateMaterial sets
+ * them), allocated when first needed. */
+static int host_materials(sim *s) {
   for (int a = 0; a < 6; ++a) {
+    if (s->h_mat[a]) continue;
     s->h_mat[a] = (float *)malloc((size_t)s->IJK * sizeof(float));
     if (!s->h_mat[a]) return fail(FDTD_ERR_OOM, "out of host memory");
     const float v = a < 3 ? 0.0f : 1.0f;
     for (int64_t n = 0; n < s->IJK; ++n) s->h_mat[a][n] = v;
   }
-  s->init_const = 1;
   return FDTD_OK;
 }
 
@@ -462,7 +535,34 @@ int fdtd_update_material(fdtd_handle h, int32_t flag, const float *values, size_
   if (!values || n < (size_t)s->IJK)
     return fail(FDTD_ERR_INVALID_ARG, "UpdateMaterial needs Imax*Jmax*Kmax=%lld values",
                 (long long)s->IJK);
+  if (s->shapes)
+    return fail(FDTD_ERR_STATE, "UpdateMaterial after SetShapes: the media are the shapes");
+  int rc = host_materials(s);
+  if (rc) return rc;
   memcpy(s->h_mat[flag - 1], values, (size_t)s->IJK * sizeof(float));
+  return FDTD_OK;
+}
+
+int fdtd_set_shapes(fdtd_handle h, float bg_eps_r, float bg_sigma, const fdtd_shape *shapes,
+                    int32_t n) {
+  GET(h);
+  if (!s->init_const) return fail(FDTD_ERR_STATE, "SetShapes requires SetConst");
+  if (s->h_mat[0]) return fail(FDTD_ERR_STATE, "SetShapes after UpdateMaterial");
+  if (n < 0 || (n > 0 && !shapes) || n > FDTD_MAX_SHAPES)
+    return fail(FDTD_ERR_INVALID_ARG, "SetShapes takes 0..%d shapes", FDTD_MAX_SHAPES);
+  for (int a = 0; a < n; ++a)
+    if (shapes[a].kind < FDTD_SHAPE_SPHERE || shapes[a].kind > FDTD_SHAPE_BOX)
+      return fail(FDTD_ERR_INVALID_ARG, "shape %d: unknown kind %d", a, shapes[a].kind);
+  fdtd_shape *copy = (fdtd_shape *)malloc((size_t)(n > 0 ? n : 1) * sizeof(fdtd_shape));
+  if (!copy) return fail(FDTD_ERR_OOM, "out of host memory");
+  if (n) memcpy(copy, shapes, (size_t)n * sizeof(fdtd_shape));
+  free(s->shapes);
+  s->shapes = copy;
+  s->n_shapes = n;
+  s->bg_eps = bg_eps_r;
+  s->bg_sigma = bg_sigma;
+  /* taking effect needs ReadySimulation (or UpdateCuda after it), like
+   * UpdateMaterial */
   return FDTD_OK;
 }
 
@@ -606,15 +706,70 @@ static void fill_dev_struct(sim *s) {
   d->num_ant = (s->init_ant && s->d_probes) ? s->num_ant : 0;
 }
 
-/* Uploads the six material arrays into the coefficient buffers and turns
- * them into Cexe..Cezh in place (src/simulation.h:924-951 / :1099-1126). */
+/* Material of cell (i,j,k) from the shapes (see k_rasterize; the same
+ * double-precision tests, each operation rounded on its own). */
+static void shape_material(const sim *s, int i, int j, int k, float *eps, float *sig) {
+  float e = s->bg_eps, sg = s->bg_sigma;
+  for (int a = 0; a < s->n_shapes; ++a) {
+    const fdtd_shape *sh = &s->shapes[a];
+    int in = 0;
+    if (sh->kind == FDTD_SHAPE_SPHERE) {
+      const double x = ((double)i + 0.5) - sh->g[0];
+      const double y = ((double)j + 0.5) - sh->g[1];
+      const double z = ((double)k + 0.5) - sh->g[2];
+      const double xx = x * x, yy = y * y, zz = z * z;
+      const double xy = xx + yy;
+      const double d2 = xy + zz;
+      const double rr = sh->g[3] * sh->g[3];
+      in = d2 <= rr;
+    } else if (sh->kind == FDTD_SHAPE_LAYER_Z) {
+      in = (double)k >= sh->g[0] && (double)k < sh->g[1];
+    } else if (sh->kind == FDTD_SHAPE_BOX) {
+      in = (double)i >= sh->g[0] && (double)i < sh->g[1] && (double)j >= sh->g[2] &&
+           (double)j < sh->g[3] && (double)k >= sh->g[4] && (double)k < sh->g[5];
+    }
+    if (in) {
+      e = sh->eps_r;
+      sg = sh->sigma;
+    }
+  }
+  *eps = e;
+  *sig = sg;
+}
+
+/* Fills the six material arrays on the device (from the shapes, or from
+ * the host arrays UpdateMaterial filled), turns them into Cexe..Cezh in
+ * place (src/simulation.h:924-951 / :1099-1126), and, when the grid's
+ * coefficient tuples fit the material table, indexes them and releases the
+ * per-cell arrays (the kernels then read the 2-byte ids only). */
 static int upload_coefficients(sim *s) {
+  const size_t bytes = (size_t)s->cells * sizeof(float);
+  int rc;
+  for (int a = 0; a < 6; ++a)
+    if (!s->d_ce[a] && (rc = dalloc(s, (void **)&s->d_ce[a], bytes))) return rc;
+  fill_dev_struct(s);
   /* sigma_x -> ce[0], sigma_y -> ce[1], sigma_z -> ce[2], eps -> ce[3..5]:
    * the kernel reads both inputs of a component before writing its outputs */
-  for (int a = 0; a < 6; ++a)
-    CU(cudaMemcpy2DAsync(s->d_ce[a], (size_t)s->Ip * sizeof(float), s->h_mat[a],
-                         (size_t)s->I * sizeof(float), (size_t)s->I * sizeof(float),
-                         (size_t)s->J * s->K, cudaMemcpyHostToDevice, s->stream));
+  if (s->shapes) {
+    fdtd_shape *d_shapes = NULL;
+    const size_t sb = (size_t)(s->n_shapes > 0 ? s->n_shapes : 1) * sizeof(fdtd_shape);
+    CU(pool_alloc((void **)&d_shapes, sb, s->stream));
+    if (s->n_shapes)
+      CU(cudaMemcpyAsync(d_shapes, s->shapes, (size_t)s->n_shapes * sizeof(fdtd_shape),
+                         cudaMemcpyHostToDevice, s->stream));
+    float *sg[3] = {s->d_ce[0], s->d_ce[1], s->d_ce[2]};
+    float *ep[3] = {s->d_ce[3], s->d_ce[4], s->d_ce[5]};
+    const int e = fdtdk_rasterize(&s->dev, sg, ep, d_shapes, s->n_shapes, s->bg_eps,
+                                  s->bg_sigma, s->stream);
+    dfree(d_shapes);
+    KL(e);
+  } else {
+    if ((rc = host_materials(s))) return rc;
+    for (int a = 0; a < 6; ++a)
+      CU(cudaMemcpy2DAsync(s->d_ce[a], (size_t)s->Ip * sizeof(float), s->h_mat[a],
+                           (size_t)s->I * sizeof(float), (size_t)s->I * sizeof(float),
+                           (size_t)s->J * s->K, cudaMemcpyHostToDevice, s->stream));
+  }
   float *ce[6];
   const float *eps[3], *sig[3];
   for (int a = 0; a < 6; ++a) ce[a] = s->d_ce[a];
@@ -639,6 +794,11 @@ static int upload_coefficients(sim *s) {
     if (!cnt[1] && !cnt[2] && cnt[0] > 0 && cnt[0] <= MAX_MATERIALS) {
       s->coef_mode = 1;
       s->num_mat = cnt[0];
+      for (int a = 0; a < 6; ++a) { /* UpdateCuda allocates them again */
+        dfree(s->d_ce[a]);
+        s->d_ce[a] = NULL;
+        s->device_bytes -= bytes;
+      }
     }
   }
   fill_dev_struct(s);
@@ -836,10 +996,8 @@ int fdtd_ready_simulation(fdtd_handle h) {
   }
   const size_t bytes = (size_t)s->cells * sizeof(float);
   int rc;
-  for (int a = 0; a < 6; ++a) {
+  for (int a = 0; a < 6; ++a)
     if ((rc = dalloc(s, (void **)&s->d_f[a], bytes))) return rc;
-    if ((rc = dalloc(s, (void **)&s->d_ce[a], bytes))) return rc;
-  }
   if ((rc = dalloc(s, (void **)&s->d_mat, (size_t)s->cells * sizeof(uint16_t)))) return rc;
   CU(cudaMemsetAsync(s->d_mat, 0, (size_t)s->cells * sizeof(uint16_t), s->stream));
   if (s->allow_compress) {
@@ -1308,6 +1466,29 @@ int fdtd_set_device(int32_t device) {
   return FDTD_OK;
 }
 
+int fdtd_estimate_device_bytes(int32_t I, int32_t J, int32_t K, int32_t pml, int32_t T,
+                               int32_t num_ant, uint64_t *bytes) {
+  if (!bytes) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  if (I < 2 * pml + 2 || J < 2 * pml + 2 || K < 2 * pml + 2 || T < 1 || num_ant < 0 ||
+      pml < 2 || pml > FDTD_MAX_PML)
+    return fail(FDTD_ERR_INVALID_ARG, "grid %dx%dx%d, pml %d, %d steps is not valid", I, J, K,
+                pml, T);
+  const uint64_t Ip = (uint64_t)(I + 7) / 8 * 8, cells = Ip * (uint64_t)J * (uint64_t)K;
+  const uint64_t S = (uint64_t)(I > J ? (I > K ? I : K) : (J > K ? J : K));
+  const uint64_t sx = (uint64_t)pml * J * K, sy = (uint64_t)I * pml * K,
+                 sz = (uint64_t)I * J * pml;
+  uint64_t b = 6 * cells * 4;                      /* fields */
+  b += 6 * cells * 4;                              /* coefficients (until indexed) */
+  b += cells * 2 + (uint64_t)MAX_MATERIALS * 6 * 4; /* material ids + table */
+  b += (uint64_t)HASH_CAP * (8 + 8 + 4) + 16 + 4;  /* indexing scratch, error word */
+  b += 8 * (sx + sy + sz) * 4;                     /* psi pairs */
+  b += 2 * (uint64_t)I * 4 + 16;                   /* stretch denominators, counters */
+  b += (uint64_t)T * num_ant * 6 * 4 + (uint64_t)num_ant * 8; /* probes */
+  b += 4 * (uint64_t)T * S * 4 + (uint64_t)T * 4 + 16 * S + (uint64_t)T * 4; /* 1D tables */
+  *bytes = b;
+  return FDTD_OK;
+}
+
 int fdtd_division_plan(float dx, float out[4]) {
   if (!out) return fail(FDTD_ERR_INVALID_ARG, "null output");
   const fdtd_div_plan p = fdtd_make_div_plan(dx);
@@ -1351,6 +1532,17 @@ int fdtd_output_vis(fdtd_handle h, float *out, size_t n, int32_t flag) {
   const size_t cnt = n < (size_t)s->IJK ? n : (size_t)s->IJK;
   if (flag <= 0 && flag >= -5) {
     const int idx = -flag; /* 0,-1,-2 sigma_x,y,z; -3,-4,-5 eps_x,y,z */
+    if (s->shapes) { /* the media are shapes: the same cells, rasterised here */
+      for (size_t n2 = 0; n2 < cnt; ++n2) {
+        const int64_t ii = (int64_t)n2 % s->I, rr = (int64_t)n2 / s->I;
+        float e, sg;
+        shape_material(s, (int)ii, (int)(rr % s->J), (int)(rr / s->J), &e, &sg);
+        out[n2] = idx < 3 ? sg : e;
+      }
+      return FDTD_OK;
+    }
+    int rc = host_materials(s);
+    if (rc) return rc;
     memcpy(out, s->h_mat[idx], cnt * sizeof(float));
     return FDTD_OK;
   }
@@ -1556,8 +1748,8 @@ int fdtd_batch_create(fdtd_batch *out) {
   if (!b) return fail(FDTD_ERR_OOM, "out of host memory");
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_work, 4 * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_err, sizeof(int32_t));
+  if (e == cudaSuccess) e = pool_alloc((void **)&b->d_work, 4 * sizeof(int32_t), b->stream);
+  if (e == cudaSuccess) e = pool_alloc((void **)&b->d_err, sizeof(int32_t), b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_work, 0, 4 * sizeof(int32_t), b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), b->stream);
   if (e != cudaSuccess) {
@@ -1573,8 +1765,9 @@ int fdtd_batch_create(fdtd_batch *out) {
     }
   if (slot < 0) {
     pthread_mutex_unlock(&g_reg_lock);
-    cudaFree(b->d_work);
-    cudaFree(b->d_err);
+    dfree_on(b->stream, b->d_work);
+    dfree_on(b->stream, b->d_err);
+    cudaStreamSynchronize(b->stream);
     cudaStreamDestroy(b->stream);
     free(b);
     return fail(FDTD_ERR_OOM, "too many batches");
@@ -1587,12 +1780,12 @@ int fdtd_batch_create(fdtd_batch *out) {
 }
 
 static void batch_free_mirrors(batch *b) {
-  dfree(b->d_devs);
-  dfree(b->d_maps);
-  dfree(b->d_ops);
-  dfree(b->d_steps);
-  dfree(b->d_tab_h);
-  dfree(b->d_tab_e);
+  dfree_on(b->stream, b->d_devs);
+  dfree_on(b->stream, b->d_maps);
+  dfree_on(b->stream, b->d_ops);
+  dfree_on(b->stream, b->d_steps);
+  dfree_on(b->stream, b->d_tab_h);
+  dfree_on(b->stream, b->d_tab_e);
   b->d_devs = NULL;
   b->d_maps = NULL;
   b->d_ops = NULL;
@@ -1621,8 +1814,9 @@ int fdtd_batch_destroy(fdtd_batch h) {
   pthread_mutex_unlock(&g_reg_lock);
   cudaStreamSynchronize(b->stream);
   batch_free_mirrors(b);
-  dfree(b->d_work);
-  dfree(b->d_err);
+  dfree_on(b->stream, b->d_work);
+  dfree_on(b->stream, b->d_err);
+  cudaStreamSynchronize(b->stream);
   cudaEventDestroy(b->ev);
   cudaStreamDestroy(b->stream);
   free(b->m);
@@ -1678,17 +1872,17 @@ int fdtd_batch_add(fdtd_batch bh, fdtd_handle h, int32_t first, int32_t count, i
   return FDTD_OK;
 }
 
-static int ensure_cap(void **d, void **hbuf, int *cap, int need, size_t elem) {
+static int ensure_cap(void **d, void **hbuf, int *cap, int need, size_t elem, cudaStream_t st) {
   if (need <= *cap) return FDTD_OK;
   int nc = *cap ? *cap : 256;
   while (nc < need) nc *= 2;
-  if (*d) cudaFree(*d);
+  dfree_on(st, *d);
   free(*hbuf);
   *d = NULL;
   *hbuf = malloc((size_t)nc * elem);
   if (!*hbuf) return fail(FDTD_ERR_OOM, "out of host memory");
-  cudaError_t e = cudaMalloc(d, (size_t)nc * elem);
-  if (e != cudaSuccess) return fail(FDTD_ERR_OOM, "cudaMalloc: %s", cudaGetErrorString(e));
+  cudaError_t e = pool_alloc(d, (size_t)nc * elem, st);
+  if (e != cudaSuccess) return fail(FDTD_ERR_OOM, "device allocation: %s", cudaGetErrorString(e));
   *cap = nc;
   return FDTD_OK;
 }
@@ -1731,10 +1925,10 @@ static int batch_rebuild(batch *b) {
     int cap = b->dev_cap ? b->dev_cap : 64;
     while (cap < na) cap *= 2;
     int c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-    dfree(b->d_devs);
-    dfree(b->d_maps);
-    dfree(b->d_ops);
-    dfree(b->d_steps);
+    dfree_on(b->stream, b->d_devs);
+    dfree_on(b->stream, b->d_maps);
+    dfree_on(b->stream, b->d_ops);
+    dfree_on(b->stream, b->d_steps);
     b->d_devs = NULL;
     b->d_maps = NULL;
     b->d_ops = NULL;
@@ -1742,22 +1936,25 @@ static int batch_rebuild(batch *b) {
     free(b->act);
     b->act = (int *)malloc((size_t)cap * sizeof(int));
     if (!b->act) return fail(FDTD_ERR_OOM, "out of host memory");
-    if ((rc = ensure_cap((void **)&b->d_devs, (void **)&b->h_devs, &c0, cap, sizeof(fdtd_dev))))
+    if ((rc = ensure_cap((void **)&b->d_devs, (void **)&b->h_devs, &c0, cap, sizeof(fdtd_dev),
+                         b->stream)))
       return rc;
     if ((rc = ensure_cap((void **)&b->d_maps, (void **)&b->h_maps, &c1, cap,
-                         sizeof(((fdtd_maps *)0)->bytes))))
+                         sizeof(((fdtd_maps *)0)->bytes), b->stream)))
       return rc;
-    if ((rc = ensure_cap((void **)&b->d_ops, (void **)&b->h_ops, &c2, cap, sizeof(fdtd_op))))
+    if ((rc = ensure_cap((void **)&b->d_ops, (void **)&b->h_ops, &c2, cap, sizeof(fdtd_op),
+                         b->stream)))
       return rc;
-    if ((rc = ensure_cap((void **)&b->d_steps, (void **)&b->h_steps, &c3, cap, sizeof(int32_t))))
+    if ((rc = ensure_cap((void **)&b->d_steps, (void **)&b->h_steps, &c3, cap, sizeof(int32_t),
+                         b->stream)))
       return rc;
     b->dev_cap = cap;
   }
   if ((rc = ensure_cap((void **)&b->d_tab_h, (void **)&b->h_tab_h, &b->cap_h, nh,
-                       4 * sizeof(int32_t))))
+                       4 * sizeof(int32_t), b->stream)))
     return rc;
   if ((rc = ensure_cap((void **)&b->d_tab_e, (void **)&b->h_tab_e, &b->cap_e, ne,
-                       4 * sizeof(int32_t))))
+                       4 * sizeof(int32_t), b->stream)))
     return rc;
   int g = 0;
   nh = ne = 0;
@@ -1867,15 +2064,9 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
   return FDTD_OK;
 }
 
-/* Runs every member to its last step. */
-int fdtd_batch_run(fdtd_batch bh) {
+int fdtd_batch_status(fdtd_batch bh) {
   batch *b = blookup(bh);
   if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
-  int32_t left = 1;
-  while (left) {
-    int rc = fdtd_batch_step(bh, 1 << 30, &left);
-    if (rc) return rc;
-  }
   CU(cudaStreamSynchronize(b->stream));
   int32_t e = 0;
   CU(cudaMemcpy(&e, b->d_err, sizeof(e), cudaMemcpyDeviceToHost));
@@ -1885,6 +2076,16 @@ int fdtd_batch_run(fdtd_batch bh) {
                                "(device error word %d); member fields are not valid", e);
   }
   return FDTD_OK;
+}
+
+/* Runs every member to its last step. */
+int fdtd_batch_run(fdtd_batch bh) {
+  int32_t left = 1;
+  while (left) {
+    int rc = fdtd_batch_step(bh, 1 << 30, &left);
+    if (rc) return rc;
+  }
+  return fdtd_batch_status(bh);
 }
 
 /* Drops the members (finished or not); device buffers are kept. */
@@ -1899,6 +2100,24 @@ int fdtd_batch_clear(fdtd_batch bh) {
   }
   b->n = 0;
   b->n_act = 0;
+  b->dirty = 1;
+  return FDTD_OK;
+}
+
+/* Drops one member, finished or not; later calls on its handle follow the
+ * batch's queued work. */
+int fdtd_batch_remove(fdtd_batch bh, fdtd_handle h) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  int idx = -1;
+  for (int i = 0; i < b->n; ++i)
+    if (b->m[i].h == h) idx = i;
+  if (idx < 0) return fail(FDTD_ERR_INVALID_ARG, "not a member of this batch");
+  CU(cudaEventRecord(b->ev, b->stream));
+  sim *s = lookup(h);
+  if (s) CU(cudaStreamWaitEvent(s->stream, b->ev, 0));
+  memmove(&b->m[idx], &b->m[idx + 1], (size_t)(b->n - idx - 1) * sizeof(bmember));
+  b->n -= 1;
   b->dirty = 1;
   return FDTD_OK;
 }

@@ -11,6 +11,8 @@
 
 #include <cuda_runtime_api.h>
 
+#include "fdtd_gb300.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -152,6 +154,11 @@ unsigned long long fdtdk_launch_count(void);
 /* Records an error message for the calling thread (fdtd_last_error) and
  * returns code. */
 int fdtd_internal_fail(int code, const char *msg);
+
+/* Media from shapes into the six material arrays (sigma, eps; pitched). */
+int fdtdk_rasterize(const fdtd_dev *d, float *const sig[3], float *const eps[3],
+                    const fdtd_shape *shapes, int32_t n_shapes, float bg_eps, float bg_sig,
+                    cudaStream_t s);
 
 /* Plan for dividing by a fixed cell size (fdtd_host.c). */
 typedef struct {

@@ -237,6 +237,50 @@ __global__ void k_compute_ce(float *ce0, float *ce1, float *ce2, float *ce3, flo
   }
 }
 
+// Media from shapes: sigma into sig[0..2], eps_r into eps[0..2] (pitched),
+// starting from the background and applying the shapes in order.  The
+// tests are done in double arithmetic with each operation rounded on its
+// own, so the host rasteriser (OutputVis) and any double-precision
+// restatement give the same cells.
+__global__ void k_rasterize(float *sg0, float *sg1, float *sg2, float *ep0, float *ep1,
+                            float *ep2, const fdtd_shape *shapes, int n_shapes, float bg_eps,
+                            float bg_sig, int64_t cells, int Ip, int I, int J) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < cells;
+       n += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(n % Ip);
+    if (i >= I) continue;
+    const int64_t r = n / Ip;
+    const int j = (int)(r % J), k = (int)(r / J);
+    float e = bg_eps, sg = bg_sig;
+    for (int a = 0; a < n_shapes; ++a) {
+      const fdtd_shape &sh = shapes[a];
+      bool in = false;
+      if (sh.kind == FDTD_SHAPE_SPHERE) {
+        const double x = __dsub_rn((double)i + 0.5, sh.g[0]);
+        const double y = __dsub_rn((double)j + 0.5, sh.g[1]);
+        const double z = __dsub_rn((double)k + 0.5, sh.g[2]);
+        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+        in = d2 <= __dmul_rn(sh.g[3], sh.g[3]);
+      } else if (sh.kind == FDTD_SHAPE_LAYER_Z) {
+        in = (double)k >= sh.g[0] && (double)k < sh.g[1];
+      } else if (sh.kind == FDTD_SHAPE_BOX) {
+        in = (double)i >= sh.g[0] && (double)i < sh.g[1] && (double)j >= sh.g[2] &&
+             (double)j < sh.g[3] && (double)k >= sh.g[4] && (double)k < sh.g[5];
+      }
+      if (in) {
+        e = sh.eps_r;
+        sg = sh.sigma;
+      }
+    }
+    sg0[n] = sg;
+    sg1[n] = sg;
+    sg2[n] = sg;
+    ep0[n] = e;
+    ep1[n] = e;
+    ep2[n] = e;
+  }
+}
+
 // src/simulation.h:43-63: delT/mu0/mu/(1 + sigma_m*delT/2/mu0/mu) * den_hx
 // (dense layout: these coefficients are stored, never read by a kernel).
 __global__ void k_compute_mu(float *out, const float *mu, const float *den_hx, int64_t IJK,
@@ -593,6 +637,16 @@ int fdtdk_init_1d(const fdtd_dev *d, float *tab[4], const float *pw, float Ceh, 
 int fdtdk_batch_probes(const fdtd_dev *devs, int32_t n, cudaStream_t s) {
   if (n <= 0) return 0;
   k_batch_probes<<<n, 256, 0, s>>>(devs, n);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_rasterize(const fdtd_dev *d, float *const sig[3], float *const eps[3],
+                    const fdtd_shape *shapes, int32_t n_shapes, float bg_eps, float bg_sig,
+                    cudaStream_t s) {
+  k_rasterize<<<152 * 8, 256, 0, s>>>(sig[0], sig[1], sig[2], eps[0], eps[1], eps[2],
+                                                  shapes, n_shapes, bg_eps, bg_sig, d->cells,
+                                                  d->Ip, d->I, d->J);
   ++g_launches;
   return (int)cudaGetLastError();
 }

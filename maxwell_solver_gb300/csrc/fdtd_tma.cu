@@ -427,7 +427,6 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
           update_e_cell<true, PML>(d, mode, inc, cm, cur_src, cur, i, j, k, px, py, pz, C, ex,
                                    ey, ez, hx, hy, hz, hz_jm, hx_jm, hz_im, hy_im, hx_km[c],
                                    hy_km[c]);
-          // the next plane's psi pairs into L2 while this plane finishes
         }
       } else {  // interior warp: i, j, k >= 1, no CPML, TF/SF face or source
         ex = C.exe * ex + C.exh * (+(hz - hz_jm) - (hy - hy_km[c]));

@@ -90,6 +90,22 @@ static float *as_f32(const mxArray *a, size_t *n) {
   return out;
 }
 
+static double *as_f64(const mxArray *a, size_t *n) {
+  size_t cnt = mxGetNumberOfElements(a);
+  if (n) *n = cnt;
+  double *out = (double *)malloc((cnt ? cnt : 1) * sizeof(double));
+  const void *d = mxGetData(a);
+  for (size_t i = 0; i < cnt; ++i) {
+    switch (mxGetClassID(a)) {
+      case mxDOUBLE_CLASS: out[i] = ((const double *)d)[i]; break;
+      case mxSINGLE_CLASS: out[i] = (double)((const float *)d)[i]; break;
+      case mxINT32_CLASS: out[i] = (double)((const int32_t *)d)[i]; break;
+      default: out[i] = 0.0;
+    }
+  }
+  return out;
+}
+
 static size_t scalar_count(const mxArray *a) {
   switch (mxGetClassID(a)) {
     case mxUINT32_CLASS: return *(const uint32_t *)mxGetData(a);
@@ -242,6 +258,31 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     int rc = fdtd_update_material(P, fl, v, n);
     free(flag);
     free(v);
+    CHECK(rc);
+  } else if (strcmp(o, "setshapes") == 0) {
+    /* SetShapes(P, [bg_eps_r bg_sigma], S): S is n x 9, one shape per row
+     * [kind eps_r sigma g1 .. g6] (column-major, as MATLAB stores it) */
+    if (nrhs < 4) mexErrMsgIdAndTxt("simFDTD:InvalidInput", "background and shapes required.");
+    size_t nb = 0, ns = 0;
+    float *bg = as_f32(prhs[2], &nb);
+    double *sv = as_f64(prhs[3], &ns);
+    const size_t rows = mxGetNumberOfElements(prhs[3]) ? mxGetM(prhs[3]) : 0;
+    if (nb < 2 || (rows && mxGetN(prhs[3]) < 9)) {
+      free(bg);
+      free(sv);
+      mexErrMsgIdAndTxt("simFDTD:InvalidInput", "background and shapes required.");
+    }
+    fdtd_shape *sh = (fdtd_shape *)calloc(rows ? rows : 1, sizeof(fdtd_shape));
+    for (size_t r = 0; r < rows; ++r) {
+      sh[r].kind = (int32_t)sv[r];
+      sh[r].eps_r = (float)sv[r + rows];
+      sh[r].sigma = (float)sv[r + 2 * rows];
+      for (int g = 0; g < 6; ++g) sh[r].g[g] = sv[r + (size_t)(3 + g) * rows];
+    }
+    int rc = fdtd_set_shapes(P, bg[0], bg[1], sh, (int32_t)rows);
+    free(sh);
+    free(bg);
+    free(sv);
     CHECK(rc);
   } else if (strcmp(o, "outputant") == 0) {
     if (nrhs < 3) mexErrMsgIdAndTxt("simFDTD:InvalidInput", "OutAntSize required.");

@@ -137,6 +137,16 @@ def simFDTD(op: str, *args):  # noqa: N802 - mirrors the MATLAB entry point
         need(2, "flag, values required.")
         flag, v = _i32(a[0]), _f32(a[1])
         _check(lib.fdtd_update_material(P, int(flag[0]), _ptr(v), v.size))
+    elif o == "setshapes":
+        # [bg_eps_r bg_sigma], rows [kind eps_r sigma g0 .. g5] (FDTD_SHAPE_*)
+        need(2, "background and shapes required.")
+        bg = _f32(a[0])
+        rows = np.asarray(a[1], dtype=np.float64).reshape(-1, 9) if np.size(a[1]) else \
+            np.zeros((0, 9))
+        if bg.size < 2:
+            raise SimFDTDError("simFDTD:InvalidInput", "background and shapes required.")
+        arr = _native.shapes_array(rows)
+        _check(lib.fdtd_set_shapes(P, float(bg[0]), float(bg[1]), arr, len(rows)))
     elif o == "outputant":
         need(1, "OutAntSize required.")
         n = int(np.asarray(a[0]).ravel()[0])

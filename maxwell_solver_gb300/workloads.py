@@ -178,6 +178,7 @@ class GridSpec:
     fctr: float
     seed: int
     delX: float = 1e-3
+    media: str = "spheres"  # or "layers"
 
     @property
     def delT(self) -> float:
@@ -201,12 +202,50 @@ def batch_mix(n: int = 256, seed: int = 3):
     return out
 
 
-def grid_materials(spec: GridSpec):
-    """eps, sigma (float32, F-order flat) with the spec's random spheres."""
+def serve_mix(n: int = 64, seed: int = 4, max_axis: int = 384, max_steps: int = 4000):
+    """c5 requests: cubic-ish grids (a base size log-uniform 48..max_axis,
+    each axis within +-15% of it), CPML 8..16 cells, random spheres or
+    layered media, steps uniform 200..max_steps, TF/SF mode 1..4, f0 uniform
+    10..60 GHz."""
+    r = rng(seed)
+    out = []
+    for g in range(n):
+        base = math.exp(r.uniform(math.log(48), math.log(max_axis)))
+        dims = tuple(int(min(max_axis, max(48, round(base * r.uniform(0.85, 1.15)))))
+                     for _ in range(3))
+        pml = int(r.integers(8, 17))
+        media = "layers" if r.random() < 0.5 else "spheres"
+        steps = int(r.integers(200, max_steps + 1))
+        out.append(GridSpec(dims, steps, pml, int(r.integers(1, 5)), int(r.integers(0, 11)),
+                            float(r.uniform(10e9, 60e9)), seed * 1000 + g, media=media))
+    return out
+
+
+SHAPE_SPHERE, SHAPE_LAYER_Z, SHAPE_BOX = 1, 2, 3
+
+
+def grid_shapes(spec: GridSpec):
+    """(bg_eps_r, bg_sigma, rows): the spec's media as shape rows
+    [kind, eps_r, sigma, g0..g5] (fdtd_shape), applied in order."""
     I, J, K = spec.dims
     r = rng(spec.seed)
-    eps = np.ones((I, J, K), dtype=np.float32, order="F")
-    sig = np.zeros((I, J, K), dtype=np.float32, order="F")
+    rows = []
+    if spec.media == "layers":  # air above, conductive layers below (config 3 style)
+        z = K - spec.pml - 2 - int(0.45 * K)
+        top = z
+        e = s = None
+        for _ in range(6):
+            t = int(r.integers(10, 81))
+            lo = max(0, top - t)
+            e = np.float32(r.uniform(5, 30))
+            s = np.float32(10.0 ** r.uniform(-4, 0))
+            rows.append([SHAPE_LAYER_Z, e, s, lo, top, 0, 0, 0, 0])
+            top = lo
+            if top == 0:
+                break
+        if top > 0:  # the deepest layer continues to the bottom
+            rows.append([SHAPE_LAYER_Z, e, s, 0, top, 0, 0, 0, 0])
+        return 1.0, 0.0, rows
     lo = spec.pml + 2
     room = min(I, J, K) - 2 * lo
     for _ in range(spec.n_spheres):
@@ -214,16 +253,60 @@ def grid_materials(spec: GridSpec):
         c = [r.uniform(lo + rad, n - lo - rad) for n in (I, J, K)]
         e = np.float32(r.uniform(1.5, 10.0))
         s = np.float32(10.0 ** r.uniform(-4, 0))
-        b0 = [max(0, int(math.floor(c[a] - rad))) for a in range(3)]
-        b1 = [min(n, int(math.ceil(c[a] + rad)) + 1) for a, n in enumerate((I, J, K))]
-        x = np.arange(b0[0], b1[0]) + 0.5 - c[0]
-        y = np.arange(b0[1], b1[1]) + 0.5 - c[1]
-        z = np.arange(b0[2], b1[2]) + 0.5 - c[2]
-        inside = (x[:, None, None] ** 2 + y[None, :, None] ** 2 + z[None, None, :] ** 2) <= rad * rad
-        sl = (slice(b0[0], b1[0]), slice(b0[1], b1[1]), slice(b0[2], b1[2]))
-        eps[sl][inside] = e
-        sig[sl][inside] = s
+        rows.append([SHAPE_SPHERE, e, s, c[0], c[1], c[2], rad, 0, 0])
+    return 1.0, 0.0, rows
+
+
+def rasterize(dims, bg_eps, bg_sig, rows):
+    """eps, sigma (float32, F-order flat) of shape rows, with the library's
+    tests: sphere ((i+0.5-x)^2 + (j+0.5-y)^2) + (k+0.5-z)^2 <= r*r in
+    float64, layer g0 <= k < g1, box g0 <= i < g1 ...; later rows win."""
+    I, J, K = dims
+    eps = np.full((I, J, K), np.float32(bg_eps), dtype=np.float32, order="F")
+    sig = np.full((I, J, K), np.float32(bg_sig), dtype=np.float32, order="F")
+    for row in rows:
+        kind, e, s = int(row[0]), np.float32(row[1]), np.float32(row[2])
+        g = [float(v) for v in row[3:9]]
+        if kind == SHAPE_SPHERE:
+            c, rad = g[:3], g[3]
+            b0 = [max(0, int(math.floor(c[a] - rad))) for a in range(3)]
+            b1 = [min(n, int(math.ceil(c[a] + rad)) + 1) for a, n in enumerate((I, J, K))]
+            x = np.arange(b0[0], b1[0]) + 0.5 - c[0]
+            y = np.arange(b0[1], b1[1]) + 0.5 - c[1]
+            z = np.arange(b0[2], b1[2]) + 0.5 - c[2]
+            inside = (x[:, None, None] ** 2 + y[None, :, None] ** 2 +
+                      z[None, None, :] ** 2) <= rad * rad
+            sl = (slice(b0[0], b1[0]), slice(b0[1], b1[1]), slice(b0[2], b1[2]))
+            eps[sl][inside] = e
+            sig[sl][inside] = s
+        else:
+            k = np.arange(K, dtype=np.float64)
+            mk = (k >= g[0]) & (k < g[1]) if kind == SHAPE_LAYER_Z else \
+                (k >= g[4]) & (k < g[5])
+            m = np.broadcast_to(mk[None, None, :], (I, J, K))
+            if kind == SHAPE_BOX:
+                i = np.arange(I, dtype=np.float64)
+                j = np.arange(J, dtype=np.float64)
+                m = m & ((i >= g[0]) & (i < g[1]))[:, None, None] & \
+                    ((j >= g[2]) & (j < g[3]))[None, :, None]
+            eps[m] = e
+            sig[m] = s
     return eps.ravel(order="F"), sig.ravel(order="F")
+
+
+def grid_materials(spec: GridSpec):
+    """eps, sigma (float32, F-order flat) of the spec's media."""
+    return rasterize(spec.dims, *grid_shapes(spec))
+
+
+def grid_probes(spec: GridSpec, n: int = 8):
+    """n probe cells inside the CPML (SetAntennaLocations order: n x 3,
+    column-major), seeded by the spec."""
+    I, J, K = spec.dims
+    r = rng(spec.seed + 7919)
+    lim = [I - 2 * spec.pml, J - 2 * spec.pml, K - 2 * spec.pml]
+    loc = np.stack([r.integers(1, max(2, lim[a] - 1), n) for a in range(3)], axis=1)
+    return np.asfortranarray(loc.astype(np.int32))
 
 
 def grid_source(spec: GridSpec):
