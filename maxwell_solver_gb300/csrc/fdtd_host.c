@@ -1728,6 +1728,8 @@ typedef struct batch {
   int32_t *h_steps, *h_tab_h, *h_tab_e;
   int *act;  /* member index of each active slot */
   int n_act, n_h, n_e, any_probes, dirty;
+  int any_split;   /* some active member's TF/SF runs as the face pass */
+  int32_t face_max; /* largest face-plane area of those members */
 } batch;
 
 static batch *g_batches[MAX_BATCHES];
@@ -1956,6 +1958,8 @@ static int batch_rebuild(batch *b) {
   if ((rc = ensure_cap((void **)&b->d_tab_e, (void **)&b->h_tab_e, &b->cap_e, ne,
                        4 * sizeof(int32_t), b->stream)))
     return rc;
+  b->any_split = 0;
+  b->face_max = 0;
   int g = 0;
   nh = ne = 0;
   b->any_probes = 0;
@@ -1975,6 +1979,15 @@ static int batch_rebuild(batch *b) {
     if (m->has_cur) {
       op->cur_mode = m->cur.mode;
       memcpy(op->cur_box, m->cur.box, sizeof(op->cur_box));
+    }
+    op->tfsf_split = fdtd_tfsf_split(&s->dev, op);
+    if (op->tfsf_split) {
+      const int32_t ax = s->I + 2, ay = s->J + 2, az = s->K + 2;
+      int32_t f = ax * ay;
+      if (ay * az > f) f = ay * az;
+      if (ax * az > f) f = ax * az;
+      if (f > b->face_max) b->face_max = f;
+      b->any_split = 1;
     }
     b->h_steps[g] = m->first + m->done;
     if (s->dev.num_ant > 0) b->any_probes = 1;
@@ -2037,8 +2050,14 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
     if (b->any_probes) KL(fdtdk_batch_probes(b->d_devs, b->n_act, b->stream));
     KL(fdtdk_batch_half(1, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_h, b->n_h,
                         b->d_work, b->d_err, b->stream));
+    if (b->any_split)
+      KL(fdtdk_batch_faces(1, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
+                           b->stream));
     KL(fdtdk_batch_half(0, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_e, b->n_e,
                         b->d_work + 2, b->d_err, b->stream));
+    if (b->any_split)
+      KL(fdtdk_batch_faces(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
+                           b->stream));
     KL(fdtdk_batch_advance(b->d_steps, b->n_act, b->stream));
   }
   int finished = 0;

@@ -97,7 +97,37 @@ typedef struct {
   int32_t step_from_dev;    /* step = *step_base + step */
   int32_t cur_mode;         /* 0 none, 1..3 Ex/Ey/Ez current source */
   int32_t cur_box[6];
+  int32_t tfsf_split;       /* TMA kernels: TF/SF applied by the face pass */
+  int32_t pad_[3];
 } fdtd_op;
+
+/* Can the TF/SF corrections of this half-step run as a separate pass over
+ * the face cells after the curl kernel?  The reference applies, per cell,
+ * curl, TF/SF, CPML (and, for E, the current source) in that order; a face
+ * cell that is in no CPML slab and outside the current-source box has
+ * curl then TF/SF only, so adding the correction afterwards gives the same
+ * value.  Faces clear of every slab: i0 >= p+1 and i1 <= I-p-1 on each axis
+ * (the H faces are at i0-1 and i1). */
+static inline int fdtd_tfsf_split(const fdtd_dev *d, const fdtd_op *op) {
+  if (!op->tfsf_mode || !op->curl) return 0;
+  const int p = d->p;
+  if (d->i0 < p + 1 || d->j0 < p + 1 || d->k0 < p + 1) return 0;
+  if (d->i1 > d->I - p - 1 || d->j1 > d->J - p - 1 || d->k1 > d->K - p - 1) return 0;
+  if (d->i0 > d->i1 || d->j0 > d->j1 || d->k0 > d->k1) return 0;
+  if (op->cur_mode) { /* current box against the six face planes */
+    const int *b = op->cur_box;
+    const int lo[3] = {d->i0, d->j0, d->k0}, hi[3] = {d->i1, d->j1, d->k1};
+    for (int a = 0; a < 3; ++a) {
+      const int u = (a + 1) % 3, v = (a + 2) % 3;
+      const int cross = b[2 * u] <= hi[u] && b[2 * u + 1] >= lo[u] - 1 &&
+                        b[2 * v] <= hi[v] && b[2 * v + 1] >= lo[v] - 1;
+      const int on_lo = b[2 * a] <= lo[a] && b[2 * a + 1] >= lo[a] - 1;
+      const int on_hi = b[2 * a] <= hi[a] && b[2 * a + 1] >= hi[a];
+      if (cross && (on_lo || on_hi)) return 0;
+    }
+  }
+  return 1;
+}
 
 /* Launchers (fdtd_kernels.cu).  Return cudaError_t as int.  With valid
  * maps and op->curl set, the TMA-pipelined kernels run (fdtd_tma.cu);
@@ -154,6 +184,13 @@ unsigned long long fdtdk_launch_count(void);
 /* Records an error message for the calling thread (fdtd_last_error) and
  * returns code. */
 int fdtd_internal_fail(int code, const char *msg);
+
+/* TF/SF corrections of a split half-step over the face cells (single grid,
+ * and every active member of a batch whose op has tfsf_split set;
+ * max_cells_per_face sizes the blocks per member). */
+int fdtdk_faces(int hfam, const fdtd_dev *d, const fdtd_op *op, cudaStream_t s);
+int fdtdk_batch_faces(int hfam, const fdtd_dev *devs, const fdtd_op *ops, const int32_t *steps,
+                      int32_t n, int32_t max_cells_per_face, cudaStream_t s);
 
 /* Media from shapes into the six material arrays (sigma, eps; pitched). */
 int fdtdk_rasterize(const fdtd_dev *d, float *const sig[3], float *const eps[3],

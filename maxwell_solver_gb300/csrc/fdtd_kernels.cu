@@ -147,6 +147,125 @@ __global__ void __launch_bounds__(TX *TY) k_half_e(const fdtd_dev d, const fdtd_
   }
 }
 
+// ------------------------------------------------------ TF/SF face pass
+//
+// After a TMA curl kernel that skipped the TF/SF corrections
+// (fdtd_tfsf_split), they are applied here to the face cells.  In every
+// mode each corrected component takes corrections from the two faces of
+// one axis only (tfsf_e / tfsf_h), so the pass walks those face planes and
+// each thread writes the one component its plane's axis owns: no two
+// threads write the same value, and a cell on two faces gets each
+// component's correction exactly once, with the reference's expression.
+
+// Component (0..2 = x,y,z) whose correction comes from the faces normal to
+// `axis` in `mode`, or -1.  E: mode 1 ey<-z ez<-y; 2 ex<-z ez<-x;
+// 3 ex<-z ez<-x; 4 ex<-y ey<-x.  H: 1 hx<-z hz<-x; 2 hy<-z hz<-y;
+// 3 hx<-y hy<-x; 4 hx<-z hz<-x.
+__host__ __device__ __forceinline__ int face_owner(bool hfam, int mode, int axis) {
+  static constexpr signed char e_tab[5][3] = {{-1, -1, -1}, {-1, 2, 1}, {2, -1, 0},
+                                              {2, -1, 0}, {1, 0, -1}};
+  static constexpr signed char h_tab[5][3] = {{-1, -1, -1}, {2, -1, 0}, {-1, 2, 1},
+                                              {1, 0, -1}, {2, -1, 0}};
+  if (mode < 1 || mode > 4) return -1;
+  return hfam ? h_tab[mode][axis] : e_tab[mode][axis];
+}
+
+// One face plane of the pass (q = 0..3: the low and high face of the first
+// axis that owns a component, then of the second), as scalars: the plane
+// sits at index `at` on `axis`, and its cells run over u (x when the plane
+// contains x, so that a warp's accesses are contiguous) and v, both across
+// the TF/SF box widened by one cell below (the H faces sit at i0-1).
+struct FacePlane {
+  int axis, at, comp, nu, nv, u0, v0;
+  bool valid;
+};
+
+__device__ __forceinline__ int box_lo(const fdtd_dev &d, int a) {
+  return a == 0 ? d.i0 : (a == 1 ? d.j0 : d.k0);
+}
+__device__ __forceinline__ int box_hi(const fdtd_dev &d, int a) {
+  return a == 0 ? d.i1 : (a == 1 ? d.j1 : d.k1);
+}
+
+template <bool HFAM>
+__device__ __forceinline__ FacePlane face_plane(const fdtd_dev &d, int mode, int q) {
+  FacePlane f;
+  f.valid = false;
+  int seen = 0;
+  for (int a = 0; a < 3; ++a) {
+    const int c = face_owner(HFAM, mode, a);
+    if (c < 0) continue;
+    if (seen++ != q / 2) continue;
+    const int p0 = HFAM ? box_lo(d, a) - 1 : box_lo(d, a), p1 = box_hi(d, a);
+    if ((q & 1) && p1 == p0) return f;  // both faces on one plane: done once
+    f.axis = a;
+    f.at = (q & 1) ? p1 : p0;
+    f.comp = c;
+    const int u = a == 0 ? 1 : 0, v = a == 2 ? 1 : 2;
+    f.u0 = box_lo(d, u) - 1;
+    f.nu = box_hi(d, u) - f.u0 + 1;
+    f.v0 = box_lo(d, v) - 1;
+    f.nv = box_hi(d, v) - f.v0 + 1;
+    f.valid = true;
+  }
+  return f;
+}
+
+// The TF/SF expressions of tfsf_e / tfsf_h for one face cell, on the owned
+// component only (the corrections of the three components are independent).
+template <bool HFAM>
+__device__ __forceinline__ void face_cell(const fdtd_dev &d, int mode, const float *inc, int comp,
+                                          int i, int j, int k) {
+  const int64_t n = i + (int64_t)j * d.Ip + (int64_t)k * d.plane;
+  float *f = d.f[(HFAM ? 3 : 0) + comp] + n;
+  const float v0 = *f;
+  float vx = comp == 0 ? v0 : 0.f, vy = comp == 1 ? v0 : 0.f, vz = comp == 2 ? v0 : 0.f;
+  if (HFAM) {
+    tfsf_h(d, mode, inc, i, j, k, vx, vy, vz);
+  } else {
+    const Coef6 C = load_coef(d, n);
+    tfsf_e(d, mode, inc, i, j, k, C.exh, C.eyh, C.ezh, vx, vy, vz);
+  }
+  *f = comp == 0 ? vx : (comp == 1 ? vy : vz);
+}
+
+template <bool HFAM>
+__device__ __forceinline__ void face_plane_cells(const fdtd_dev &d, int mode, const float *inc,
+                                                 int q, int first, int stride) {
+  const FacePlane f = face_plane<HFAM>(d, mode, q);
+  if (!f.valid) return;
+  const int64_t total = (int64_t)f.nu * f.nv;
+  for (int64_t t = first; t < total; t += stride) {
+    const int u = f.u0 + (int)(t % f.nu), v = f.v0 + (int)(t / f.nu);
+    if (f.axis == 0) face_cell<HFAM>(d, mode, inc, f.comp, f.at, u, v);
+    else if (f.axis == 1) face_cell<HFAM>(d, mode, inc, f.comp, u, f.at, v);
+    else face_cell<HFAM>(d, mode, inc, f.comp, u, v, f.at);
+  }
+}
+
+// blockIdx.y = face plane 0..3
+template <bool HFAM>
+__global__ void k_faces(const fdtd_dev d, const fdtd_op op) {
+  const int mode = op.tfsf_mode, step = op_step(d, op);
+  const float *inc = HFAM ? inc_h_row(d, mode, step) : inc_e_row(d, mode, step);
+  face_plane_cells<HFAM>(d, mode, inc, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x,
+                         gridDim.x * blockDim.x);
+}
+
+// Batched: blockIdx.z = active member g (its op says whether it split),
+// blockIdx.y = face plane.
+template <bool HFAM>
+__global__ void k_batch_faces(const fdtd_dev *devs, const fdtd_op *ops, const int32_t *steps) {
+  const int g = blockIdx.z;
+  const fdtd_op &op = ops[g];
+  if (!op.tfsf_split) return;
+  const fdtd_dev &d = devs[g];
+  const int mode = op.tfsf_mode, step = steps[g] + op.step;
+  const float *inc = HFAM ? inc_h_row(d, mode, step) : inc_e_row(d, mode, step);
+  face_plane_cells<HFAM>(d, mode, inc, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x,
+                         gridDim.x * blockDim.x);
+}
+
 // --------------------------------------------------------------- probes
 
 // Records the six components at every probe into row *probe_row (one thread
@@ -550,6 +669,31 @@ int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_
   if (op->tfsf_mode || op->cur_mode)
     return launch_half(k_half_e<false, false>, d, op, s, ni, nj, nk);
   return 0;
+}
+
+int fdtdk_faces(int hfam, const fdtd_dev *d, const fdtd_op *op, cudaStream_t s) {
+  int32_t a = (d->I + 2) * (d->J + 2);
+  if ((d->J + 2) * (d->K + 2) > a) a = (d->J + 2) * (d->K + 2);
+  if ((d->I + 2) * (d->K + 2) > a) a = (d->I + 2) * (d->K + 2);
+  int bx = (a + 255) / 256;
+  if (bx > 152 * 2) bx = 152 * 2;
+  const dim3 grid(bx > 0 ? bx : 1, 4);
+  if (hfam) k_faces<true><<<grid, 256, 0, s>>>(*d, *op);
+  else k_faces<false><<<grid, 256, 0, s>>>(*d, *op);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_batch_faces(int hfam, const fdtd_dev *devs, const fdtd_op *ops, const int32_t *steps,
+                      int32_t n, int32_t max_cells_per_face, cudaStream_t s) {
+  if (n <= 0) return 0;
+  int bx = (max_cells_per_face + 255) / 256;
+  if (bx > 4) bx = 4;
+  const dim3 grid(bx > 0 ? bx : 1, 4, (unsigned)n);
+  if (hfam) k_batch_faces<true><<<grid, 256, 0, s>>>(devs, ops, steps);
+  else k_batch_faces<false><<<grid, 256, 0, s>>>(devs, ops, steps);
+  ++g_launches;
+  return (int)cudaGetLastError();
 }
 
 int fdtdk_probe_gather(const fdtd_dev *d, cudaStream_t s) {

@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
       kb = m.w;
       y0 = m1.z;
       i = m1.y + xo;
-      mode = op.tfsf_mode;
+      mode = op.tfsf_split ? 0 : op.tfsf_mode;  // split: the face pass applies it
       cm = op.cur_mode;
       use_mat = d.coef_mode == 1;
       tab_local = BATCH ? (use_mat && d.n_mat <= kStageTabMax) : tab_in_smem;
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
     const fdtd_op &op =
         BATCH ? *reinterpret_cast<const fdtd_op *>(st_item + H_STAGE + DESC_B) : op0;
     const int I = d.I, J = d.J, K = d.K, p = d.p;
-    const int mode = op.tfsf_mode;
+    const int mode = op.tfsf_split ? 0 : op.tfsf_mode;  // split: the face pass applies it
     const float *inc = mode ? inc_h_row(d, mode, m1.w) : nullptr;
     const float Chh = d.Chh, Che = d.Che;
     const int i = x0 + xo;
@@ -718,20 +718,28 @@ int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) {
   return e;
 }
 
+// The curl kernel, then (when the TF/SF corrections can be split off) the
+// face pass.
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
-  if (op->pml)
-    return launch(k_half_e_tma<true, false>, E_SMEM, &g_blocks_e[1], d, m, op, s, d->I, d->J,
-                  d->K, d->zc_e);
-  return launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, op, s, d->I, d->J,
-                d->K, d->zc_e);
+  fdtd_op o = *op;
+  o.tfsf_split = fdtd_tfsf_split(d, op);
+  const int e = o.pml ? launch(k_half_e_tma<true, false>, E_SMEM, &g_blocks_e[1], d, m, &o, s,
+                               d->I, d->J, d->K, d->zc_e)
+                      : launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, &o, s,
+                               d->I, d->J, d->K, d->zc_e);
+  if (e || !o.tfsf_split) return e;
+  return fdtdk_faces(0, d, &o, s);
 }
 
 int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
-  if (op->pml)
-    return launch(k_half_h_tma<true, false>, H_SMEM, &g_blocks_h[1], d, m, op, s, d->I - 1,
-                  d->J - 1, d->K - 1, d->zc_h);
-  return launch(k_half_h_tma<false, false>, H_SMEM, &g_blocks_h[0], d, m, op, s, d->I - 1,
-                d->J - 1, d->K - 1, d->zc_h);
+  fdtd_op o = *op;
+  o.tfsf_split = fdtd_tfsf_split(d, op);
+  const int e = o.pml ? launch(k_half_h_tma<true, false>, H_SMEM, &g_blocks_h[1], d, m, &o, s,
+                               d->I - 1, d->J - 1, d->K - 1, d->zc_h)
+                      : launch(k_half_h_tma<false, false>, H_SMEM, &g_blocks_h[0], d, m, &o, s,
+                               d->I - 1, d->J - 1, d->K - 1, d->zc_h);
+  if (e || !o.tfsf_split) return e;
+  return fdtdk_faces(1, d, &o, s);
 }
 
 int fdtdk_batch_half(int hfam, const fdtd_dev *devs, const void *maps, const fdtd_op *ops,
