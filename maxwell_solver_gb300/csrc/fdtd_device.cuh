@@ -232,6 +232,51 @@ __device__ __forceinline__ Coef6 load_coef(const fdtd_dev &d, int64_t n) {
   return d.coef_mode == 0 ? coef_from_arrays(d, n) : coef_from_table(d, __ldg(d.mat + n));
 }
 
+// One CPML axis of a cell's H update: the psi pair's recurrence from its
+// old value ps (stored back to *dst) and the field corrections
+// (gpu.h:644-685 Y, :604-642 X, :687-725 Z).
+__device__ __forceinline__ void h_corr_y(const fdtd_dev &d, int py, float2 ps, float2 *dst,
+                                         float dEz_y, float dEx_y, float &hx, float &hz) {
+  const float Che = d.Che, dx = d.dx;  // {psi_Hxy, psi_Hzy}
+  const float b = d.bH[py], c = d.cH[py];
+  const float v0 = b * ps.x + div_dx(d, c * dEz_y);
+  hx = hx - Che * v0 * dx;
+  const float v1 = b * ps.y + div_dx(d, c * dEx_y);
+  hz = hz + Che * v1 * dx;
+  *dst = make_float2(v0, v1);
+}
+__device__ __forceinline__ void h_corr_x(const fdtd_dev &d, int px, float2 ps, float2 *dst,
+                                         float dEz_x, float dEy_x, float &hy, float &hz) {
+  const float Che = d.Che, dx = d.dx;  // {psi_Hyx, psi_Hzx}
+  const float b = d.bH[px], c = d.cH[px];
+  const float v0 = b * ps.x + div_dx(d, c * dEz_x);
+  hy = hy + Che * v0 * dx;
+  const float v1 = b * ps.y + div_dx(d, c * dEy_x);
+  hz = hz - Che * v1 * dx;
+  *dst = make_float2(v0, v1);
+}
+__device__ __forceinline__ void h_corr_z(const fdtd_dev &d, int pz, float2 ps, float2 *dst,
+                                         float dEy_z, float dEx_z, float &hx, float &hy) {
+  const float Che = d.Che, dx = d.dx;  // {psi_Hxz, psi_Hyz}
+  const float b = d.bH[pz], c = d.cH[pz];
+  const float v0 = b * ps.x + div_dx(d, c * dEy_z);
+  hx = hx + Che * v0 * dx;
+  const float v1 = b * ps.y + div_dx(d, c * dEx_z);
+  hy = hy - Che * v1 * dx;
+  *dst = make_float2(v0, v1);
+}
+
+// psi pair addresses of a cell (H and E share the slab layouts).
+__device__ __forceinline__ float2 *psi_at_y(const fdtd_dev &d, int a, int i, int py, int k) {
+  return psi_pairs(d, a) + (i + py * (int64_t)d.I + k * 2 * (int64_t)d.p * d.I);
+}
+__device__ __forceinline__ float2 *psi_at_x(const fdtd_dev &d, int a, int px, int j, int k) {
+  return psi_pairs(d, a) + (px + j * 2 * (int64_t)d.p + k * 2 * (int64_t)d.p * d.J);
+}
+__device__ __forceinline__ float2 *psi_at_z(const fdtd_dev &d, int a, int i, int j, int pz) {
+  return psi_pairs(d, a) + (i + j * (int64_t)d.I + pz * d.IJ);
+}
+
 // New H of one cell from its old H and the six forward E differences:
 // curl (gpu.h:575-602), TF/SF, CPML Y (gpu.h:644-685), X (:604-642),
 // Z (:687-725).  px/py/pz: H-slab positions (-1 outside).
@@ -260,30 +305,9 @@ __device__ __forceinline__ void update_h_cell(const fdtd_dev &d, int mode, const
     if (py >= 0) y = *Y;
     if (px >= 0) x = *X;
     if (pz >= 0) z = *Z;
-    if (py >= 0) {  // {psi_Hxy, psi_Hzy}
-      const float b = d.bH[py], c = d.cH[py];
-      const float v0 = b * y.x + div_dx(d, c * dEz_y);
-      hx = hx - Che * v0 * dx;
-      const float v1 = b * y.y + div_dx(d, c * dEx_y);
-      hz = hz + Che * v1 * dx;
-      *Y = make_float2(v0, v1);
-    }
-    if (px >= 0) {  // {psi_Hyx, psi_Hzx}
-      const float b = d.bH[px], c = d.cH[px];
-      const float v0 = b * x.x + div_dx(d, c * dEz_x);
-      hy = hy + Che * v0 * dx;
-      const float v1 = b * x.y + div_dx(d, c * dEy_x);
-      hz = hz - Che * v1 * dx;
-      *X = make_float2(v0, v1);
-    }
-    if (pz >= 0) {  // {psi_Hxz, psi_Hyz}
-      const float b = d.bH[pz], c = d.cH[pz];
-      const float v0 = b * z.x + div_dx(d, c * dEy_z);
-      hx = hx + Che * v0 * dx;
-      const float v1 = b * z.y + div_dx(d, c * dEx_z);
-      hy = hy - Che * v1 * dx;
-      *Z = make_float2(v0, v1);
-    }
+    if (py >= 0) h_corr_y(d, py, y, Y, dEz_y, dEx_y, hx, hz);
+    if (px >= 0) h_corr_x(d, px, x, X, dEz_x, dEy_x, hy, hz);
+    if (pz >= 0) h_corr_z(d, pz, z, Z, dEy_z, dEx_z, hx, hy);
   }
 }
 
@@ -297,6 +321,42 @@ __device__ __forceinline__ void e_slabs(const fdtd_dev &d, int i, int j, int k, 
   px = (j_in && k_in) ? slab_e(i, d.I, d.p) : -1;
   py = (i_in && k_in) ? slab_e(j, d.J, d.p) : -1;
   pz = (i_in && j_in) ? slab_e(k, d.K, d.p) : -1;
+}
+
+// One CPML axis of a cell's E update (gpu.h:790-827 Y, :829-868 Z,
+// :765-788 X), as h_corr_*.
+__device__ __forceinline__ void e_corr_y(const fdtd_dev &d, int py, float2 ps, float2 *dst,
+                                         const Coef6 &C, float hz, float hz_jm, float hx,
+                                         float hx_jm, float &ex, float &ez) {
+  const float dx = d.dx;  // {psi_Exy, psi_Ezy}
+  const float b = d.bE[py], c = d.cE[py];
+  const float v0 = b * ps.x + div_dx(d, c * (hz - hz_jm));
+  ex = ex + C.exh * v0 * dx;
+  const float v1 = b * ps.y + div_dx(d, c * (hx - hx_jm));
+  ez = ez - C.ezh * v1 * dx;
+  *dst = make_float2(v0, v1);
+}
+__device__ __forceinline__ void e_corr_z(const fdtd_dev &d, int pz, float2 ps, float2 *dst,
+                                         const Coef6 &C, float hy, float hy_km, float hx,
+                                         float hx_km, float &ex, float &ey) {
+  const float dx = d.dx;  // {psi_Exz, psi_Eyz}
+  const float b = d.bE[pz], c = d.cE[pz];
+  const float v0 = b * ps.x + div_dx(d, c * (hy - hy_km));
+  ex = ex - C.exh * v0 * dx;
+  const float v1 = b * ps.y + div_dx(d, c * (hx - hx_km));
+  ey = ey + C.eyh * v1 * dx;
+  *dst = make_float2(v0, v1);
+}
+__device__ __forceinline__ void e_corr_x(const fdtd_dev &d, int px, float2 ps, float2 *dst,
+                                         const Coef6 &C, float hz, float hz_im, float hy,
+                                         float hy_im, float &ey, float &ez) {
+  const float dx = d.dx;  // {psi_Eyx, psi_Ezx}
+  const float b = d.bE[px], c = d.cE[px];
+  const float v0 = b * ps.x + div_dx(d, c * (hz - hz_im));
+  ey = ey - C.eyh * v0 * dx;
+  const float v1 = b * ps.y + div_dx(d, c * (hy - hy_im));
+  ez = ez + C.ezh * v1 * dx;
+  *dst = make_float2(v0, v1);
 }
 
 // New E of one cell: curl with the reference's guards (gpu.h:727-763),
@@ -327,30 +387,9 @@ __device__ __forceinline__ void update_e_cell(const fdtd_dev &d, int mode, const
     if (py >= 0) y = *Y;
     if (pz >= 0) z = *Z;
     if (px >= 0) x = *X;
-    if (py >= 0) {  // {psi_Exy, psi_Ezy}
-      const float b = d.bE[py], c = d.cE[py];
-      const float v0 = b * y.x + div_dx(d, c * (hz - hz_jm));
-      ex = ex + C.exh * v0 * dx;
-      const float v1 = b * y.y + div_dx(d, c * (hx - hx_jm));
-      ez = ez - C.ezh * v1 * dx;
-      *Y = make_float2(v0, v1);
-    }
-    if (pz >= 0) {  // {psi_Exz, psi_Eyz}
-      const float b = d.bE[pz], c = d.cE[pz];
-      const float v0 = b * z.x + div_dx(d, c * (hy - hy_km));
-      ex = ex - C.exh * v0 * dx;
-      const float v1 = b * z.y + div_dx(d, c * (hx - hx_km));
-      ey = ey + C.eyh * v1 * dx;
-      *Z = make_float2(v0, v1);
-    }
-    if (px >= 0) {  // {psi_Eyx, psi_Ezx}
-      const float b = d.bE[px], c = d.cE[px];
-      const float v0 = b * x.x + div_dx(d, c * (hz - hz_im));
-      ey = ey - C.eyh * v0 * dx;
-      const float v1 = b * x.y + div_dx(d, c * (hy - hy_im));
-      ez = ez + C.ezh * v1 * dx;
-      *X = make_float2(v0, v1);
-    }
+    if (py >= 0) e_corr_y(d, py, y, Y, C, hz, hz_jm, hx, hx_jm, ex, ez);
+    if (pz >= 0) e_corr_z(d, pz, z, Z, C, hy, hy_km, hx, hx_km, ex, ey);
+    if (px >= 0) e_corr_x(d, px, x, X, C, hz, hz_im, hy, hy_im, ey, ez);
   }
   if (cur) {  // E -= Ce?h * source * dx / dx / dx
     if (cur_mode == 1) ex = ex - C.exh * cur_src * dx / dx / dx;

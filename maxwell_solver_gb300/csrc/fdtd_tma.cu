@@ -522,8 +522,8 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
     const float Chh = d.Chh, Che = d.Che;
     const int i = x0 + xo;
     const int px = PML ? slab_h(i, I, p) : -1;
-    const bool x_special = px >= 0 || (mode && (i == d.i0 - 1 || i == d.i1));
-    bool valid[2], col_special[2];
+    const bool x_face = mode && (i == d.i0 - 1 || i == d.i1);
+    bool valid[2], col_face[2];  // col_face: a TF/SF face cell (not split off)
     int py[2];
     int64_t n0[2];
 #pragma unroll
@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
       const int j = y0 + r0 + 4 * c;
       valid[c] = i < I - 1 && j < J - 1;
       py[c] = PML ? slab_h(j, J, p) : -1;
-      col_special[c] = x_special || py[c] >= 0 || (mode && (j == d.j0 - 1 || j == d.j1));
+      col_face[c] = x_face || (mode && (j == d.j0 - 1 || j == d.j1));
       n0[c] = valid[c] ? i + (int64_t)j * d.Ip + (int64_t)kb * d.plane : 0;
     }
     int prev = s;
@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
       const float *sHy = sHx + BX * BY;
       const float *sHz = sHy + BX * BY;
       const int pz = PML ? slab_h(k, K, p) : -1;
-      const bool plane_special = pz >= 0 || (mode && (k == dp.k0 - 1 || k == dp.k1));
+      const bool plane_face = mode && (k == dp.k0 - 1 || k == dp.k1);
       const int64_t off = (int64_t)t * dp.plane;
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
@@ -570,15 +570,35 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
         const float dEz_x = sEz[eb + 1] - ez, dEy_x = sEy[eb + 1] - ey;
         const float dEy_z = sEy1[eb] - ey, dEx_z = sEx1[eb] - ex;
         float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
-        if (__any_sync(0xffffffffu, act && (col_special[c] || plane_special))) {
+        // lean path (curl, then at most one CPML axis) unless a cell is on
+        // a TF/SF face or in two slabs
+        const bool oth = __any_sync(0xffffffffu, act && (col_face[c] || plane_face));
+        const bool ax = PML && __any_sync(0xffffffffu, act && px >= 0);
+        const bool ay = PML && py[c] >= 0, az = PML && pz >= 0;
+        const int j = y0 + ty;
+        if (oth || (int)ax + (int)ay + (int)az > 1) {
           if (act) {
-            update_h_cell<true, PML>(dp, mode, inc, i, y0 + ty, k, px, py[c], pz, hx, hy, hz,
-                                     dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z);
+            update_h_cell<true, PML>(dp, mode, inc, i, j, k, px, py[c], pz, hx, hy, hz, dEz_y,
+                                     dEx_y, dEz_x, dEy_x, dEy_z, dEx_z);
           }
         } else {
           hx = Chh * hx + Che * (-dEz_y + dEy_z);
           hy = Chh * hy + Che * (-dEx_z + dEz_x);
           hz = Chh * hz + Che * (-dEy_x + dEx_y);
+          if (PML && act) {
+            if (ax) {
+              if (px >= 0) {
+                float2 *X = psi_at_x(dp, PSI_HX, px, j, k);
+                h_corr_x(dp, px, *X, X, dEz_x, dEy_x, hy, hz);
+              }
+            } else if (ay) {
+              float2 *Y = psi_at_y(dp, PSI_HY, i, py[c], k);
+              h_corr_y(dp, py[c], *Y, Y, dEz_y, dEx_y, hx, hz);
+            } else if (az) {
+              float2 *Z = psi_at_z(dp, PSI_HZ, i, j, pz);
+              h_corr_z(dp, pz, *Z, Z, dEy_z, dEx_z, hx, hy);
+            }
+          }
         }
         if (act) {
           dp.f[3][n0[c] + off] = hx;
