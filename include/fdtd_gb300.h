@@ -296,6 +296,9 @@ typedef struct {
   int32_t round_steps;    /* most steps per batch round between admissions
                              (0: 32) */
   int32_t one_at_a_time;  /* 1: plain FIFO queue through fdtd_step_n */
+  int64_t fill_cells;     /* cells stepped per round: the resident requests
+                             with the least remaining work are taken until
+                             their cells reach this (0: 2^25) */
 } fdtd_server_config;
 
 typedef struct {

@@ -13,9 +13,15 @@
  *   2. sets each admitted request up as an ordinary handle (SetParams,
  *      SetConst, SetShapes, SetAntennaLocations, ReadySimulation, Init1D):
  *      its fields, psi arrays and coefficients are resident from here on;
- *   3. advances every active request together with one fdtd_batch_step
- *      (at most round_steps steps; a round ends early when a member
- *      finishes);
+ *   3. picks the resident requests with the least remaining work (cells x
+ *      steps left) until their cells reach the fill target that keeps the
+ *      GPU busy, and advances those together with one fdtd_batch_step (at
+ *      most round_steps steps; a round ends early when a member finishes);
+ *      the others stay resident and wait -- shortest remaining work first,
+ *      so small solves are not held back by large ones sharing the device;
+ *      a round with a single request runs it with fdtd_step_n instead (the
+ *      plain solver's graph-replayed kernels, for grids that fill the GPU
+ *      alone);
  *   4. retires finished requests: outputs to host buffers, handle deleted,
  *      memory back to the budget, waiters woken.
  * Requests that arrive while others run are admitted at the next turn and
@@ -59,6 +65,10 @@ typedef struct req {
   char message[128];
   float *out_probes, *out_field;
   size_t n_out_probes, n_out_field;
+  /* batched mode: stepping this round, steps completed before its current
+   * stretch in the batch, and steps completed now */
+  int in_batch;
+  int32_t done_base, done;
   struct req *next;
 } req;
 
@@ -218,9 +228,47 @@ static void fail_active(server *S, int rc) {
   fdtd_batch_clear(S->batch);
 }
 
+static int64_t req_cells(const req *r) { return (int64_t)r->r.I * r->r.J * r->r.K; }
+
+static int by_remaining(const void *a, const void *b) {
+  const req *x = *(req *const *)a, *y = *(req *const *)b;
+  const double wx = (double)req_cells(x) * (x->r.steps - x->done);
+  const double wy = (double)req_cells(y) * (y->r.steps - y->done);
+  return wx < wy ? -1 : wx > wy;
+}
+
+/* This round's members: resident requests by least remaining work until
+ * their cells reach `fill`; members that drop out leave the batch (their
+ * state stays resident) and rejoin later at the step they reached.  A
+ * single member runs alone (*solo), outside the batch. */
+static int select_round(server *S, int64_t fill, req **solo) {
+  qsort(S->act, (size_t)S->n_act, sizeof(req *), by_remaining);
+  int n_want = 0;
+  for (int64_t cells = 0; n_want < S->n_act && cells < fill; ++n_want)
+    cells += req_cells(S->act[n_want]);
+  *solo = n_want == 1 ? S->act[0] : NULL;
+  for (int a = 0; a < S->n_act; ++a) {
+    req *r = S->act[a];
+    const int want = a < n_want && r != *solo;
+    int rc = FDTD_OK;
+    if (want && !r->in_batch) {
+      r->done_base = r->done;
+      rc = fdtd_batch_add(S->batch, r->h, r->done, r->r.steps - r->done, r->r.tfsf_mode, NULL);
+      r->in_batch = rc == FDTD_OK;
+    } else if (!want && r->in_batch) {
+      rc = fdtd_batch_remove(S->batch, r->h);
+      r->in_batch = 0;
+      r->done_base = r->done;
+    }
+    if (rc) return rc;
+  }
+  return FDTD_OK;
+}
+
 static void *serve_loop(void *arg) {
   server *S = (server *)arg;
   const int32_t round = S->cfg.round_steps > 0 ? S->cfg.round_steps : 32;
+  const int64_t fill = S->cfg.fill_cells > 0 ? S->cfg.fill_cells : ((int64_t)1 << 25);
   req *adm[ADMIT_MAX];
   pthread_mutex_lock(&S->mu);
   for (;;) {
@@ -267,7 +315,6 @@ static void *serve_loop(void *arg) {
         finish(S, r, rc, NULL);
         continue;
       }
-      if (!rc) rc = fdtd_batch_add(S->batch, r->h, 0, r->r.steps, r->r.tfsf_mode, NULL);
       if (rc) {
         drop_handle(S, r);
         finish(S, r, rc, NULL);
@@ -287,20 +334,39 @@ static void *serve_loop(void *arg) {
       S->act[S->n_act++] = r;
     }
 
-    /* 3. one batch round for every active request */
+    /* 3. the round's members, then one round: the batch, or one request
+     * alone through fdtd_step_n */
+    req *solo = NULL;
     if (S->n_act > 0) {
-      int32_t left = 0;
-      const int rc = fdtd_batch_step(S->batch, round, &left);
+      int rc = select_round(S, fill, &solo);
+      if (!rc && solo) {
+        const int32_t n = solo->r.steps - solo->done < round ? solo->r.steps - solo->done : round;
+        rc = fdtd_step_n(solo->h, solo->done, n, solo->r.tfsf_mode, NULL);
+        if (!rc) solo->done_base = solo->done + n;
+        else {
+          drop_handle(S, solo);
+          for (int a = 0; a < S->n_act; ++a)
+            if (S->act[a] == solo) S->act[a] = S->act[--S->n_act];
+          finish(S, solo, rc, NULL);
+          solo = NULL;
+          rc = FDTD_OK; /* only that request failed */
+        }
+      } else if (!rc) {
+        int32_t left = 0;
+        rc = fdtd_batch_step(S->batch, round, &left);
+      }
       if (rc) fail_active(S, rc);
     }
 
     /* 4. retire the finished ones (after checking the batch's pipelines
      * completed: a bounded wait that timed out invalidates the round) */
     int any = 0;
-    for (int a = 0; a < S->n_act && !any; ++a) {
-      int32_t done = 0;
-      fdtd_batch_progress(S->batch, S->act[a]->h, &done);
-      any = done >= S->act[a]->r.steps;
+    for (int a = 0; a < S->n_act; ++a) {
+      req *r = S->act[a];
+      int32_t p = 0;
+      if (r->in_batch) fdtd_batch_progress(S->batch, r->h, &p);
+      r->done = r->done_base + (p > 0 ? p : 0);
+      any |= r->done >= r->r.steps;
     }
     if (any) {
       const int rc = fdtd_batch_status(S->batch);
@@ -308,9 +374,7 @@ static void *serve_loop(void *arg) {
     }
     for (int a = 0; a < S->n_act;) {
       req *r = S->act[a];
-      int32_t done = 0;
-      fdtd_batch_progress(S->batch, r->h, &done);
-      if (done < r->r.steps) {
+      if (r->done < r->r.steps) {
         ++a;
         continue;
       }
