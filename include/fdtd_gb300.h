@@ -210,6 +210,17 @@ int fdtd_get_info(fdtd_handle h, fdtd_info *out);
  * Cexe Ceye Ceze Cexh Ceyh Cezh per id; coef_mode 1 only). */
 int fdtd_get_table(fdtd_handle h, int32_t which, float *out, size_t n);
 
+/* Checkpoint / resume (no reference counterpart): the evolving state of a
+ * ready handle -- the six fields, the CPML psi arrays, the step and probe
+ * counters and the probe record -- as an opaque byte image in host memory.
+ * Load it into a handle set up the same way (SetParams, SetConst, media,
+ * probes, ReadySimulation, Init1D) and stepping continues exactly as the
+ * saved handle would have (steps are numbered by the caller, as always).
+ * A different set-up is rejected with FDTD_ERR_INVALID_ARG. */
+int fdtd_checkpoint_size(fdtd_handle h, size_t *bytes);
+int fdtd_checkpoint_save(fdtd_handle h, void *buf, size_t n);
+int fdtd_checkpoint_load(fdtd_handle h, const void *buf, size_t n);
+
 /* Timing on the handle's stream (CUDA events).  slot 0..15. */
 int fdtd_event_record(fdtd_handle h, int32_t slot);
 int fdtd_event_elapsed_ms(fdtd_handle h, int32_t slot_a, int32_t slot_b, float *ms);

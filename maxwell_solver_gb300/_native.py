@@ -118,6 +118,9 @@ SIGNATURES = {
     "fdtd_synchronize": (ctypes.c_int, [U64]),
     "fdtd_get_info": (ctypes.c_int, [U64, ctypes.POINTER(FdtdInfo)]),
     "fdtd_get_table": (ctypes.c_int, [U64, I32, P, SZ]),
+    "fdtd_checkpoint_size": (ctypes.c_int, [U64, ctypes.POINTER(SZ)]),
+    "fdtd_checkpoint_save": (ctypes.c_int, [U64, P, SZ]),
+    "fdtd_checkpoint_load": (ctypes.c_int, [U64, P, SZ]),
     "fdtd_event_record": (ctypes.c_int, [U64, I32]),
     "fdtd_event_elapsed_ms": (ctypes.c_int, [U64, I32, I32, ctypes.POINTER(ctypes.c_float)]),
     "fdtd_profile_steps": (ctypes.c_int, [U64, I32, I32, I32, ctypes.POINTER(FdtdCurrent),

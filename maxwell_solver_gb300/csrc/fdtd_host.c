@@ -511,6 +511,7 @@ int fdtd_set_source(fdtd_handle h, const float *src, size_t n) {
 }
 
 static int flush(sim *s);
+static int check_device_error(sim *s);
 static int issue(sim *s, int hfam, const fdtd_op *op);
 
 /* src/simulation.h:1084-1095 */
@@ -1064,6 +1065,107 @@ int fdtd_update_cuda(fdtd_handle h) {
 }
 
 /* src/simulation.h:1128-1151 */
+/* ------------------------------------------------------------ checkpoint
+ * Image: header, the six pitched field arrays, the psi pool, the four
+ * device counters, the probe record.  Loading checks the header against
+ * the handle (same grid, CPML, steps, probes and coefficient mode). */
+typedef struct {
+  char magic[8];
+  int32_t version, I, J, K, Ip, p, T, num_ant, coef_mode, pad;
+  int64_t psi_floats, probe_floats;
+} ckpt_header;
+
+static void ckpt_describe(const sim *s, ckpt_header *hd) {
+  memset(hd, 0, sizeof(*hd));
+  memcpy(hd->magic, "FDTDCKP1", 8);
+  hd->version = 1;
+  hd->I = s->I;
+  hd->J = s->J;
+  hd->K = s->K;
+  hd->Ip = s->Ip;
+  hd->p = s->p;
+  hd->T = s->T;
+  hd->num_ant = s->d_probes ? s->num_ant : 0;
+  hd->coef_mode = s->coef_mode;
+  hd->psi_floats = 8 * (s->size_x + s->size_y + s->size_z);
+  hd->probe_floats = s->d_probes ? (int64_t)s->T * s->num_ant * 6 : 0;
+}
+
+static size_t ckpt_bytes(const ckpt_header *hd, const sim *s) {
+  return sizeof(*hd) + 6 * (size_t)s->cells * sizeof(float) +
+         (size_t)hd->psi_floats * sizeof(float) + 4 * sizeof(int32_t) +
+         (size_t)hd->probe_floats * sizeof(float);
+}
+
+int fdtd_checkpoint_size(fdtd_handle h, size_t *bytes) {
+  GET(h);
+  if (!bytes) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "checkpoints exist after ReadySimulation");
+  ckpt_header hd;
+  ckpt_describe(s, &hd);
+  *bytes = ckpt_bytes(&hd, s);
+  return FDTD_OK;
+}
+
+int fdtd_checkpoint_save(fdtd_handle h, void *buf, size_t n) {
+  GET(h);
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "checkpoints exist after ReadySimulation");
+  ckpt_header hd;
+  ckpt_describe(s, &hd);
+  if (!buf || n < ckpt_bytes(&hd, s))
+    return fail(FDTD_ERR_INVALID_ARG, "checkpoint needs %zu bytes", ckpt_bytes(&hd, s));
+  int rc = flush(s);
+  if (rc) return rc;
+  unsigned char *o = (unsigned char *)buf;
+  memcpy(o, &hd, sizeof(hd));
+  o += sizeof(hd);
+  const size_t fb = (size_t)s->cells * sizeof(float);
+  for (int a = 0; a < 6; ++a, o += fb)
+    CU(cudaMemcpyAsync(o, s->d_f[a], fb, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaMemcpyAsync(o, s->d_psi_pool, (size_t)hd.psi_floats * sizeof(float),
+                     cudaMemcpyDeviceToHost, s->stream));
+  o += (size_t)hd.psi_floats * sizeof(float);
+  CU(cudaMemcpyAsync(o, s->d_ctr, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+  o += 4 * sizeof(int32_t);
+  if (hd.probe_floats)
+    CU(cudaMemcpyAsync(o, s->d_probes, (size_t)hd.probe_floats * sizeof(float),
+                       cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return check_device_error(s);
+}
+
+int fdtd_checkpoint_load(fdtd_handle h, const void *buf, size_t n) {
+  GET(h);
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "checkpoints load after ReadySimulation");
+  ckpt_header want, got;
+  ckpt_describe(s, &want);
+  if (!buf || n < sizeof(got)) return fail(FDTD_ERR_INVALID_ARG, "not a checkpoint");
+  memcpy(&got, buf, sizeof(got));
+  if (memcmp(&got, &want, sizeof(got)) != 0)
+    return fail(FDTD_ERR_INVALID_ARG, "checkpoint of a different set-up (grid %dx%dx%d, "
+                "pml %d, %d steps, %d probes, coefficient mode %d)", got.I, got.J, got.K,
+                got.p, got.T, got.num_ant, got.coef_mode);
+  if (n < ckpt_bytes(&want, s))
+    return fail(FDTD_ERR_INVALID_ARG, "checkpoint truncated (%zu of %zu bytes)", n,
+                ckpt_bytes(&want, s));
+  int rc = flush(s);
+  if (rc) return rc;
+  const unsigned char *o = (const unsigned char *)buf + sizeof(got);
+  const size_t fb = (size_t)s->cells * sizeof(float);
+  for (int a = 0; a < 6; ++a, o += fb)
+    CU(cudaMemcpyAsync(s->d_f[a], o, fb, cudaMemcpyHostToDevice, s->stream));
+  CU(cudaMemcpyAsync(s->d_psi_pool, o, (size_t)want.psi_floats * sizeof(float),
+                     cudaMemcpyHostToDevice, s->stream));
+  o += (size_t)want.psi_floats * sizeof(float);
+  CU(cudaMemcpyAsync(s->d_ctr, o, 4 * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream));
+  o += 4 * sizeof(int32_t);
+  if (want.probe_floats)
+    CU(cudaMemcpyAsync(s->d_probes, o, (size_t)want.probe_floats * sizeof(float),
+                       cudaMemcpyHostToDevice, s->stream));
+  CU(cudaStreamSynchronize(s->stream)); /* the host buffer may go away */
+  return FDTD_OK;
+}
+
 int fdtd_reset_field_all(fdtd_handle h) {
   GET(h);
   if (!s->init_ready) return fail(FDTD_ERR_STATE, "ResetFieldAll requires ReadySimulation");

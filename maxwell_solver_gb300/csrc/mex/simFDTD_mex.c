@@ -284,6 +284,17 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     free(bg);
     free(sv);
     CHECK(rc);
+  } else if (strcmp(o, "savecheckpoint") == 0) {
+    size_t n = 0;
+    CHECK(fdtd_checkpoint_size(P, &n));
+    const mwSize dims[2] = {1, (mwSize)n};
+    plhs[0] = mxCreateNumericArray(2, dims, mxUINT8_CLASS, mxREAL);
+    CHECK(fdtd_checkpoint_save(P, mxGetData(plhs[0]), n));
+  } else if (strcmp(o, "loadcheckpoint") == 0) {
+    if (nrhs < 3) mexErrMsgIdAndTxt("simFDTD:InvalidInput", "checkpoint required.");
+    if (mxGetClassID(prhs[2]) != mxUINT8_CLASS)
+      mexErrMsgIdAndTxt("simFDTD:InvalidInput", "checkpoint must be uint8.");
+    CHECK(fdtd_checkpoint_load(P, mxGetData(prhs[2]), mxGetNumberOfElements(prhs[2])));
   } else if (strcmp(o, "outputant") == 0) {
     if (nrhs < 3) mexErrMsgIdAndTxt("simFDTD:InvalidInput", "OutAntSize required.");
     const size_t n = scalar_count(prhs[2]);

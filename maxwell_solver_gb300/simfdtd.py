@@ -189,6 +189,16 @@ def simFDTD(op: str, *args):  # noqa: N802 - mirrors the MATLAB entry point
         _check(lib.fdtd_set_params(P, ctypes.byref(pr)))
     elif o == "synchronize":
         _check(lib.fdtd_synchronize(P))
+    elif o == "savecheckpoint":
+        n = ctypes.c_size_t(0)
+        _check(lib.fdtd_checkpoint_size(P, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.uint8)
+        _check(lib.fdtd_checkpoint_save(P, _ptr(out), out.size))
+        return out
+    elif o == "loadcheckpoint":
+        need(1, "checkpoint required.")
+        buf = np.ascontiguousarray(a[0], dtype=np.uint8)
+        _check(lib.fdtd_checkpoint_load(P, _ptr(buf), buf.size))
     else:
         raise SimFDTDError("simFDTD:UnknownOperation", f"Unknown operation: {o}")
     return None

@@ -26,6 +26,7 @@ typedef enum {
   mxCHAR_CLASS = 4,
   mxDOUBLE_CLASS = 6,
   mxSINGLE_CLASS = 7,
+  mxUINT8_CLASS = 9,
   mxINT32_CLASS = 12,
   mxUINT32_CLASS = 13,
   mxUINT64_CLASS = 15

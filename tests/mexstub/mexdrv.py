@@ -12,7 +12,9 @@ import ctypes
 import numpy as np
 
 MX_CHAR, MX_DOUBLE, MX_SINGLE, MX_INT32, MX_UINT32, MX_UINT64 = 4, 6, 7, 12, 13, 15
+MX_UINT8 = 9
 _CLASS_OF = {
+    np.dtype(np.uint8): MX_UINT8,
     np.dtype(np.float64): MX_DOUBLE,
     np.dtype(np.float32): MX_SINGLE,
     np.dtype(np.int32): MX_INT32,
