@@ -79,6 +79,17 @@ int fdtd_set_source(fdtd_handle h, const float *src, size_t n);
 /* 'SetSource' with a 4th argument -- updateSource src/simulation.h:1084-1095. */
 int fdtd_update_source(fdtd_handle h, const float *src, size_t n);
 
+/* Oblique plane-wave incidence, TF/SF mode 5 (no reference counterpart:
+ * the reference has the axis-aligned modes 1-4 of src/simulation.h:330-369).
+ * Propagation along (sin t cos p, sin t sin p, cos t), E along
+ * cos(psi) theta_hat + sin(psi) phi_hat (radians).  Call after SetConst and
+ * before Init1D; Init1D then also runs the 1D line along that direction
+ * (speed matched to the 3D grid's numerical phase velocity there at the
+ * centre frequency fctr), and the PlaneWave ops / fdtd_step_n accept mode 5.
+ * Needs the TF/SF box at least one cell inside the CPML (tfsf_width >=
+ * pml + 1) and no current source on its faces. */
+int fdtd_set_incidence(fdtd_handle h, double theta, double phi, double psi);
+
 /* 'UpdateMaterial' -- src/simFDTD.cu:150-157, updateMaterial
  * src/simulation.h:288-328.  flag 1,2,3 = sigma_x,y,z; 4,5,6 = eps_x,y,z;
  * other flags are ignored.  Takes effect at ReadySimulation / UpdateCuda. */
@@ -298,6 +309,7 @@ typedef struct {
   const int32_t *probes;
   int32_t out_field;      /* OutputVis flag 1..6 of a field returned at the end,
                              0: none */
+  double theta, phi, psi; /* tfsf_mode 5: incidence (fdtd_set_incidence) */
 } fdtd_request;           /* everything is copied at submission */
 
 typedef struct {

@@ -53,7 +53,8 @@ class FdtdRequest(ctypes.Structure):
                 ("waveform", ctypes.POINTER(ctypes.c_float)),
                 ("bg_eps_r", ctypes.c_float), ("bg_sigma", ctypes.c_float),
                 ("shapes", ctypes.POINTER(FdtdShape)), ("n_shapes", I32),
-                ("n_probes", I32), ("probes", ctypes.POINTER(I32)), ("out_field", I32)]
+                ("n_probes", I32), ("probes", ctypes.POINTER(I32)), ("out_field", I32),
+                ("theta", ctypes.c_double), ("phi", ctypes.c_double), ("psi", ctypes.c_double)]
 
 
 class FdtdServerConfig(ctypes.Structure):
@@ -96,6 +97,8 @@ SIGNATURES = {
     "fdtd_set_source": (ctypes.c_int, [U64, P, SZ]),
     "fdtd_update_source": (ctypes.c_int, [U64, P, SZ]),
     "fdtd_update_material": (ctypes.c_int, [U64, I32, P, SZ]),
+    "fdtd_set_incidence": (ctypes.c_int, [U64, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double]),
     "fdtd_set_shapes": (ctypes.c_int, [U64, ctypes.c_float, ctypes.c_float,
                                        ctypes.POINTER(FdtdShape), I32]),
     "fdtd_create_mu": (ctypes.c_int, [U64, P, P, P, SZ]),

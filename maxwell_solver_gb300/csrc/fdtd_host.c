@@ -110,6 +110,12 @@ typedef struct sim {
   cudaEvent_t ev[MAX_EVENTS];
   float *d_f[6], *d_ce[6], *d_psi_pool, *d_psi[FDTD_NUM_PSI];
   float *d_den_ex, *d_den_hx, *d_inc[4], *d_src, *d_probes, *d_mu[3];
+  /* oblique plane wave (TF/SF mode 5) */
+  int has_ob;
+  double ob_theta, ob_phi, ob_psi;
+  float ob_k[3], ob_e[3], ob_h[3], ob_x0, ob_speed, ob_rho;
+  int32_t ob_r0[3], ob_w;
+  float *d_ob[2];
   int64_t *d_probe_idx;
   int32_t *d_ctr; /* [0] step base, [1] probe row, [2..3] work queue */
   int32_t *d_err; /* device error word (bounded-wait timeouts) */
@@ -368,6 +374,8 @@ int fdtd_destroy(fdtd_handle h) {
   }
   free(s->shapes);
   for (int a = 0; a < 4; ++a) dfree(s->d_inc[a]);
+  dfree(s->d_ob[0]);
+  dfree(s->d_ob[1]);
   for (int a = 0; a < 3; ++a) dfree(s->d_mu[a]);
   dfree(s->d_psi_pool);
   dfree(s->d_den_ex);
@@ -699,6 +707,17 @@ static void fill_dev_struct(sim *s) {
   for (int a = 0; a < FDTD_NUM_PSI; ++a) d->psi[a] = s->d_psi[a];
   for (int a = 0; a < 4; ++a) d->inc[a] = s->d_inc[a];
   d->src = s->d_src;
+  for (int a = 0; a < 3; ++a) {
+    d->ob_k[a] = s->ob_k[a];
+    d->ob_e[a] = s->ob_e[a];
+    d->ob_h[a] = s->ob_h[a];
+    d->ob_r0[a] = s->ob_r0[a];
+  }
+  d->ob_x0 = s->ob_x0;
+  d->ob_rho = s->ob_rho;
+  d->ob_w = s->ob_w;
+  d->ob_inc[0] = s->d_ob[0];
+  d->ob_inc[1] = s->d_ob[1];
   d->step_base = s->d_ctr;
   d->probe_row = s->d_ctr ? s->d_ctr + 1 : NULL;
   d->work = s->d_ctr ? s->d_ctr + 2 : NULL;
@@ -1207,6 +1226,132 @@ int fdtd_create_mu(fdtd_handle h, const float *mu_x, const float *mu_y, const fl
 }
 
 /* src/simulation.h:134-254 */
+/* ------------------------------------------------------ oblique incidence */
+
+int fdtd_set_incidence(fdtd_handle h, double theta, double phi, double psi) {
+  GET(h);
+  if (!s->init_const) return fail(FDTD_ERR_STATE, "SetIncidence requires SetConst");
+  if (s->init_1d) return fail(FDTD_ERR_STATE, "SetIncidence must precede Init1D");
+  if (!isfinite(theta) || !isfinite(phi) || !isfinite(psi))
+    return fail(FDTD_ERR_INVALID_ARG, "incidence angles must be finite");
+  s->has_ob = 1;
+  s->ob_theta = theta;
+  s->ob_phi = phi;
+  s->ob_psi = psi;
+  return FDTD_OK;
+}
+
+/* Numerical wavenumber of the 3D Yee grid in direction n at angular
+ * frequency w (cubic cells of size dx, time step dt):
+ * sum_a sin^2(k n_a dx / 2) = (dx / (c dt))^2 sin^2(w dt / 2), by Newton. */
+static double yee_wavenumber(const double n[3], double w, double dx, double dt) {
+  const double rhs = pow(dx / (k_c0 * dt) * sin(w * dt / 2), 2.0);
+  double k = w / k_c0;
+  for (int it = 0; it < 60; ++it) {
+    double f = -rhs, df = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      const double x = k * n[a] * dx / 2;
+      f += sin(x) * sin(x);
+      df += n[a] * dx * sin(x) * cos(x);
+    }
+    if (df == 0.0) break;
+    const double step = f / df;
+    k -= step;
+    if (fabs(step) < 1e-15 * fabs(k)) break;
+  }
+  return k;
+}
+
+/* The 1D line of an oblique plane wave: direction k = (sin t cos p,
+ * sin t sin p, cos t), E along cos(psi) theta_hat + sin(psi) phi_hat, H
+ * along k x E.  Its spacing dx1 = dx sqrt(k_x^4 + k_y^4 + k_z^4) matches
+ * the 3D grid's numerical dispersion in direction k to fourth order in
+ * (k dx) at every frequency; its speed factor then makes the wavenumbers
+ * equal at the source's centre frequency fctr.  The stored window spans
+ * the TF/SF box's projection on k. */
+static int init_1d_oblique(sim *s, float rate, const float *pw_source) {
+  const double t = s->ob_theta, p = s->ob_phi, q = s->ob_psi;
+  const double k[3] = {sin(t) * cos(p), sin(t) * sin(p), cos(t)};
+  const double th[3] = {cos(t) * cos(p), cos(t) * sin(p), -sin(t)}, ph[3] = {-sin(p), cos(p), 0};
+  double e[3], hv[3];
+  for (int a = 0; a < 3; ++a) e[a] = cos(q) * th[a] + sin(q) * ph[a];
+  hv[0] = k[1] * e[2] - k[2] * e[1];
+  hv[1] = k[2] * e[0] - k[0] * e[2];
+  hv[2] = k[0] * e[1] - k[1] * e[0];
+  const int lo[3] = {s->i0, s->j0, s->k0}, hi[3] = {s->i1, s->j1, s->k1};
+  double span = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    s->ob_k[a] = (float)k[a];
+    s->ob_e[a] = (float)e[a];
+    s->ob_h[a] = (float)hv[a];
+    s->ob_r0[a] = k[a] >= 0 ? lo[a] : hi[a];
+    span += fabs(k[a]) * (double)(hi[a] - lo[a]);
+  }
+  /* window coordinates x = ob_x0 + k.(r - r0): positions used lie within
+   * 1.5 cells of the box, i.e. |k.(r - r0)| beyond [0, span] by < 2.6 */
+  const double dx = s->delX, dt = s->delT;
+  double dx1 = dx * sqrt(pow(k[0], 4) + pow(k[1], 4) + pow(k[2], 4));
+  if (k_c0 * dt / dx1 > 0.995) dx1 = k_c0 * dt / 0.995; /* keep the line stable */
+  double speed = 1.0;
+  const double w = 2.0 * K_PI * (double)s->fctr;
+  if (w > 0) {
+    const double kn = yee_wavenumber(k, w, dx, dt);
+    const double sk = sin(kn * dx1 / 2);
+    if (sk > 0) speed = sin(w * dt / 2) * dx1 / (k_c0 * dt * sk);
+  }
+  if (speed * k_c0 * dt / dx1 > 0.999) speed = 0.999 * dx1 / (k_c0 * dt);
+  s->ob_speed = (float)speed;
+  s->ob_rho = (float)(dx / dx1);
+  /* window: positions used lie within 1.5 cells of the box */
+  s->ob_x0 = 4.0f * s->ob_rho;
+  s->ob_w = (int32_t)ceil((span + 2.6) * dx / dx1 + 4.0 * s->ob_rho) + 4;
+  const int T = s->T, W = s->ob_w;
+  const int m_src = T + 8, mb = m_src + 2, n1 = mb + W + T + 8;
+  int rc;
+  const size_t tab = (size_t)T * (size_t)W * sizeof(float);
+  for (int a = 0; a < 2; ++a) {
+    dfree(s->d_ob[a]);
+    s->d_ob[a] = NULL;
+    if ((rc = dalloc(s, (void **)&s->d_ob[a], tab))) return rc;
+  }
+  float *pw = (float *)malloc((size_t)T * sizeof(float));
+  if (!pw) return fail(FDTD_ERR_OOM, "out of host memory");
+  /* a soft source radiates ~1/(2 x Courant number) of its strength: scaled
+   * by the line's Courant number over the 3D grid's, the plane wave has the
+   * amplitude the axis-aligned modes give for the same PW_source */
+  const float gain = (float)(speed * dx / dx1);
+  for (int n = 0; n < T; ++n) {
+    const float v = pw_source[n] * rate;
+    pw[n] = v * gain;
+  }
+  float *d_pw = NULL, *scratch = NULL;
+  if ((rc = dalloc(s, (void **)&d_pw, (size_t)T * sizeof(float)))) {
+    free(pw);
+    return rc;
+  }
+  if (2 * (size_t)n1 * sizeof(float) > 200 * 1024 &&
+      (rc = dalloc(s, (void **)&scratch, 2 * (size_t)n1 * sizeof(float)))) {
+    free(pw);
+    return rc;
+  }
+  cudaMemcpyAsync(d_pw, pw, (size_t)T * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+  const float cE = (float)(speed * dt / K_EPS0 / dx1), cH = (float)(speed * dt / K_MU0 / dx1);
+  const int e2 = fdtdk_init_1d_oblique(n1, m_src, mb, W, T, cE, cH, d_pw, s->d_ob[0], s->d_ob[1],
+                                       scratch, s->stream);
+  const cudaError_t se = cudaStreamSynchronize(s->stream);
+  dfree(d_pw);
+  s->device_bytes -= (size_t)T * sizeof(float);
+  if (scratch) {
+    dfree(scratch);
+    s->device_bytes -= 2 * (size_t)n1 * sizeof(float);
+  }
+  free(pw);
+  fill_dev_struct(s);
+  if (e2) return fail(FDTD_ERR_CUDA, "oblique 1D launch: %s", cudaGetErrorString((cudaError_t)e2));
+  if (se != cudaSuccess) return fail(FDTD_ERR_CUDA, "oblique 1D: %s", cudaGetErrorString(se));
+  return FDTD_OK;
+}
+
 int fdtd_init_1d(fdtd_handle h, float rate, const float *pw_source, size_t n) {
   GET(h);
   if (!s->init_ready) return fail(FDTD_ERR_STATE, "Init1D requires ReadySimulation");
@@ -1235,7 +1380,7 @@ int fdtd_init_1d(fdtd_handle h, float rate, const float *pw_source, size_t n) {
   const size_t smem = 2 * (size_t)S * sizeof(float);
   if (smem > fdtdk_init_1d_smem_limit()) {
     if ((rc = dalloc(s, (void **)&scratch, 4 * (size_t)S * sizeof(float)))) {
-      cudaFree(d_pw);
+      dfree(d_pw);
       free(pw);
       return rc;
     }
@@ -1245,15 +1390,16 @@ int fdtd_init_1d(fdtd_handle h, float rate, const float *pw_source, size_t n) {
   const float Ceh = (float)((double)s->delT / K_EPS0 / (double)s->delX); /* :144 */
   int e = fdtdk_init_1d(&s->dev, s->d_inc, d_pw, Ceh, scratch, s->stream);
   cudaError_t se = cudaStreamSynchronize(s->stream);
-  cudaFree(d_pw);
+  dfree(d_pw);
   s->device_bytes -= (size_t)s->T * sizeof(float);
   if (scratch) {
-    cudaFree(scratch);
+    dfree(scratch);
     s->device_bytes -= 4 * (size_t)S * sizeof(float);
   }
   free(pw);
   if (e) return fail(FDTD_ERR_CUDA, "init_1d launch: %s", cudaGetErrorString((cudaError_t)e));
   if (se != cudaSuccess) return fail(FDTD_ERR_CUDA, "init_1d: %s", cudaGetErrorString(se));
+  if (s->has_ob && (rc = init_1d_oblique(s, rate, pw_source))) return rc;
   s->init_1d = 1;
   return FDTD_OK;
 }
@@ -1295,6 +1441,15 @@ static int tfsf_check(sim *s, int32_t step, int32_t mode) {
   if (!s->init_1d) return fail(FDTD_ERR_STATE, "PlaneWave update requires Init1D");
   if (step < 0 || step >= s->T)
     return fail(FDTD_ERR_INVALID_ARG, "time step %d outside [0, %d)", step, s->T);
+  if (mode == FDTD_MODE_OBLIQUE) {
+    if (!s->d_ob[0])
+      return fail(FDTD_ERR_STATE, "mode 5 needs SetIncidence before Init1D");
+    fdtd_op none;
+    memset(&none, 0, sizeof(none));
+    if (!fdtd_tfsf_faces_clear(&s->dev, &none))
+      return fail(FDTD_ERR_UNSUPPORTED, "mode 5 needs the TF/SF box at least one cell inside "
+                                        "the CPML (tfsf_width >= pml + 1)");
+  }
   if (mode >= 1 && mode <= 4) {
     if (s->i0 < 1 || s->j0 < 1 || s->k0 < 1 || s->i1 <= s->i0 || s->j1 <= s->j0 ||
         s->k1 <= s->k0)
@@ -1392,7 +1547,7 @@ int fdtd_update_h_planewave(fdtd_handle h, int32_t step, int32_t mode) {
   int rc = need_ready(s);
   if (rc) return rc;
   if ((rc = tfsf_check(s, step, mode))) return rc;
-  if (mode < 1 || mode > 4) return FDTD_OK;
+  if (mode < 1 || mode > FDTD_MODE_OBLIQUE) return FDTD_OK;
   fdtd_op st;
   memset(&st, 0, sizeof(st));
   st.tfsf_mode = mode;
@@ -1406,7 +1561,7 @@ int fdtd_update_e_planewave(fdtd_handle h, int32_t step, int32_t mode) {
   int rc = need_ready(s);
   if (rc) return rc;
   if ((rc = tfsf_check(s, step, mode))) return rc;
-  if (mode < 1 || mode > 4) return FDTD_OK;
+  if (mode < 1 || mode > FDTD_MODE_OBLIQUE) return FDTD_OK;
   fdtd_op st;
   memset(&st, 0, sizeof(st));
   st.tfsf_mode = mode;
@@ -1468,7 +1623,7 @@ int fdtd_step_n(fdtd_handle h, int32_t first, int32_t count, int32_t mode,
   if (rc) return rc;
   if (count < 0 || first < 0) return fail(FDTD_ERR_INVALID_ARG, "negative step range");
   if (count == 0) return FDTD_OK;
-  if (mode < 1 || mode > 4) mode = 0;
+  if (mode < 1 || mode > FDTD_MODE_OBLIQUE) mode = 0;
   const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
   if ((mode || use_cur) && (int64_t)first + count > s->T)
     return fail(FDTD_ERR_INVALID_ARG, "steps [%d, %d) exceed T=%d", first, first + count, s->T);
@@ -1526,7 +1681,7 @@ int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t mode
   int rc = need_ready(s);
   if (rc) return rc;
   if (!ms_out || count < 0) return fail(FDTD_ERR_INVALID_ARG, "bad profile arguments");
-  if (mode < 1 || mode > 4) mode = 0;
+  if (mode < 1 || mode > FDTD_MODE_OBLIQUE) mode = 0;
   const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
   if ((mode || use_cur) && (int64_t)first + count > s->T)
     return fail(FDTD_ERR_INVALID_ARG, "steps [%d, %d) exceed T=%d", first, first + count, s->T);
@@ -1831,6 +1986,7 @@ typedef struct batch {
   int *act;  /* member index of each active slot */
   int n_act, n_h, n_e, any_probes, dirty;
   int any_split;   /* some active member's TF/SF runs as the face pass */
+  int any_oblique; /* ... in mode 5 */
   int32_t face_max; /* largest face-plane area of those members */
 } batch;
 
@@ -1937,13 +2093,21 @@ int fdtd_batch_add(fdtd_batch bh, fdtd_handle h, int32_t first, int32_t count, i
   if (!s->init_ready) return fail(FDTD_ERR_STATE, "batch members need ReadySimulation");
   if (!s->maps.valid) return fail(FDTD_ERR_UNSUPPORTED, "batch members need the TMA kernels");
   if (first < 0 || count < 0) return fail(FDTD_ERR_INVALID_ARG, "negative step range");
-  if (mode < 1 || mode > 4) mode = 0;
+  if (mode < 1 || mode > FDTD_MODE_OBLIQUE) mode = 0;
   const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
   if ((mode || use_cur) && (int64_t)first + count > s->T)
     return fail(FDTD_ERR_INVALID_ARG, "steps [%d, %d) exceed T=%d", first, first + count, s->T);
   if (mode) {
     int rc = tfsf_check(s, first, mode);
     if (rc) return rc;
+  }
+  if (mode == FDTD_MODE_OBLIQUE && use_cur) { /* mode 5 runs as face passes only */
+    fdtd_op o;
+    memset(&o, 0, sizeof(o));
+    o.cur_mode = cur->mode;
+    memcpy(o.cur_box, cur->box, sizeof(o.cur_box));
+    if (!fdtd_tfsf_faces_clear(&s->dev, &o))
+      return fail(FDTD_ERR_UNSUPPORTED, "mode 5 with a current source on a TF/SF face");
   }
   if (use_cur && !s->init_src) return fail(FDTD_ERR_STATE, "current source requires SetSource");
   for (int i = 0; i < b->n; ++i)
@@ -2061,6 +2225,7 @@ static int batch_rebuild(batch *b) {
                        4 * sizeof(int32_t), b->stream)))
     return rc;
   b->any_split = 0;
+  b->any_oblique = 0;
   b->face_max = 0;
   int g = 0;
   nh = ne = 0;
@@ -2090,6 +2255,7 @@ static int batch_rebuild(batch *b) {
       if (ax * az > f) f = ax * az;
       if (f > b->face_max) b->face_max = f;
       b->any_split = 1;
+      if (op->tfsf_mode == FDTD_MODE_OBLIQUE) b->any_oblique = 1;
     }
     b->h_steps[g] = m->first + m->done;
     if (s->dev.num_ant > 0) b->any_probes = 1;
@@ -2155,11 +2321,17 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
     if (b->any_split)
       KL(fdtdk_batch_faces(1, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
                            b->stream));
+    if (b->any_oblique)
+      KL(fdtdk_batch_faces_oblique(1, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
+                                   b->stream));
     KL(fdtdk_batch_half(0, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_e, b->n_e,
                         b->d_work + 2, b->d_err, b->stream));
     if (b->any_split)
       KL(fdtdk_batch_faces(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
                            b->stream));
+    if (b->any_oblique)
+      KL(fdtdk_batch_faces_oblique(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
+                                   b->stream));
     KL(fdtdk_batch_advance(b->d_steps, b->n_act, b->stream));
   }
   int finished = 0;

@@ -72,6 +72,16 @@ typedef struct {
   int32_t num_ant;
   int32_t *err;             /* device error word (bounded-wait timeouts) */
   int32_t zc_h, zc_e;       /* z-planes per TMA work item (0: heuristic) */
+  /* oblique plane wave (TF/SF mode 5): unit propagation direction, E
+   * polarisation, H direction (k x e); the TF/SF box corner the wave reaches
+   * first; its coordinate in the stored 1D window; 1D nodes per cell along
+   * k; the window width; the window tables [T][ob_w] of the 1D E (at nodes)
+   * and H (at half nodes) */
+  float ob_k[3], ob_e[3], ob_h[3], ob_x0;
+  int32_t ob_r0[3], ob_w;
+  const float *ob_inc[2];
+  float ob_rho;
+  int32_t pad_;             /* size: a multiple of 16 bytes (bulk copies) */
 } fdtd_dev;
 
 /* TMA descriptors (CUtensorMap, 128 B each) of one grid: 0..5 = Ex Ey Ez Hx
@@ -108,8 +118,7 @@ typedef struct {
  * curl then TF/SF only, so adding the correction afterwards gives the same
  * value.  Faces clear of every slab: i0 >= p+1 and i1 <= I-p-1 on each axis
  * (the H faces are at i0-1 and i1). */
-static inline int fdtd_tfsf_split(const fdtd_dev *d, const fdtd_op *op) {
-  if (!op->tfsf_mode || !op->curl) return 0;
+static inline int fdtd_tfsf_faces_clear(const fdtd_dev *d, const fdtd_op *op) {
   const int p = d->p;
   if (d->i0 < p + 1 || d->j0 < p + 1 || d->k0 < p + 1) return 0;
   if (d->i1 > d->I - p - 1 || d->j1 > d->J - p - 1 || d->k1 > d->K - p - 1) return 0;
@@ -128,6 +137,16 @@ static inline int fdtd_tfsf_split(const fdtd_dev *d, const fdtd_op *op) {
   }
   return 1;
 }
+
+static inline int fdtd_tfsf_split(const fdtd_dev *d, const fdtd_op *op) {
+  if (!op->tfsf_mode || !op->curl) return 0;
+  return fdtd_tfsf_faces_clear(d, op);
+}
+
+/* TF/SF mode 5: an oblique plane wave (fdtd_set_incidence), applied only as
+ * face passes after the curl / CPML kernels, which needs the faces clear of
+ * the CPML and the current source (fdtd_tfsf_faces_clear). */
+#define FDTD_MODE_OBLIQUE 5
 
 /* Launchers (fdtd_kernels.cu).  Return cudaError_t as int.  With valid
  * maps and op->curl set, the TMA-pipelined kernels run (fdtd_tma.cu);
@@ -191,6 +210,15 @@ int fdtd_internal_fail(int code, const char *msg);
 int fdtdk_faces(int hfam, const fdtd_dev *d, const fdtd_op *op, cudaStream_t s);
 int fdtdk_batch_faces(int hfam, const fdtd_dev *devs, const fdtd_op *ops, const int32_t *steps,
                       int32_t n, int32_t max_cells_per_face, cudaStream_t s);
+
+int fdtdk_batch_faces_oblique(int hfam, const fdtd_dev *devs, const fdtd_op *ops,
+                              const int32_t *steps, int32_t n, int32_t max_cells_per_face,
+                              cudaStream_t s);
+/* The 1D line of an oblique plane wave for all T steps (one block; the line
+ * in shared memory, or in scratch[2*n1] when scratch is given). */
+int fdtdk_init_1d_oblique(int n1, int m_src, int mb, int w, int T, float cE, float cH,
+                          const float *pw, float *out_e, float *out_h, float *scratch,
+                          cudaStream_t s);
 
 /* Media from shapes into the six material arrays (sigma, eps; pitched). */
 int fdtdk_rasterize(const fdtd_dev *d, float *const sig[3], float *const eps[3],

@@ -266,6 +266,143 @@ __global__ void k_batch_faces(const fdtd_dev *devs, const fdtd_op *ops, const in
                          gridDim.x * blockDim.x);
 }
 
+// ---------------------------------------------- oblique plane wave (mode 5)
+//
+// The incident field of an oblique plane wave comes from a 1D FDTD line
+// along the propagation direction k (E at nodes, H at half nodes), run once
+// for all steps (k_init_1d_oblique) with its speed scaled so that its
+// numerical phase velocity equals the 3D grid's in direction k at the
+// source's centre frequency; the line extends T cells beyond the source on
+// both sides, so nothing reflected returns within T steps.  Only the window
+// spanning the TF/SF box's projection on k is stored per step:
+// ob_inc[0][n][w] = E before step n, ob_inc[1][n][w] = H after the H update
+// of step n (the reference's 1D bookkeeping, src/simulation.h:201-215).
+//
+// The line's spacing is dx * sqrt(k_x^4 + k_y^4 + k_z^4), which makes its
+// numerical dispersion agree with the 3D grid's in direction k to fourth
+// order in (k dx) at every frequency; the speed factor removes the residual
+// at the centre frequency.  A Yee component at position r (cells; Ex at
+// (i+1/2, j, k), Hx at (i, j+1/2, k+1/2), ...) sees e_c * E1(x) and
+// h_c * H1(x - 1/2) with x = ob_x0 + ob_rho * k . (r - r0) (1D nodes),
+// linearly interpolated in the window.
+
+// 1D line, one block: E[0..n1), H[0..n1-1) (H[m] at m + 1/2).
+__global__ void k_init_1d_oblique(float *E, float *H, int n1, int m_src, int mb, int w, int T,
+                                  float cE, float cH, const float *pw, float *out_e,
+                                  float *out_h) {
+  extern __shared__ float sh1d[];
+  if (!E) {  // the line fits in shared memory
+    E = sh1d;
+    H = sh1d + n1;
+  }
+  for (int m = threadIdx.x; m < n1; m += blockDim.x) E[m] = H[m] = 0.f;
+  __syncthreads();
+  for (int n = 0; n < T; ++n) {
+    for (int t = threadIdx.x; t < w; t += blockDim.x) out_e[(int64_t)n * w + t] = E[mb + t];
+    for (int m = threadIdx.x; m < n1 - 1; m += blockDim.x) H[m] = H[m] - cH * (E[m + 1] - E[m]);
+    __syncthreads();
+    for (int t = threadIdx.x; t < w; t += blockDim.x) out_h[(int64_t)n * w + t] = H[mb + t];
+    for (int m = 1 + threadIdx.x; m < n1 - 1; m += blockDim.x)
+      E[m] = E[m] - cE * (H[m] - H[m - 1]);
+    __syncthreads();
+    if (threadIdx.x == 0) E[m_src] = E[m_src] + pw[n];
+    __syncthreads();
+  }
+}
+
+// Window value at coordinate x (linear interpolation between nodes).
+__device__ __forceinline__ float ob_interp(const float *row, float x, int w) {
+  int m = (int)floorf(x);
+  m = m < 0 ? 0 : (m > w - 2 ? w - 2 : m);
+  const float f = x - (float)m;
+  return row[m] + f * (row[m + 1] - row[m]);
+}
+
+// Window coordinate of a point (px, py, pz) in cells: ob_rho 1D nodes per
+// cell of distance along k.
+__device__ __forceinline__ float ob_coord(const fdtd_dev &d, float px, float py, float pz) {
+  const float s = d.ob_k[0] * (px - (float)d.ob_r0[0]) + d.ob_k[1] * (py - (float)d.ob_r0[1]) +
+                  d.ob_k[2] * (pz - (float)d.ob_r0[2]);
+  return d.ob_x0 + d.ob_rho * s;
+}
+
+// Position of Yee component c of family E (or H) at cell index x[3].
+__device__ __forceinline__ void yee_pos(bool hfam, int c, const int x[3], float p[3]) {
+  for (int a = 0; a < 3; ++a) {
+    const bool half = hfam ? (a != c) : (a == c);
+    p[a] = (float)x[a] + (half ? 0.5f : 0.f);
+  }
+}
+
+// One axis of the oblique TF/SF corrections (faces normal to `axis`).
+// E pass: E_u and E_v on the faces' E planes take +-C * h_{v,u} H1 at the
+// half cell outside; H pass: H_v and H_u at that half cell take
+// +-Che * e_{u,v} E1 of the face plane (u, v = the axes after `axis`).  Sign:
+// + for (E_u, H_v) on the low face, - on the high face, opposite for
+// (E_v, H_u) -- the reference's axis modes are the special cases.
+// blockIdx.y = side * 2 + t (t = 0: pair (E_u, H_v), t = 1: pair (E_v, H_u)).
+template <bool HFAM>
+__device__ __forceinline__ void ob_face_cells(const fdtd_dev &d, int axis, int q, int step,
+                                              int first, int stride) {
+  const int side = q >> 1, t = q & 1;
+  const int u = (axis + 1) % 3, v = (axis + 2) % 3;
+  const int lo[3] = {d.i0, d.j0, d.k0}, hi[3] = {d.i1, d.j1, d.k1};
+  const int ce = t == 0 ? u : v;  // corrected E / source E component
+  const int ch = t == 0 ? v : u;  // corrected H / source H component
+  const bool plus = (t == 0) == (side == 0);
+  // tangential ranges of the pair: E_u spans [lo_u, hi_u-1] x [lo_v, hi_v]
+  const int nu = hi[u] - lo[u] + (ce == u ? 0 : 1), nv = hi[v] - lo[v] + (ce == v ? 0 : 1);
+  const int64_t total = (int64_t)nu * nv;
+  const int w = d.ob_w;
+  const float *rowE = d.ob_inc[0] + (int64_t)step * w;
+  const float *rowH = d.ob_inc[1] + (int64_t)step * w;
+  for (int64_t r = first; r < total; r += stride) {
+    int xe[3], xh[3];  // the E cell on the face plane, the H cell outside
+    xe[u] = lo[u] + (int)(r % nu);
+    xe[v] = lo[v] + (int)(r / nu);
+    xe[axis] = side ? hi[axis] : lo[axis];
+    xh[u] = xe[u];
+    xh[v] = xe[v];
+    xh[axis] = side ? hi[axis] : lo[axis] - 1;
+    float p[3];
+    if (HFAM) {  // H_ch at xh += +- Che * e_ce * E1(at the E_ce position)
+      yee_pos(false, ce, xe, p);
+      const float inc = d.ob_e[ce] * ob_interp(rowE, ob_coord(d, p[0], p[1], p[2]), w);
+      const int64_t n = xh[0] + (int64_t)xh[1] * d.Ip + (int64_t)xh[2] * d.plane;
+      float *f = d.f[3 + ch] + n;
+      const float val = d.Che * inc;
+      *f = plus ? *f + val : *f - val;
+    } else {  // E_ce at xe += +- C * h_ch * H1(at the H_ch position)
+      yee_pos(true, ch, xh, p);
+      const float inc =
+          d.ob_h[ch] * ob_interp(rowH, ob_coord(d, p[0], p[1], p[2]) - 0.5f, w);
+      const int64_t n = xe[0] + (int64_t)xe[1] * d.Ip + (int64_t)xe[2] * d.plane;
+      const Coef6 C = load_coef(d, n);
+      const float c = ce == 0 ? C.exh : (ce == 1 ? C.eyh : C.ezh);
+      float *f = d.f[ce] + n;
+      const float val = c * inc;
+      *f = plus ? *f + val : *f - val;
+    }
+  }
+}
+
+template <bool HFAM>
+__global__ void k_faces_oblique(const fdtd_dev d, const fdtd_op op, int axis) {
+  ob_face_cells<HFAM>(d, axis, blockIdx.y, op_step(d, op), blockIdx.x * blockDim.x + threadIdx.x,
+                      gridDim.x * blockDim.x);
+}
+
+// Batched: blockIdx.z = active member; members in other modes skip.
+template <bool HFAM>
+__global__ void k_batch_faces_oblique(const fdtd_dev *devs, const fdtd_op *ops,
+                                      const int32_t *steps, int axis) {
+  const int g = blockIdx.z;
+  const fdtd_op &op = ops[g];
+  if (!op.tfsf_split || op.tfsf_mode != FDTD_MODE_OBLIQUE) return;
+  ob_face_cells<HFAM>(devs[g], axis, blockIdx.y, steps[g] + op.step,
+                      blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
 // --------------------------------------------------------------- probes
 
 // Records the six components at every probe into row *probe_row (one thread
@@ -648,8 +785,23 @@ int launch_half(KH kern, const fdtd_dev *d, const fdtd_op *op, cudaStream_t s, i
 
 extern "C" {
 
+// Mode 5 (oblique): the curl / CPML / source kernels without TF/SF, then the
+// face passes (valid when the faces are clear of the CPML and the source).
+static int half_oblique(int hfam, const fdtd_dev *d, const fdtd_maps *m, int use_tma,
+                        const fdtd_op *op, cudaStream_t s) {
+  if (!d->ob_inc[0] || !fdtd_tfsf_faces_clear(d, op)) return (int)cudaErrorNotSupported;
+  fdtd_op o = *op;
+  o.tfsf_mode = 0;
+  int e = 0;
+  if (o.curl || o.pml || (!hfam && o.cur_mode))
+    e = hfam ? fdtdk_half_h(d, m, use_tma, &o, s) : fdtdk_half_e(d, m, use_tma, &o, s);
+  if (e) return e;
+  return fdtdk_faces(hfam, d, op, s);
+}
+
 int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s) {
+  if (op->tfsf_mode == FDTD_MODE_OBLIQUE) return half_oblique(1, d, m, use_tma, op, s);
   if (use_tma && m && m->valid && op->curl) return fdtdk_half_h_tma(d, m, op, s);
   const int ni = d->I - 1, nj = d->J - 1, nk = d->K - 1;
   if (op->curl && op->pml) return launch_half(k_half_h<true, true>, d, op, s, ni, nj, nk);
@@ -661,6 +813,7 @@ int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_
 
 int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s) {
+  if (op->tfsf_mode == FDTD_MODE_OBLIQUE) return half_oblique(0, d, m, use_tma, op, s);
   if (use_tma && m && m->valid && op->curl) return fdtdk_half_e_tma(d, m, op, s);
   const int ni = d->I, nj = d->J, nk = d->K;
   if (op->curl && op->pml) return launch_half(k_half_e<true, true>, d, op, s, ni, nj, nk);
@@ -672,6 +825,19 @@ int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_
 }
 
 int fdtdk_faces(int hfam, const fdtd_dev *d, const fdtd_op *op, cudaStream_t s) {
+  if (op->tfsf_mode == FDTD_MODE_OBLIQUE) {  // x, y, z faces in turn
+    int32_t a = (d->j1 - d->j0 + 1) * (d->k1 - d->k0 + 1);
+    if ((d->i1 - d->i0 + 1) * (d->k1 - d->k0 + 1) > a) a = (d->i1 - d->i0 + 1) * (d->k1 - d->k0 + 1);
+    if ((d->i1 - d->i0 + 1) * (d->j1 - d->j0 + 1) > a) a = (d->i1 - d->i0 + 1) * (d->j1 - d->j0 + 1);
+    int bx = (a + 255) / 256;
+    bx = bx < 1 ? 1 : (bx > 152 * 2 ? 152 * 2 : bx);
+    for (int axis = 0; axis < 3; ++axis) {
+      if (hfam) k_faces_oblique<true><<<dim3(bx, 4), 256, 0, s>>>(*d, *op, axis);
+      else k_faces_oblique<false><<<dim3(bx, 4), 256, 0, s>>>(*d, *op, axis);
+    }
+    g_launches += 3;
+    return (int)cudaGetLastError();
+  }
   int32_t a = (d->I + 2) * (d->J + 2);
   if ((d->J + 2) * (d->K + 2) > a) a = (d->J + 2) * (d->K + 2);
   if ((d->I + 2) * (d->K + 2) > a) a = (d->I + 2) * (d->K + 2);
@@ -692,6 +858,36 @@ int fdtdk_batch_faces(int hfam, const fdtd_dev *devs, const fdtd_op *ops, const 
   const dim3 grid(bx > 0 ? bx : 1, 4, (unsigned)n);
   if (hfam) k_batch_faces<true><<<grid, 256, 0, s>>>(devs, ops, steps);
   else k_batch_faces<false><<<grid, 256, 0, s>>>(devs, ops, steps);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_batch_faces_oblique(int hfam, const fdtd_dev *devs, const fdtd_op *ops,
+                              const int32_t *steps, int32_t n, int32_t max_cells_per_face,
+                              cudaStream_t s) {
+  if (n <= 0) return 0;
+  int bx = (max_cells_per_face + 255) / 256;
+  bx = bx < 1 ? 1 : (bx > 4 ? 4 : bx);
+  for (int axis = 0; axis < 3; ++axis) {
+    if (hfam) k_batch_faces_oblique<true><<<dim3(bx, 4, n), 256, 0, s>>>(devs, ops, steps, axis);
+    else k_batch_faces_oblique<false><<<dim3(bx, 4, n), 256, 0, s>>>(devs, ops, steps, axis);
+  }
+  g_launches += 3;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_init_1d_oblique(int n1, int m_src, int mb, int w, int T, float cE, float cH,
+                          const float *pw, float *out_e, float *out_h, float *scratch,
+                          cudaStream_t s) {
+  const size_t smem = 2 * (size_t)n1 * sizeof(float);
+  if (!scratch) {
+    cudaError_t e = cudaFuncSetAttribute(k_init_1d_oblique,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+  }
+  k_init_1d_oblique<<<1, 1024, scratch ? 0 : smem, s>>>(scratch, scratch ? scratch + n1 : nullptr,
+                                                        n1, m_src, mb, w, T, cE, cH, pw, out_e,
+                                                        out_h);
   ++g_launches;
   return (int)cudaGetLastError();
 }

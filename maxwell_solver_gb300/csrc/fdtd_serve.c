@@ -174,6 +174,7 @@ static int setup(req *r) {
   if ((rc = fdtd_set_params(r->h, &q->params))) return rc;
   if ((rc = fdtd_set_const(r->h, fr, td))) return rc;
   if ((rc = fdtd_set_shapes(r->h, q->bg_eps_r, q->bg_sigma, r->shapes, q->n_shapes))) return rc;
+  if (q->tfsf_mode == 5 && (rc = fdtd_set_incidence(r->h, q->theta, q->phi, q->psi))) return rc;
   if (q->n_probes > 0 &&
       (rc = fdtd_set_antenna_locations(r->h, r->probes, (size_t)q->n_probes * 3)))
     return rc;

@@ -259,6 +259,18 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     free(flag);
     free(v);
     CHECK(rc);
+  } else if (strcmp(o, "setincidence") == 0) {
+    /* SetIncidence(P, [theta phi psi]) in radians: TF/SF mode 5 */
+    if (nrhs < 3) mexErrMsgIdAndTxt("simFDTD:InvalidInput", "[theta phi psi] required.");
+    size_t na = 0;
+    double *ang = as_f64(prhs[2], &na);
+    if (na < 3) {
+      free(ang);
+      mexErrMsgIdAndTxt("simFDTD:InvalidInput", "[theta phi psi] required.");
+    }
+    int rc = fdtd_set_incidence(P, ang[0], ang[1], ang[2]);
+    free(ang);
+    CHECK(rc);
   } else if (strcmp(o, "setshapes") == 0) {
     /* SetShapes(P, [bg_eps_r bg_sigma], S): S is n x 9, one shape per row
      * [kind eps_r sigma g1 .. g6] (column-major, as MATLAB stores it) */

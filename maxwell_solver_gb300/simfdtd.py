@@ -137,6 +137,12 @@ def simFDTD(op: str, *args):  # noqa: N802 - mirrors the MATLAB entry point
         need(2, "flag, values required.")
         flag, v = _i32(a[0]), _f32(a[1])
         _check(lib.fdtd_update_material(P, int(flag[0]), _ptr(v), v.size))
+    elif o == "setincidence":
+        need(1, "[theta phi psi] required.")
+        v = np.asarray(a[0], dtype=np.float64).ravel()
+        if v.size < 3:
+            raise SimFDTDError("simFDTD:InvalidInput", "[theta phi psi] required.")
+        _check(lib.fdtd_set_incidence(P, float(v[0]), float(v[1]), float(v[2])))
     elif o == "setshapes":
         # [bg_eps_r bg_sigma], rows [kind eps_r sigma g0 .. g5] (FDTD_SHAPE_*)
         need(2, "background and shapes required.")

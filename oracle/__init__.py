@@ -27,7 +27,7 @@ COEFS = ("Cexe", "Ceye", "Ceze", "Cexh", "Ceyh", "Cezh")
 PSI = ("Exy", "Exz", "Eyx", "Eyz", "Ezx", "Ezy",
        "Hxy", "Hxz", "Hyx", "Hyz", "Hzx", "Hzy")
 ARRAYS = ("b_E", "c_E", "b_H", "c_H", "den_ex", "den_hx",
-          "Ez_1D", "Hy_1D", "E_inv_1D", "H_inv_1D", "probes")
+          "Ez_1D", "Hy_1D", "E_inv_1D", "H_inv_1D", "probes", "ob_E", "ob_H")
 
 _lock = threading.Lock()
 _lib = None
@@ -84,6 +84,7 @@ def _load():
                 f("set_antenna_locations").argtypes = [P, P]
                 f("ready_simulation").argtypes = [P]
                 f("init_1d").argtypes = [P, ctypes.c_float, P]
+                f("set_incidence").argtypes = [P] + [ctypes.c_double] * 3
                 f("update_cuda").argtypes = [P]
                 f("reset_field_all").argtypes = [P]
                 for n in ("update_h_all", "update_e_all", "update_h_pml", "update_e_pml"):
@@ -164,6 +165,10 @@ class OracleSim:
     def ready_simulation(self):
         self._f("ready_simulation")(self._h)
 
+    def set_incidence(self, theta, phi, psi):
+        """TF/SF mode 5 (oblique plane wave); before init_1d."""
+        assert self._f("set_incidence")(self._h, float(theta), float(phi), float(psi)) == 0
+
     def init_1d(self, rate, pw):
         a = np.ascontiguousarray(pw, dtype=np.float32)
         self._f("init_1d")(self._h, float(rate), _ptr(a))
@@ -206,7 +211,7 @@ class OracleSim:
     # --- readout ---
     def dim(self, which):
         names = ("I", "J", "K", "T", "numAnt", "p", "size1d",
-                 "i0", "i1", "j0", "j1", "k0", "k1")
+                 "i0", "i1", "j0", "j1", "k0", "k1", "ob_w")
         return int(self._f("dim")(self._h, names.index(which)))
 
     @property
@@ -238,7 +243,8 @@ class OracleSim:
         n = {"b_E": 2 * p, "c_E": 2 * p, "b_H": 2 * p, "c_H": 2 * p,
              "den_ex": I, "den_hx": I, "Ez_1D": T * s1, "Hy_1D": T * s1,
              "E_inv_1D": T * s1, "H_inv_1D": T * s1,
-             "probes": T * self.dim("numAnt") * 6}[name]
+             "probes": T * self.dim("numAnt") * 6,
+             "ob_E": T * max(self.dim("ob_w"), 0), "ob_H": T * max(self.dim("ob_w"), 0)}[name]
         return self._copy(self._f("array")(self._h, ARRAYS.index(name)), n)
 
     def scalar(self, name):

@@ -19,8 +19,13 @@
  * tests/test_oracle_golden.py checks this file against them.
  *
  * Extensions over the reference (all default to the reference's constants):
- * runtime CPML thickness / grading, TF/SF inset, and a probe gather that
- * records (Ex,Ey,Ez,Hx,Hy,Hz) at each probe at the start of every step.
+ * runtime CPML thickness / grading, TF/SF inset, a probe gather that
+ * records (Ex,Ey,Ez,Hx,Hy,Hz) at each probe at the start of every step, and
+ * TF/SF mode 5, an oblique plane wave (set_incidence): a 1D line along the
+ * propagation direction with its speed matched to the 3D grid's numerical
+ * phase velocity there, the incident field linearly interpolated from it at
+ * every Yee position of the six faces, faces corrected axis by axis (x, y,
+ * z).  It has no reference counterpart; it restates the library's mode 5.
  */
 #define _GNU_SOURCE
 #include <math.h>
@@ -78,6 +83,13 @@ typedef struct or_sim {
   real *Ez1d, *Hy1d, *Einv1d, *Hinv1d;
   size_t *ant_idx;
   real *probes; /* [T][numAnt][6] */
+  /* TF/SF mode 5 */
+  int has_ob;
+  double ob_theta, ob_phi, ob_psi;
+  real ob_k[3], ob_e[3], ob_h[3], ob_x0, ob_rho;
+  long ob_r0[3];
+  size_t ob_w;
+  real *obE, *obH; /* [T][ob_w] */
 } or_sim;
 
 static void *xcalloc(size_t n, size_t sz) {
@@ -112,7 +124,17 @@ void OR(destroy)(or_sim *s) {
   free(s->src);
   free(s->Ez1d); free(s->Hy1d); free(s->Einv1d); free(s->Hinv1d);
   free(s->ant_idx); free(s->probes);
+  free(s->obE); free(s->obH);
   free(s);
+}
+
+int OR(set_incidence)(or_sim *s, double theta, double phi, double psi) {
+  if (!s->init_const || s->init_1d) return -1;
+  s->has_ob = 1;
+  s->ob_theta = theta;
+  s->ob_phi = phi;
+  s->ob_psi = psi;
+  return 0;
 }
 
 /* Extension: CPML / TF/SF parameters; must precede set_const. */
@@ -420,6 +442,80 @@ static void run_1d(or_sim *s, real *Estore, real *Hstore, size_t src_at,
   free(E); free(H); free(psiE); free(psiH);
 }
 
+/* Mode 5: numerical wavenumber of the 3D grid in direction n at angular
+ * frequency w, sum_a sin^2(k n_a dx/2) = (dx/(c dt))^2 sin^2(w dt/2). */
+static double yee_wavenumber(const double n[3], double w, double dx, double dt) {
+  const double rhs = pow(dx / (k_c0 * dt) * sin(w * dt / 2), 2.0);
+  double k = w / k_c0;
+  for (int it = 0; it < 60; ++it) {
+    double f = -rhs, df = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      const double x = k * n[a] * dx / 2;
+      f += sin(x) * sin(x);
+      df += n[a] * dx * sin(x) * cos(x);
+    }
+    if (df == 0.0) break;
+    const double step = f / df;
+    k -= step;
+    if (fabs(step) < 1e-15 * fabs(k)) break;
+  }
+  return k;
+}
+
+/* Mode 5: the 1D line (E at nodes, H at half nodes) for all T steps; the
+ * window [mb, mb + ob_w) of E before each step and of H after its H
+ * update. */
+static void init_1d_oblique(or_sim *s, const real *pw) {
+  const double t = s->ob_theta, p = s->ob_phi, q = s->ob_psi;
+  const double k[3] = {sin(t) * cos(p), sin(t) * sin(p), cos(t)};
+  const double th[3] = {cos(t) * cos(p), cos(t) * sin(p), -sin(t)}, ph[3] = {-sin(p), cos(p), 0};
+  double e[3], hv[3];
+  for (int a = 0; a < 3; ++a) e[a] = cos(q) * th[a] + sin(q) * ph[a];
+  hv[0] = k[1] * e[2] - k[2] * e[1];
+  hv[1] = k[2] * e[0] - k[0] * e[2];
+  hv[2] = k[0] * e[1] - k[1] * e[0];
+  const size_t lo[3] = {s->i0, s->j0, s->k0}, hi[3] = {s->i1, s->j1, s->k1};
+  double span = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    s->ob_k[a] = (real)k[a];
+    s->ob_e[a] = (real)e[a];
+    s->ob_h[a] = (real)hv[a];
+    s->ob_r0[a] = (long)(k[a] >= 0 ? lo[a] : hi[a]);
+    span += fabs(k[a]) * (double)(hi[a] - lo[a]);
+  }
+  const double dx = (double)(float)s->delX, dt = (double)(float)s->delT;
+  double dx1 = dx * sqrt(pow(k[0], 4) + pow(k[1], 4) + pow(k[2], 4));
+  if (k_c0 * dt / dx1 > 0.995) dx1 = k_c0 * dt / 0.995;
+  double speed = 1.0;
+  const double w = 2.0 * 3.14159265358979323846 * (double)(float)s->fctr;
+  if (w > 0) {
+    const double kn = yee_wavenumber(k, w, dx, dt);
+    const double sk = sin(kn * dx1 / 2);
+    if (sk > 0) speed = sin(w * dt / 2) * dx1 / (k_c0 * dt * sk);
+  }
+  if (speed * k_c0 * dt / dx1 > 0.999) speed = 0.999 * dx1 / (k_c0 * dt);
+  const float rho = (float)(dx / dx1);
+  s->ob_rho = (real)rho;
+  s->ob_x0 = (real)(4.0f * rho);
+  s->ob_w = (size_t)ceil((span + 2.6) * dx / dx1 + 4.0 * rho) + 4;
+  const size_t T = s->T, W = s->ob_w;
+  const size_t m_src = T + 8, mb = m_src + 2, n1 = mb + W + T + 8;
+  const real cE = (real)(speed * dt / K_EPS0 / dx1), cH = (real)(speed * dt / K_MU0 / dx1);
+  const real gain = (real)(float)(speed * dx / dx1); /* source strength per line Courant */
+  real *E = (real *)xcalloc(n1, sizeof(real)), *H = (real *)xcalloc(n1, sizeof(real));
+  free(s->obE); free(s->obH);
+  s->obE = (real *)xcalloc(T * W, sizeof(real));
+  s->obH = (real *)xcalloc(T * W, sizeof(real));
+  for (size_t n = 0; n < T; ++n) {
+    memcpy(s->obE + n * W, E + mb, W * sizeof(real));
+    for (size_t m = 0; m + 1 < n1; ++m) H[m] = H[m] - cH * (E[m + 1] - E[m]);
+    memcpy(s->obH + n * W, H + mb, W * sizeof(real));
+    for (size_t m = 1; m + 1 < n1; ++m) E[m] = E[m] - cE * (H[m] - H[m - 1]);
+    E[m_src] = E[m_src] + pw[n] * gain;
+  }
+  free(E); free(H);
+}
+
 /* src/simulation.h:134-254 (init1D) */
 int OR(init_1d)(or_sim *s, float rate, const float *pw_source) {
   size_t S = s->I;
@@ -437,6 +533,7 @@ int OR(init_1d)(or_sim *s, float rate, const float *pw_source) {
    * the 1D CPML, kept so for other thicknesses (extension) */
   run_1d(s, s->Ez1d, s->Hy1d, S - (s->p + 3), pw);
   run_1d(s, s->Einv1d, s->Hinv1d, s->p + 3, pw);
+  if (s->has_ob) init_1d_oblique(s, pw);
   free(pw);
   s->init_1d = 1;
   return 0;
@@ -603,11 +700,83 @@ void OR(update_e_pml)(or_sim *s) {
 
 /* ----------------------------------------------------------- TF/SF faces */
 
+/* Mode 5 helpers: window value at coordinate x, window coordinate of a
+ * point, position of Yee component c of family E / H at cell x[3]. */
+static real ob_interp(const real *row, real x, size_t w) {
+  long m = (long)floor((double)x);
+  m = m < 0 ? 0 : (m > (long)w - 2 ? (long)w - 2 : m);
+  const real f = x - (real)m;
+  return row[m] + f * (row[m + 1] - row[m]);
+}
+static real ob_coord(const or_sim *s, real px, real py, real pz) {
+  const real v = s->ob_k[0] * (px - (real)s->ob_r0[0]) + s->ob_k[1] * (py - (real)s->ob_r0[1]) +
+                 s->ob_k[2] * (pz - (real)s->ob_r0[2]);
+  return s->ob_x0 + s->ob_rho * v;
+}
+static void yee_pos(int hfam, int c, const long x[3], real p[3]) {
+  for (int a = 0; a < 3; ++a) {
+    const int half = hfam ? (a != c) : (a == c);
+    p[a] = (real)x[a] + (half ? (real)0.5 : (real)0);
+  }
+}
+
+/* Mode 5, faces normal to each axis in turn (x, y, z): E pass, E_u and E_v
+ * on the face planes take +-C * h_{v,u} H1 at the half cell outside; H pass,
+ * H_v and H_u at that half cell take +-Che * e_{u,v} E1 of the face plane;
+ * + for (E_u, H_v) on the low face, - on the high face, opposite for
+ * (E_v, H_u). */
+static void oblique_faces(or_sim *s, int hfam, int n) {
+  const long lo[3] = {(long)s->i0, (long)s->j0, (long)s->k0};
+  const long hi[3] = {(long)s->i1, (long)s->j1, (long)s->k1};
+  const size_t W = s->ob_w;
+  const real *rowE = s->obE + (size_t)n * W, *rowH = s->obH + (size_t)n * W;
+  for (int axis = 0; axis < 3; ++axis) {
+    const int u = (axis + 1) % 3, v = (axis + 2) % 3;
+    for (int side = 0; side < 2; ++side)
+      for (int t = 0; t < 2; ++t) {
+        const int ce = t == 0 ? u : v, ch = t == 0 ? v : u;
+        const int plus = (t == 0) == (side == 0);
+        const long nu = hi[u] - lo[u] + (ce == u ? 0 : 1), nv = hi[v] - lo[v] + (ce == v ? 0 : 1);
+        for (long b = 0; b < nv; ++b)
+          for (long a = 0; a < nu; ++a) {
+            long xe[3], xh[3];
+            xe[u] = lo[u] + a;
+            xe[v] = lo[v] + b;
+            xe[axis] = side ? hi[axis] : lo[axis];
+            xh[u] = xe[u];
+            xh[v] = xe[v];
+            xh[axis] = side ? hi[axis] : lo[axis] - 1;
+            real p[3];
+            if (hfam) {
+              yee_pos(0, ce, xe, p);
+              const real inc = s->ob_e[ce] * ob_interp(rowE, ob_coord(s, p[0], p[1], p[2]), W);
+              real *f = &s->f[F_HX + ch][IDX(xh[0], xh[1], xh[2])];
+              const real val = s->Che * inc;
+              *f = plus ? *f + val : *f - val;
+            } else {
+              yee_pos(1, ch, xh, p);
+              const real inc =
+                  s->ob_h[ch] * ob_interp(rowH, ob_coord(s, p[0], p[1], p[2]) - (real)0.5, W);
+              const size_t id = IDX(xe[0], xe[1], xe[2]);
+              real *f = &s->f[F_EX + ce][id];
+              const real val = s->Ce[3 + ce][id] * inc;
+              *f = plus ? *f + val : *f - val;
+            }
+          }
+      }
+  }
+}
+
 /* H-side TF/SF corrections, src/simulation.h:330-349 with the launchers at
  * :421-492 and kernels at src/gpu.h:152-182 (mode 3), :217-247 (mode 4),
  * :424-477 (mode 1), :512-541 (mode 2).  c = +1 for every H launcher. */
 int OR(update_h_planewave)(or_sim *s, int n, int mode) {
   if (!s->init_1d || n < 0 || (size_t)n >= s->T) return -1;
+  if (mode == 5) {
+    if (!s->obE) return -1;
+    oblique_faces(s, 1, n);
+    return 0;
+  }
   const size_t I = s->I, IJ = s->IJ, S = s->size1d;
   const size_t i0 = s->i0, i1 = s->i1, j0 = s->j0, j1 = s->j1, k0 = s->k0, k1 = s->k1;
   const real Ch = s->Che; /* Chxe = Chye = Chze = Che, :920-922 */
@@ -671,6 +840,11 @@ int OR(update_h_planewave)(or_sim *s, int n, int mode) {
  * c=-1), :479-509 (mode 1, c=+1), :543-573 (mode 2, c=-1). */
 int OR(update_e_planewave)(or_sim *s, int n, int mode) {
   if (!s->init_1d || n < 0 || (size_t)n >= s->T) return -1;
+  if (mode == 5) {
+    if (!s->obE) return -1;
+    oblique_faces(s, 0, n);
+    return 0;
+  }
   const size_t I = s->I, IJ = s->IJ, S = s->size1d;
   const size_t i0 = s->i0, i1 = s->i1, j0 = s->j0, j1 = s->j1, k0 = s->k0, k1 = s->k1;
   real *Ex = s->f[F_EX], *Ey = s->f[F_EY], *Ez = s->f[F_EZ];
@@ -813,10 +987,13 @@ real *OR(array)(or_sim *s, int which) {
     case 8: return s->Einv1d;
     case 9: return s->Hinv1d;
     case 10: return s->probes;
+    case 11: return s->obE;
+    case 12: return s->obH;
   }
   return NULL;
 }
-/* 0 I,1 J,2 K,3 T,4 numAnt,5 p,6 size1d,7 i0,8 i1,9 j0,10 j1,11 k0,12 k1 */
+/* 0 I,1 J,2 K,3 T,4 numAnt,5 p,6 size1d,7 i0,8 i1,9 j0,10 j1,11 k0,12 k1,
+ * 13 ob_w */
 long long OR(dim)(or_sim *s, int which) {
   switch (which) {
     case 0: return (long long)s->I;
@@ -832,6 +1009,7 @@ long long OR(dim)(or_sim *s, int which) {
     case 10: return (long long)s->j1;
     case 11: return (long long)s->k0;
     case 12: return (long long)s->k1;
+    case 13: return (long long)s->ob_w;
   }
   return -1;
 }
