@@ -168,6 +168,8 @@ def cpu_oracle_rate(w, target_s: float, max_steps: int):
     for flag, arr in materials(w).items():
         o.update_material(flag, arr)
     o.ready_simulation()
+    if w.mode == 5:
+        o.set_incidence(*w.angles)
     o.init_1d(1.0, pw)
     o.step(0, w.mode)  # warm-up
     n, t0 = 1, time.perf_counter()
@@ -213,6 +215,7 @@ def workload_config(w):
     return {"workload": f"{w.name}: {w.dims[0]}x{w.dims[1]}x{w.dims[2]} Yee grid",
             "cells": w.cells, "pml": w.pml, "media": w.media, "tfsf_mode": w.mode,
             "probes": w.n_probes, "config_steps": w.steps,
+            **({"incidence_rad": [round(a, 6) for a in w.angles]} if w.mode == 5 else {}),
             "l2": (f"inputs larger than L2 (fields+coefficients {w.cells * 48 / 1e6:.0f} MB"
                    " > 129 MB), no flush needed" if w.cells * 48 > 129e6 else
                    f"state {w.cells * 48 / 1e6:.0f} MB fits in L2: not a headline configuration")}
@@ -344,6 +347,8 @@ def run_e2e(w, K, simFDTD, materials, probe_locations, sources):
     for flag, arr in mats.items():
         simFDTD("UpdateMaterial", P, np.int32(flag), arr)
     simFDTD("ReadySimulation", P)
+    if w.mode == 5:
+        simFDTD("SetIncidence", P, np.float64(w.angles))
     simFDTD("Init1D", P, np.float32(1.0), pw)
     simFDTD("UpdateCuda", P)
     simFDTD("ResetFieldAll", P)
@@ -433,7 +438,8 @@ def run_batched(n_grids: int, batched_only: bool = False):
     rate = lambda t: None if t is None else round(len(mix) / t, 3)  # noqa: E731
     return {
         "workload": f"c4: {len(mix)} grids, axes U{{32..128}}, 8-cell CPML, 0-10 spheres, "
-                    "TF/SF axis mode U{1..4}, f0 U[10,60] GHz, steps U[300,1500] (seed 3)",
+                    "TF/SF oblique plane wave (mode 5, seeded angles), f0 U[10,60] GHz, "
+                    "steps U[300,1500] (seed 3)",
         "solves": len(mix),
         "batched_solves_per_s": rate(t_batch),
         "one_at_a_time_solves_per_s": rate(t_one),
@@ -506,8 +512,9 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4):
                            plain["p99_s"] / max(served["p99_s"], 1e-9), 2)})
     return {
         "workload": f"c5: {len(specs)} requests (seed {seed}), cubic-ish axes log-U[48,384], "
-                    "CPML 8..16, spheres or layers, steps U[200,4000], TF/SF mode 1..4, "
-                    "8 probes each; Poisson arrivals",
+                    "CPML 8..16, spheres (oblique TF/SF, mode 5) or layers (mode 1), "
+                    "steps U[200,4000], 8 probes each; Poisson arrivals; requests of >= 2^22 "
+                    "cells run alone between batched rounds of the smaller ones",
         "hbm_budget_GB": budget_gb, "capacity_solves_per_s": capacity,
         "saturated": cap, "loads": points, "identical_results": bool(same),
         "timing": "wall clock from each request's submission to its result on the host "

@@ -322,6 +322,10 @@ typedef struct {
   int64_t fill_cells;     /* cells stepped per round: the resident requests
                              with the least remaining work are taken until
                              their cells reach this (0: 2^25) */
+  int64_t solo_cells;     /* a request of at least this many cells fills the
+                             device alone: it runs by itself (fdtd_step_n)
+                             when its turn comes, and the batched rounds take
+                             only the smaller ones (0: 2^22; -1: never) */
 } fdtd_server_config;
 
 typedef struct {

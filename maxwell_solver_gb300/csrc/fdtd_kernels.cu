@@ -326,81 +326,116 @@ __device__ __forceinline__ float ob_coord(const fdtd_dev &d, float px, float py,
   return d.ob_x0 + d.ob_rho * s;
 }
 
-// Position of Yee component c of family E (or H) at cell index x[3].
-__device__ __forceinline__ void yee_pos(bool hfam, int c, const int x[3], float p[3]) {
-  for (int a = 0; a < 3; ++a) {
-    const bool half = hfam ? (a != c) : (a == c);
-    p[a] = (float)x[a] + (half ? 0.5f : 0.f);
-  }
+// The oblique TF/SF corrections, one face plane per blockIdx.y = q (0..11):
+// the faces normal to AXIS = q / 4, SIDE = (q / 2) % 2 (low, high), pair
+// P = q % 2 (0: E_u with H_v, 1: E_v with H_u; u, v = the axes after AXIS).
+// E pass: E_ce on the face's E plane takes +-C * h_ch * H1 of the H cell
+// half a cell outside; H pass: H_ch at that half cell takes +-Che * e_ce *
+// E1 of the face plane.  Sign: + for (E_u, H_v) on the low face, - on the
+// high face, opposite for (E_v, H_u) -- the reference's axis modes are the
+// special cases.  Tangential ranges: E_ce and H_ch span [lo, hi-1] along ce
+// and [lo, hi] along ch.
+//
+// The corrections are applied plane after plane in the order (AXIS, SIDE)
+// (the oracle's loops).  H planes never share an element: H_ch is corrected
+// by the faces of AXIS and of ce, and along ce the H_ch plane of AXIS spans
+// [lo, hi-1], inside the ce faces' H planes at lo-1 and hi.  E planes share
+// the box edges: E_ce is corrected by the faces of AXIS and of ch, and along
+// ch the E_ce plane of AXIS spans [lo, hi], which holds the ch faces.
+// The plane that comes first in the order owns such an element and applies
+// all its corrections in order, so that each element has one writer and its
+// additions happen in the oracle's sequence.
+template <int A, int CE>
+__device__ __forceinline__ float ob_e_corr(const fdtd_dev &d, const float *rowH, int x0, int x1,
+                                           int x2, int side, float c, float val) {
+  constexpr int CH = 3 - A - CE;            // the H component the face pairs with E_ce
+  constexpr bool T0 = CE == (A + 1) % 3;    // pair (E_u, H_v)
+  const int lo = A == 0 ? d.i0 : (A == 1 ? d.j0 : d.k0);
+  const int hi = A == 0 ? d.i1 : (A == 1 ? d.j1 : d.k1);
+  const int xa = side ? hi : lo - 1;        // the H cell outside the face
+  const float p0 = (float)(A == 0 ? xa : x0) + (CH != 0 ? 0.5f : 0.f);
+  const float p1 = (float)(A == 1 ? xa : x1) + (CH != 1 ? 0.5f : 0.f);
+  const float p2 = (float)(A == 2 ? xa : x2) + (CH != 2 ? 0.5f : 0.f);
+  const float inc = d.ob_h[CH] * ob_interp(rowH, ob_coord(d, p0, p1, p2) - 0.5f, d.ob_w);
+  const float t = c * inc;
+  return (T0 == (side == 0)) ? val + t : val - t;
 }
 
-// One axis of the oblique TF/SF corrections (faces normal to `axis`).
-// E pass: E_u and E_v on the faces' E planes take +-C * h_{v,u} H1 at the
-// half cell outside; H pass: H_v and H_u at that half cell take
-// +-Che * e_{u,v} E1 of the face plane (u, v = the axes after `axis`).  Sign:
-// + for (E_u, H_v) on the low face, - on the high face, opposite for
-// (E_v, H_u) -- the reference's axis modes are the special cases.
-// blockIdx.y = side * 2 + t (t = 0: pair (E_u, H_v), t = 1: pair (E_v, H_u)).
-template <bool HFAM>
-__device__ __forceinline__ void ob_face_cells(const fdtd_dev &d, int axis, int q, int step,
-                                              int first, int stride) {
-  const int side = q >> 1, t = q & 1;
-  const int u = (axis + 1) % 3, v = (axis + 2) % 3;
+template <bool HFAM, int Q>
+__device__ __forceinline__ void ob_plane(const fdtd_dev &d, int step, int first, int stride) {
+  constexpr int AXIS = Q >> 2, SIDE = (Q >> 1) & 1, P = Q & 1;
+  constexpr int U = (AXIS + 1) % 3, V = (AXIS + 2) % 3;
+  constexpr int CE = P == 0 ? U : V, CH = P == 0 ? V : U;
+  constexpr int F = U < V ? U : V, G = U < V ? V : U;  // F: the thread-fastest axis
   const int lo[3] = {d.i0, d.j0, d.k0}, hi[3] = {d.i1, d.j1, d.k1};
-  const int ce = t == 0 ? u : v;  // corrected E / source E component
-  const int ch = t == 0 ? v : u;  // corrected H / source H component
-  const bool plus = (t == 0) == (side == 0);
-  // tangential ranges of the pair: E_u spans [lo_u, hi_u-1] x [lo_v, hi_v]
-  const int nu = hi[u] - lo[u] + (ce == u ? 0 : 1), nv = hi[v] - lo[v] + (ce == v ? 0 : 1);
-  const int64_t total = (int64_t)nu * nv;
+  const int nf = hi[F] - lo[F] + (CE == F ? 0 : 1), ng = hi[G] - lo[G] + (CE == G ? 0 : 1);
+  const int64_t total = (int64_t)nf * ng;
   const int w = d.ob_w;
-  const float *rowE = d.ob_inc[0] + (int64_t)step * w;
-  const float *rowH = d.ob_inc[1] + (int64_t)step * w;
+  const float *row = d.ob_inc[HFAM ? 0 : 1] + (int64_t)step * w;
   for (int64_t r = first; r < total; r += stride) {
-    int xe[3], xh[3];  // the E cell on the face plane, the H cell outside
-    xe[u] = lo[u] + (int)(r % nu);
-    xe[v] = lo[v] + (int)(r / nu);
-    xe[axis] = side ? hi[axis] : lo[axis];
-    xh[u] = xe[u];
-    xh[v] = xe[v];
-    xh[axis] = side ? hi[axis] : lo[axis] - 1;
-    float p[3];
-    if (HFAM) {  // H_ch at xh += +- Che * e_ce * E1(at the E_ce position)
-      yee_pos(false, ce, xe, p);
-      const float inc = d.ob_e[ce] * ob_interp(rowE, ob_coord(d, p[0], p[1], p[2]), w);
-      const int64_t n = xh[0] + (int64_t)xh[1] * d.Ip + (int64_t)xh[2] * d.plane;
-      float *f = d.f[3 + ch] + n;
-      const float val = d.Che * inc;
-      *f = plus ? *f + val : *f - val;
-    } else {  // E_ce at xe += +- C * h_ch * H1(at the H_ch position)
-      yee_pos(true, ch, xh, p);
-      const float inc =
-          d.ob_h[ch] * ob_interp(rowH, ob_coord(d, p[0], p[1], p[2]) - 0.5f, w);
-      const int64_t n = xe[0] + (int64_t)xe[1] * d.Ip + (int64_t)xe[2] * d.plane;
+    int x[3];
+    x[F] = lo[F] + (int)(r % nf);
+    x[G] = lo[G] + (int)(r / nf);
+    if (HFAM) {  // H_ch at the half cell outside += +- Che * e_ce * E1(E_ce position)
+      x[AXIS] = SIDE ? hi[AXIS] : lo[AXIS];
+      const float p0 = (float)x[0] + (CE == 0 ? 0.5f : 0.f);
+      const float p1 = (float)x[1] + (CE == 1 ? 0.5f : 0.f);
+      const float p2 = (float)x[2] + (CE == 2 ? 0.5f : 0.f);
+      const float inc = d.ob_e[CE] * ob_interp(row, ob_coord(d, p0, p1, p2), w);
+      x[AXIS] = SIDE ? hi[AXIS] : lo[AXIS] - 1;
+      const int64_t n = x[0] + (int64_t)x[1] * d.Ip + (int64_t)x[2] * d.plane;
+      float *f = d.f[3 + CH] + n;
+      const float t = d.Che * inc;
+      *f = (P == 0) == (SIDE == 0) ? *f + t : *f - t;
+    } else {
+      x[AXIS] = SIDE ? hi[AXIS] : lo[AXIS];
+      const bool on_ch_lo = x[CH] == lo[CH], on_ch_hi = x[CH] == hi[CH];
+      const bool flat = lo[AXIS] == hi[AXIS];  // both faces of AXIS on one plane
+      if (CH < AXIS && (on_ch_lo || on_ch_hi)) continue;  // owned by a face of CH
+      if (SIDE == 1 && flat) continue;                    // owned by the low face
+      const int64_t n = x[0] + (int64_t)x[1] * d.Ip + (int64_t)x[2] * d.plane;
       const Coef6 C = load_coef(d, n);
-      const float c = ce == 0 ? C.exh : (ce == 1 ? C.eyh : C.ezh);
-      float *f = d.f[ce] + n;
-      const float val = c * inc;
-      *f = plus ? *f + val : *f - val;
+      const float c = CE == 0 ? C.exh : (CE == 1 ? C.eyh : C.ezh);
+      float *f = d.f[CE] + n;
+      float val = ob_e_corr<AXIS, CE>(d, row, x[0], x[1], x[2], SIDE, c, *f);
+      if (SIDE == 0 && flat) val = ob_e_corr<AXIS, CE>(d, row, x[0], x[1], x[2], 1, c, val);
+      if (CH > AXIS) {
+        if (on_ch_lo) val = ob_e_corr<CH, CE>(d, row, x[0], x[1], x[2], 0, c, val);
+        if (on_ch_hi) val = ob_e_corr<CH, CE>(d, row, x[0], x[1], x[2], 1, c, val);
+      }
+      *f = val;
     }
   }
 }
 
 template <bool HFAM>
-__global__ void k_faces_oblique(const fdtd_dev d, const fdtd_op op, int axis) {
-  ob_face_cells<HFAM>(d, axis, blockIdx.y, op_step(d, op), blockIdx.x * blockDim.x + threadIdx.x,
-                      gridDim.x * blockDim.x);
+__device__ __forceinline__ void ob_planes(const fdtd_dev &d, int q, int step, int first,
+                                          int stride) {
+  switch (q) {
+#define OB_Q(Q) \
+  case Q: ob_plane<HFAM, Q>(d, step, first, stride); break;
+    OB_Q(0) OB_Q(1) OB_Q(2) OB_Q(3) OB_Q(4) OB_Q(5)
+    OB_Q(6) OB_Q(7) OB_Q(8) OB_Q(9) OB_Q(10) OB_Q(11)
+#undef OB_Q
+    default: break;
+  }
+}
+
+template <bool HFAM>
+__global__ void k_faces_oblique(const fdtd_dev d, const fdtd_op op) {
+  ob_planes<HFAM>(d, blockIdx.y, op_step(d, op), blockIdx.x * blockDim.x + threadIdx.x,
+                  gridDim.x * blockDim.x);
 }
 
 // Batched: blockIdx.z = active member; members in other modes skip.
 template <bool HFAM>
 __global__ void k_batch_faces_oblique(const fdtd_dev *devs, const fdtd_op *ops,
-                                      const int32_t *steps, int axis) {
+                                      const int32_t *steps) {
   const int g = blockIdx.z;
   const fdtd_op &op = ops[g];
   if (!op.tfsf_split || op.tfsf_mode != FDTD_MODE_OBLIQUE) return;
-  ob_face_cells<HFAM>(devs[g], axis, blockIdx.y, steps[g] + op.step,
-                      blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+  ob_planes<HFAM>(devs[g], blockIdx.y, steps[g] + op.step, blockIdx.x * blockDim.x + threadIdx.x,
+                  gridDim.x * blockDim.x);
 }
 
 // --------------------------------------------------------------- probes
@@ -825,17 +860,15 @@ int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_
 }
 
 int fdtdk_faces(int hfam, const fdtd_dev *d, const fdtd_op *op, cudaStream_t s) {
-  if (op->tfsf_mode == FDTD_MODE_OBLIQUE) {  // x, y, z faces in turn
+  if (op->tfsf_mode == FDTD_MODE_OBLIQUE) {  // the twelve face planes in one launch
     int32_t a = (d->j1 - d->j0 + 1) * (d->k1 - d->k0 + 1);
     if ((d->i1 - d->i0 + 1) * (d->k1 - d->k0 + 1) > a) a = (d->i1 - d->i0 + 1) * (d->k1 - d->k0 + 1);
     if ((d->i1 - d->i0 + 1) * (d->j1 - d->j0 + 1) > a) a = (d->i1 - d->i0 + 1) * (d->j1 - d->j0 + 1);
     int bx = (a + 255) / 256;
     bx = bx < 1 ? 1 : (bx > 152 * 2 ? 152 * 2 : bx);
-    for (int axis = 0; axis < 3; ++axis) {
-      if (hfam) k_faces_oblique<true><<<dim3(bx, 4), 256, 0, s>>>(*d, *op, axis);
-      else k_faces_oblique<false><<<dim3(bx, 4), 256, 0, s>>>(*d, *op, axis);
-    }
-    g_launches += 3;
+    if (hfam) k_faces_oblique<true><<<dim3(bx, 12), 256, 0, s>>>(*d, *op);
+    else k_faces_oblique<false><<<dim3(bx, 12), 256, 0, s>>>(*d, *op);
+    ++g_launches;
     return (int)cudaGetLastError();
   }
   int32_t a = (d->I + 2) * (d->J + 2);
@@ -868,11 +901,9 @@ int fdtdk_batch_faces_oblique(int hfam, const fdtd_dev *devs, const fdtd_op *ops
   if (n <= 0) return 0;
   int bx = (max_cells_per_face + 255) / 256;
   bx = bx < 1 ? 1 : (bx > 4 ? 4 : bx);
-  for (int axis = 0; axis < 3; ++axis) {
-    if (hfam) k_batch_faces_oblique<true><<<dim3(bx, 4, n), 256, 0, s>>>(devs, ops, steps, axis);
-    else k_batch_faces_oblique<false><<<dim3(bx, 4, n), 256, 0, s>>>(devs, ops, steps, axis);
-  }
-  g_launches += 3;
+  if (hfam) k_batch_faces_oblique<true><<<dim3(bx, 12, n), 256, 0, s>>>(devs, ops, steps);
+  else k_batch_faces_oblique<false><<<dim3(bx, 12, n), 256, 0, s>>>(devs, ops, steps);
+  ++g_launches;
   return (int)cudaGetLastError();
 }
 

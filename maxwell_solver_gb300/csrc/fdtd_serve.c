@@ -67,7 +67,7 @@ typedef struct req {
   size_t n_out_probes, n_out_field;
   /* batched mode: stepping this round, steps completed before its current
    * stretch in the batch, and steps completed now */
-  int in_batch;
+  int in_batch, want;
   int32_t done_base, done;
   struct req *next;
 } req;
@@ -238,19 +238,39 @@ static int by_remaining(const void *a, const void *b) {
   return wx < wy ? -1 : wx > wy;
 }
 
-/* This round's members: resident requests by least remaining work until
- * their cells reach `fill`; members that drop out leave the batch (their
- * state stays resident) and rejoin later at the step they reached.  A
- * single member runs alone (*solo), outside the batch. */
-static int select_round(server *S, int64_t fill, req **solo) {
+/* This round's members, in order of least remaining work.  When the first
+ * request has at least `solo` cells it runs alone (*solo, through
+ * fdtd_step_n, whose kernels are tuned to its shape); otherwise the smaller
+ * requests are taken in order until their cells reach `fill`, and the large
+ * ones wait.  Members that drop out leave the batch (their state stays
+ * resident) and rejoin later at the step they reached.  A round of one
+ * member also runs alone. */
+static int select_round(server *S, int64_t fill, int64_t solo_cells, req **solo) {
   qsort(S->act, (size_t)S->n_act, sizeof(req *), by_remaining);
-  int n_want = 0;
-  for (int64_t cells = 0; n_want < S->n_act && cells < fill; ++n_want)
-    cells += req_cells(S->act[n_want]);
-  *solo = n_want == 1 ? S->act[0] : NULL;
+  for (int a = 0; a < S->n_act; ++a) S->act[a]->want = 0;
+  *solo = NULL;
+  if (req_cells(S->act[0]) >= solo_cells) {
+    *solo = S->act[0];
+  } else {
+    int n_want = 0;
+    req *last = NULL;
+    int64_t cells = 0;
+    for (int a = 0; a < S->n_act && cells < fill; ++a) {
+      req *r = S->act[a];
+      if (req_cells(r) >= solo_cells) continue;
+      r->want = 1;
+      cells += req_cells(r);
+      ++n_want;
+      last = r;
+    }
+    if (n_want == 1) {
+      *solo = last;
+      last->want = 0;
+    }
+  }
   for (int a = 0; a < S->n_act; ++a) {
     req *r = S->act[a];
-    const int want = a < n_want && r != *solo;
+    const int want = r->want;
     int rc = FDTD_OK;
     if (want && !r->in_batch) {
       r->done_base = r->done;
@@ -270,6 +290,9 @@ static void *serve_loop(void *arg) {
   server *S = (server *)arg;
   const int32_t round = S->cfg.round_steps > 0 ? S->cfg.round_steps : 32;
   const int64_t fill = S->cfg.fill_cells > 0 ? S->cfg.fill_cells : ((int64_t)1 << 25);
+  const int64_t solo_cells = S->cfg.solo_cells > 0    ? S->cfg.solo_cells
+                             : S->cfg.solo_cells == 0 ? ((int64_t)1 << 22)
+                                                      : INT64_MAX;
   req *adm[ADMIT_MAX];
   pthread_mutex_lock(&S->mu);
   for (;;) {
@@ -339,7 +362,7 @@ static void *serve_loop(void *arg) {
      * alone through fdtd_step_n */
     req *solo = NULL;
     if (S->n_act > 0) {
-      int rc = select_round(S, fill, &solo);
+      int rc = select_round(S, fill, solo_cells, &solo);
       if (!rc && solo) {
         const int32_t n = solo->r.steps - solo->done < round ? solo->r.steps - solo->done : round;
         rc = fdtd_step_n(solo->h, solo->done, n, solo->r.tfsf_mode, NULL);

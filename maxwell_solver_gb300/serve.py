@@ -24,10 +24,10 @@ from .workloads import GridSpec, grid_probes, grid_shapes, grid_source
 
 class Server:
     def __init__(self, hbm_budget: int = 120 << 30, max_active: int = 0, round_steps: int = 0,
-                 one_at_a_time: bool = False, fill_cells: int = 0):
+                 one_at_a_time: bool = False, fill_cells: int = 0, solo_cells: int = 0):
         self._lib = _native.load()
         cfg = _native.FdtdServerConfig(int(hbm_budget), int(max_active), int(round_steps),
-                                       int(bool(one_at_a_time)), int(fill_cells))
+                                       int(bool(one_at_a_time)), int(fill_cells), int(solo_cells))
         h = ctypes.c_uint64(0)
         _check(self._lib.fdtd_server_create(ctypes.byref(h), ctypes.byref(cfg)))
         self.handle = h.value
@@ -36,7 +36,7 @@ class Server:
     # ------------------------------------------------------------ requests
     def submit_request(self, dims, steps, fctr, delX, delT, pml, tfsf_mode, waveform,
                        shapes=(), bg=(1.0, 0.0), probes=None, out_field=0, rate=1.0,
-                       tfsf_width=None) -> int:
+                       tfsf_width=None, angles=(0.0, 0.0, 0.0)) -> int:
         I, J, K = (int(x) for x in dims)
         prm = self._lib.fdtd_default_params()
         prm.pml = int(pml)
@@ -58,6 +58,7 @@ class Server:
         req.n_probes = int(pr.shape[0])
         req.probes = pr.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
         req.out_field = int(out_field)
+        req.theta, req.phi, req.psi = (float(a) for a in angles)
         t = ctypes.c_uint64(0)
         _check(self._lib.fdtd_server_submit(self.handle, ctypes.byref(req), ctypes.byref(t)))
         self._shape[t.value] = (int(steps), int(pr.shape[0]), I * J * K, int(out_field))
@@ -67,7 +68,8 @@ class Server:
         bg_e, bg_s, rows = grid_shapes(spec)
         return self.submit_request(spec.dims, spec.steps, spec.fctr, spec.delX, spec.delT,
                                    spec.pml, spec.mode, grid_source(spec), rows, (bg_e, bg_s),
-                                   grid_probes(spec, n_probes) if n_probes else None, out_field)
+                                   grid_probes(spec, n_probes) if n_probes else None, out_field,
+                                   angles=spec.angles if spec.mode == 5 else (0.0, 0.0, 0.0))
 
     def wait(self, ticket: int, timeout: float | None = None) -> None:
         _check(self._lib.fdtd_server_wait(self.handle, int(ticket),

@@ -30,12 +30,17 @@ class Workload:
     dims: tuple          # (I, J, K) including the CPML
     steps: int
     pml: int
-    mode: int            # TF/SF mode of the reference (1..4)
+    mode: int            # TF/SF mode: the reference's 1..4, or 5 (oblique)
     media: str           # vacuum | spheres | layers
     n_probes: int
     seed: int
     delX: float = 1e-3
     fctr: float = 30e9
+
+    @property
+    def angles(self) -> tuple:
+        """Mode 5: (theta, phi, psi) in radians, seeded."""
+        return incidence_angles(self.seed)
 
     @property
     def delT(self) -> float:
@@ -46,9 +51,17 @@ class Workload:
         return int(np.prod(self.dims))
 
 
+def incidence_angles(seed: int) -> tuple:
+    """Seeded oblique incidence: theta uniform in [0, pi], phi and the
+    polarisation angle psi uniform in [0, 2 pi)."""
+    r = np.random.default_rng(np.random.PCG64(seed + 104729))
+    return (float(r.uniform(0, math.pi)), float(r.uniform(0, 2 * math.pi)),
+            float(r.uniform(0, 2 * math.pi)))
+
+
 WORKLOADS = {
     "c1": Workload("c1", (64, 64, 64), 500, 10, 3, "vacuum", 8, 0),
-    "c2": Workload("c2", (256, 256, 256), 2000, 12, 3, "spheres", 64, 1),
+    "c2": Workload("c2", (256, 256, 256), 2000, 12, 5, "spheres", 64, 1),
     "c3": Workload("c3", (512, 512, 448), 4000, 16, 1, "layers", 256, 2, delX=5e-3, fctr=1e9),
 }
 
@@ -161,6 +174,8 @@ def setup(api, w: Workload, steps: int | None = None, params=None):
     for flag, arr in materials(w).items():
         api("UpdateMaterial", P, np.int32(flag), arr)
     api("ReadySimulation", P)
+    if w.mode == 5:
+        api("SetIncidence", P, np.float64(w.angles))
     api("Init1D", P, np.float32(1.0), pw)
     return P
 
@@ -181,6 +196,11 @@ class GridSpec:
     media: str = "spheres"  # or "layers"
 
     @property
+    def angles(self) -> tuple:
+        """Mode 5: (theta, phi, psi) in radians, seeded."""
+        return incidence_angles(self.seed)
+
+    @property
     def delT(self) -> float:
         return 0.99 * self.delX / (math.sqrt(3.0) * C0)
 
@@ -190,23 +210,25 @@ class GridSpec:
 
 
 def batch_mix(n: int = 256, seed: int = 3):
-    """c4: axes uniform-integer 32..128, 8-cell CPML, 0..10 spheres, TF/SF with
-    a random axis-aligned incidence (modes 1..4) and f0 uniform 10..60 GHz,
-    steps uniform 300..1500."""
+    """c4: axes uniform-integer 32..128, 8-cell CPML, 0..10 spheres, TF/SF
+    plane wave at a random oblique incidence and polarisation (mode 5,
+    `incidence_angles`), f0 uniform 10..60 GHz, steps uniform 300..1500."""
     r = rng(seed)
     out = []
     for g in range(n):
         dims = tuple(int(x) for x in r.integers(32, 129, 3))
-        out.append(GridSpec(dims, int(r.integers(300, 1501)), 8, int(r.integers(1, 5)),
-                            int(r.integers(0, 11)), float(r.uniform(10e9, 60e9)), seed * 1000 + g))
+        steps = int(r.integers(300, 1501))
+        r.integers(1, 5)  # (the axis-mode draw of earlier mixes: keeps the sequence)
+        out.append(GridSpec(dims, steps, 8, 5, int(r.integers(0, 11)),
+                            float(r.uniform(10e9, 60e9)), seed * 1000 + g))
     return out
 
 
 def serve_mix(n: int = 64, seed: int = 4, max_axis: int = 384, max_steps: int = 4000):
     """c5 requests: cubic-ish grids (a base size log-uniform 48..max_axis,
-    each axis within +-15% of it), CPML 8..16 cells, random spheres or
-    layered media, steps uniform 200..max_steps, TF/SF mode 1..4, f0 uniform
-    10..60 GHz."""
+    each axis within +-15% of it), CPML 8..16 cells, random spheres (oblique
+    incidence, mode 5) or layered media (vertical incidence, mode 1), steps
+    uniform 200..max_steps, f0 uniform 10..60 GHz."""
     r = rng(seed)
     out = []
     for g in range(n):
@@ -216,7 +238,9 @@ def serve_mix(n: int = 64, seed: int = 4, max_axis: int = 384, max_steps: int = 
         pml = int(r.integers(8, 17))
         media = "layers" if r.random() < 0.5 else "spheres"
         steps = int(r.integers(200, max_steps + 1))
-        out.append(GridSpec(dims, steps, pml, int(r.integers(1, 5)), int(r.integers(0, 11)),
+        r.integers(1, 5)  # (the axis-mode draw of earlier mixes: keeps the sequence)
+        mode = 1 if media == "layers" else 5
+        out.append(GridSpec(dims, steps, pml, mode, int(r.integers(0, 11)),
                             float(r.uniform(10e9, 60e9)), seed * 1000 + g, media=media))
     return out
 
@@ -332,5 +356,7 @@ def setup_grid(api, spec: GridSpec):
     for flag in (4, 5, 6):
         api("UpdateMaterial", P, np.int32(flag), eps)
     api("ReadySimulation", P)
+    if spec.mode == 5:
+        api("SetIncidence", P, np.float64(spec.angles))
     api("Init1D", P, np.float32(1.0), grid_source(spec))
     return P

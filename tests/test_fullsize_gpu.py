@@ -33,6 +33,8 @@ def oracle_for(w, T):
     for flag, arr in materials(w).items():
         o.update_material(flag, arr)
     o.ready_simulation()
+    if w.mode == 5:
+        o.set_incidence(*w.angles)
     o.init_1d(1.0, pw)
     return o
 
@@ -78,6 +80,8 @@ def test_c2_linearity():
         for flag, arr in materials(w).items():
             simFDTD("UpdateMaterial", P, np.int32(flag), arr)
         simFDTD("ReadySimulation", P)
+        if w.mode == 5:
+            simFDTD("SetIncidence", P, np.float64(w.angles))
         simFDTD("Init1D", P, np.float32(rate), pw)
         simFDTD("StepN", P, np.int32([0, T, w.mode]))
         out.append([simFDTD("OutputVis", P, np.uint32(w.cells), np.int32(f)) for f in range(1, 7)])

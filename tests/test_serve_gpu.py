@@ -21,8 +21,10 @@ def _small_specs(n, seed=11):
     out = []
     for g in range(n):
         dims = tuple(int(x) for x in r.integers(36, 73, 3))
-        out.append(GridSpec(dims, int(r.integers(60, 161)), int(r.integers(8, 11)),
-                            int(r.integers(1, 5)), int(r.integers(0, 6)),
+        steps, pml, mode = int(r.integers(60, 161)), int(r.integers(8, 11)), int(r.integers(1, 5))
+        if g % 3 == 1:
+            mode = 5  # oblique incidence, seeded angles
+        out.append(GridSpec(dims, steps, pml, mode, int(r.integers(0, 6)),
                             float(r.uniform(10e9, 60e9)), seed * 1000 + g,
                             media="layers" if g % 3 == 2 else "spheres"))
     return out
@@ -47,6 +49,8 @@ def _ready(spec, shapes: bool):
         for f in (4, 5, 6):
             simFDTD("UpdateMaterial", P, np.int32(f), eps)
     simFDTD("ReadySimulation", P)
+    if spec.mode == 5:
+        simFDTD("SetIncidence", P, np.float64(spec.angles))
     simFDTD("Init1D", P, np.float32(1.0), grid_source(spec))
     return P
 
@@ -109,6 +113,22 @@ def test_served_results_equal_alone():
         np.testing.assert_array_equal(a["probes"], b["probes"], err_msg=str(spec))
 
 
+def test_solo_rounds_equal_alone():
+    """With a solo threshold inside the mix the larger requests run alone
+    through fdtd_step_n between batched rounds of the smaller ones; every
+    result still equals the one-at-a-time run."""
+    specs = _small_specs(8, seed=17)
+    cells = sorted(int(np.prod(s.dims)) for s in specs)
+    solo = cells[len(cells) // 2]
+    mixed, st = _serve(specs, [0.0] * len(specs), hbm_budget=16 << 30, round_steps=16,
+                       solo_cells=solo)
+    alone, _ = _serve(specs, [0.0] * len(specs), hbm_budget=16 << 30, one_at_a_time=True)
+    assert st["completed"] == len(specs) and st["failed"] == 0
+    for spec, a, b in zip(specs, mixed, alone):
+        np.testing.assert_array_equal(a["field"], b["field"], err_msg=str(spec))
+        np.testing.assert_array_equal(a["probes"], b["probes"], err_msg=str(spec))
+
+
 def test_served_result_equals_plain_handle():
     """One request through the server equals the same solve set up by hand
     (shapes) and run with StepN."""
@@ -139,6 +159,8 @@ def _ready_with_probes(spec, probes):
     simFDTD("SetShapes", P, np.float32([bg_e, bg_s]), np.array(rows, dtype=np.float64))
     simFDTD("SetAntennaLocations", P, np.asfortranarray(probes).ravel(order="F"))
     simFDTD("ReadySimulation", P)
+    if spec.mode == 5:
+        simFDTD("SetIncidence", P, np.float64(spec.angles))
     simFDTD("Init1D", P, np.float32(1.0), grid_source(spec))
     return P
 

@@ -52,7 +52,7 @@ def test_serve_mix_ranges_and_determinism():
     for s in a:
         assert all(48 <= d <= 384 for d in s.dims)
         assert max(s.dims) / min(s.dims) <= 1.15 / 0.85 + 1e-9
-        assert 8 <= s.pml <= 16 and 200 <= s.steps <= 4000 and 1 <= s.mode <= 4
+        assert 8 <= s.pml <= 16 and 200 <= s.steps <= 4000 and s.mode == (1 if s.media == "layers" else 5)
         assert s.media in ("spheres", "layers")
     assert {s.media for s in a} == {"spheres", "layers"}
     # log-uniform base size: both ends of the range are visited
