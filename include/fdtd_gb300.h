@@ -124,6 +124,20 @@ int fdtd_set_shapes(fdtd_handle h, float bg_eps_r, float bg_sigma, const fdtd_sh
 int fdtd_create_mu(fdtd_handle h, const float *mu_x, const float *mu_y,
                    const float *mu_z, size_t n);
 
+/* 'SetMagnetic' -- per-cell magnetic media, what createMu
+ * (src/simulation.h:28-68) sets out to do: relative permeability mu_r and
+ * magnetic conductivity sigma_m (ohm/m) of each H component at its Yee
+ * position, Imax*Jmax*Kmax values each (x fastest); sm_* may
+ * all be NULL (lossless).  After ReadySimulation; applies from the next H
+ * update to the curl, the CPML corrections and the TF/SF corrections:
+ * q = sigma_m delT / (2 mu0 mu_r), Chh = (1 - q) / (1 + q),
+ * Che = delT / (mu0 mu_r) / (1 + q) / delX, in double, rounded once
+ * (mu_r = 1, sigma_m = 0 give the scalar coefficients exactly).  Handles
+ * with per-cell H coefficients cannot join a batch. */
+int fdtd_set_magnetic(fdtd_handle h, const float *mu_x, const float *mu_y,
+                      const float *mu_z, const float *sm_x, const float *sm_y,
+                      const float *sm_z, size_t n);
+
 /* 'SetAntennaLocations' -- src/simFDTD.cu:126-132, setAntennaLocations
  * src/simulation.h:1047-1067.  loc is numAnt x 3 int32, column-major
  * (x column, then y, then z), offsets inside the CPML (pml is added).
@@ -212,6 +226,8 @@ typedef struct {
   float Chh, Che;
   int32_t zchunk_h, zchunk_e; /* z-planes per work item of the TMA half-steps
                                  (autotuned; 0 = built-in heuristic) */
+  int32_t hcoef_mode;      /* H coefficients: 0 uniform, per cell
+                              (fdtd_set_magnetic): 1 arrays, 2 indexed */
 } fdtd_info;
 int fdtd_get_info(fdtd_handle h, fdtd_info *out);
 

@@ -85,7 +85,7 @@ class FdtdInfo(ctypes.Structure):
                 ("j1", I32), ("k0", I32), ("k1", I32), ("coef_mode", I32),
                 ("num_materials", I32), ("device_bytes", ctypes.c_uint64),
                 ("Chh", ctypes.c_float), ("Che", ctypes.c_float),
-                ("zchunk_h", I32), ("zchunk_e", I32)]
+                ("zchunk_h", I32), ("zchunk_e", I32), ("hcoef_mode", I32)]
 
 
 # name -> (restype, argtypes)
@@ -103,6 +103,7 @@ SIGNATURES = {
     "fdtd_set_shapes": (ctypes.c_int, [U64, ctypes.c_float, ctypes.c_float,
                                        ctypes.POINTER(FdtdShape), I32]),
     "fdtd_create_mu": (ctypes.c_int, [U64, P, P, P, SZ]),
+    "fdtd_set_magnetic": (ctypes.c_int, [U64, P, P, P, P, P, P, SZ]),
     "fdtd_set_antenna_locations": (ctypes.c_int, [U64, P, SZ]),
     "fdtd_ready_simulation": (ctypes.c_int, [U64]),
     "fdtd_init_1d": (ctypes.c_int, [U64, ctypes.c_float, P, SZ]),

@@ -99,45 +99,47 @@ __device__ __forceinline__ const float *inc_e_row(const fdtd_dev &d, int mode, i
 
 // H-side TF/SF corrections of one cell (all launchers pass c = +1):
 // mode 3 gpu.h:152-182, mode 4 :217-247, mode 1 :424-477, mode 2 :512-541.
+// chx, chy, chz: the Che of each component (the reference's scalar Che, or
+// per cell).
 __device__ __forceinline__ void tfsf_h(const fdtd_dev &d, int mode, const float *inc, int i,
-                                       int j, int k, float &hx, float &hy, float &hz) {
-  const float Ch = d.Che;
+                                       int j, int k, float &hx, float &hy, float &hz,
+                                       float chx, float chy, float chz) {
   const int i0 = d.i0, i1 = d.i1, j0 = d.j0, j1 = d.j1, k0 = d.k0, k1 = d.k1;
   if (mode == 3) {
     if (in_range(i, i0, i1) && in_range(k, k0, k1 - 1)) {
-      if (j == j0 - 1) hx = hx + Ch * inc[i];
-      if (j == j1) hx = hx - Ch * inc[i];
+      if (j == j0 - 1) hx = hx + chx * inc[i];
+      if (j == j1) hx = hx - chx * inc[i];
     }
     if (in_range(j, j0, j1) && in_range(k, k0, k1 - 1)) {
-      if (i == i0 - 1) hy = hy - Ch * inc[i0];
-      if (i == i1) hy = hy + Ch * inc[i1];
+      if (i == i0 - 1) hy = hy - chy * inc[i0];
+      if (i == i1) hy = hy + chy * inc[i1];
     }
   } else if (mode == 4) {
     if (in_range(i, i0, i1) && in_range(j, j0, j1 - 1)) {
-      if (k == k0 - 1) hx = hx - Ch * inc[i];
-      if (k == k1) hx = hx + Ch * inc[i];
+      if (k == k0 - 1) hx = hx - chx * inc[i];
+      if (k == k1) hx = hx + chx * inc[i];
     }
     if (in_range(j, j0, j1 - 1) && in_range(k, k0, k1)) {
-      if (i == i0 - 1) hz = hz + Ch * inc[i0];
-      if (i == i1) hz = hz - Ch * inc[i1];
+      if (i == i0 - 1) hz = hz + chz * inc[i0];
+      if (i == i1) hz = hz - chz * inc[i1];
     }
   } else if (mode == 1) {
     if (in_range(i, i0, i1) && in_range(j, j0, j1 - 1)) {
-      if (k == k0 - 1) hx = hx - Ch * inc[k0];
-      if (k == k1) hx = hx + Ch * inc[k1];
+      if (k == k0 - 1) hx = hx - chx * inc[k0];
+      if (k == k1) hx = hx + chx * inc[k1];
     }
     if (in_range(j, j0, j1 - 1) && in_range(k, k0, k1)) {
-      if (i == i0 - 1) hz = hz + Ch * inc[k];
-      if (i == i1) hz = hz - Ch * inc[k];
+      if (i == i0 - 1) hz = hz + chz * inc[k];
+      if (i == i1) hz = hz - chz * inc[k];
     }
   } else if (mode == 2) {
     if (in_range(i, i0, i1 - 1) && in_range(j, j0, j1)) {
-      if (k == k0 - 1) hy = hy + Ch * inc[k0];
-      if (k == k1) hy = hy - Ch * inc[k1];
+      if (k == k0 - 1) hy = hy + chy * inc[k0];
+      if (k == k1) hy = hy - chy * inc[k1];
     }
     if (in_range(i, i0, i1 - 1) && in_range(k, k0, k1)) {
-      if (j == j0 - 1) hz = hz - Ch * inc[k];
-      if (j == j1) hz = hz + Ch * inc[k];
+      if (j == j0 - 1) hz = hz - chz * inc[k];
+      if (j == j1) hz = hz + chz * inc[k];
     }
   }
 }
@@ -232,37 +234,66 @@ __device__ __forceinline__ Coef6 load_coef(const fdtd_dev &d, int64_t n) {
   return d.coef_mode == 0 ? coef_from_arrays(d, n) : coef_from_table(d, __ldg(d.mat + n));
 }
 
+// H update coefficients of one cell: Chh and Che per component.  Uniform
+// (the reference's scalars) unless fdtd_set_magnetic gave per-cell ones.
+struct HCoef {
+  float hhx, hhy, hhz, hex, hey, hez;
+};
+__device__ __forceinline__ HCoef hcoef_uniform(const fdtd_dev &d) {
+  return HCoef{d.Chh, d.Chh, d.Chh, d.Che, d.Che, d.Che};
+}
+__device__ __forceinline__ HCoef hcoef_at(const fdtd_dev &d, int64_t n) {
+  if (d.hcoef_mode == 0) return hcoef_uniform(d);
+  if (d.hcoef_mode == 2) {
+    const float *t = d.hmat_tab + 6 * (int)__ldg(d.hmat + n);
+    return HCoef{__ldg(t), __ldg(t + 1), __ldg(t + 2), __ldg(t + 3), __ldg(t + 4), __ldg(t + 5)};
+  }
+  const int64_t c = d.cells;
+  return HCoef{__ldg(d.hc + n), __ldg(d.hc + c + n), __ldg(d.hc + 2 * c + n),
+               __ldg(d.hc + 3 * c + n), __ldg(d.hc + 4 * c + n), __ldg(d.hc + 5 * c + n)};
+}
+// Che of component comp (0..2) at cell n.
+__device__ __forceinline__ float hche_at(const fdtd_dev &d, int64_t n, int comp) {
+  if (d.hcoef_mode == 0) return d.Che;
+  if (d.hcoef_mode == 2) return __ldg(d.hmat_tab + 6 * (int)__ldg(d.hmat + n) + 3 + comp);
+  return __ldg(d.hc + (3 + comp) * d.cells + n);
+}
+
 // One CPML axis of a cell's H update: the psi pair's recurrence from its
 // old value ps (stored back to *dst) and the field corrections
-// (gpu.h:644-685 Y, :604-642 X, :687-725 Z).
+// (gpu.h:644-685 Y, :604-642 X, :687-725 Z), with the Che of each
+// corrected component (the reference's scalar Che, or per cell).
 __device__ __forceinline__ void h_corr_y(const fdtd_dev &d, int py, float2 ps, float2 *dst,
-                                         float dEz_y, float dEx_y, float &hx, float &hz) {
-  const float Che = d.Che, dx = d.dx;  // {psi_Hxy, psi_Hzy}
+                                         float dEz_y, float dEx_y, float &hx, float &hz,
+                                         float che_x, float che_z) {
+  const float dx = d.dx;  // {psi_Hxy, psi_Hzy}
   const float b = d.bH[py], c = d.cH[py];
   const float v0 = b * ps.x + div_dx(d, c * dEz_y);
-  hx = hx - Che * v0 * dx;
+  hx = hx - che_x * v0 * dx;
   const float v1 = b * ps.y + div_dx(d, c * dEx_y);
-  hz = hz + Che * v1 * dx;
+  hz = hz + che_z * v1 * dx;
   *dst = make_float2(v0, v1);
 }
 __device__ __forceinline__ void h_corr_x(const fdtd_dev &d, int px, float2 ps, float2 *dst,
-                                         float dEz_x, float dEy_x, float &hy, float &hz) {
-  const float Che = d.Che, dx = d.dx;  // {psi_Hyx, psi_Hzx}
+                                         float dEz_x, float dEy_x, float &hy, float &hz,
+                                         float che_y, float che_z) {
+  const float dx = d.dx;  // {psi_Hyx, psi_Hzx}
   const float b = d.bH[px], c = d.cH[px];
   const float v0 = b * ps.x + div_dx(d, c * dEz_x);
-  hy = hy + Che * v0 * dx;
+  hy = hy + che_y * v0 * dx;
   const float v1 = b * ps.y + div_dx(d, c * dEy_x);
-  hz = hz - Che * v1 * dx;
+  hz = hz - che_z * v1 * dx;
   *dst = make_float2(v0, v1);
 }
 __device__ __forceinline__ void h_corr_z(const fdtd_dev &d, int pz, float2 ps, float2 *dst,
-                                         float dEy_z, float dEx_z, float &hx, float &hy) {
-  const float Che = d.Che, dx = d.dx;  // {psi_Hxz, psi_Hyz}
+                                         float dEy_z, float dEx_z, float &hx, float &hy,
+                                         float che_x, float che_y) {
+  const float dx = d.dx;  // {psi_Hxz, psi_Hyz}
   const float b = d.bH[pz], c = d.cH[pz];
   const float v0 = b * ps.x + div_dx(d, c * dEy_z);
-  hx = hx + Che * v0 * dx;
+  hx = hx + che_x * v0 * dx;
   const float v1 = b * ps.y + div_dx(d, c * dEx_z);
-  hy = hy - Che * v1 * dx;
+  hy = hy - che_y * v1 * dx;
   *dst = make_float2(v0, v1);
 }
 
@@ -279,21 +310,20 @@ __device__ __forceinline__ float2 *psi_at_z(const fdtd_dev &d, int a, int i, int
 
 // New H of one cell from its old H and the six forward E differences:
 // curl (gpu.h:575-602), TF/SF, CPML Y (gpu.h:644-685), X (:604-642),
-// Z (:687-725).  px/py/pz: H-slab positions (-1 outside).
+// Z (:687-725).  px/py/pz: H-slab positions (-1 outside).  C: the cell's
+// coefficients (hcoef_uniform: the reference's scalars).
 template <bool CURL, bool PML>
-__device__ __forceinline__ void update_h_cell(const fdtd_dev &d, int mode, const float *inc,
-                                              int i, int j, int k, int px, int py, int pz,
-                                              float &hx, float &hy, float &hz, float dEz_y,
-                                              float dEx_y, float dEz_x, float dEy_x,
-                                              float dEy_z, float dEx_z) {
-  const float Che = d.Che, dx = d.dx;
+__device__ __forceinline__ void update_h_cell(const fdtd_dev &d, const HCoef &C, int mode,
+                                              const float *inc, int i, int j, int k, int px,
+                                              int py, int pz, float &hx, float &hy, float &hz,
+                                              float dEz_y, float dEx_y, float dEz_x,
+                                              float dEy_x, float dEy_z, float dEx_z) {
   if (CURL) {
-    const float Chh = d.Chh;
-    hx = Chh * hx + Che * (-dEz_y + dEy_z);
-    hy = Chh * hy + Che * (-dEx_z + dEz_x);
-    hz = Chh * hz + Che * (-dEy_x + dEx_y);
+    hx = C.hhx * hx + C.hex * (-dEz_y + dEy_z);
+    hy = C.hhy * hy + C.hey * (-dEx_z + dEz_x);
+    hz = C.hhz * hz + C.hez * (-dEy_x + dEx_y);
   }
-  if (mode) tfsf_h(d, mode, inc, i, j, k, hx, hy, hz);
+  if (mode) tfsf_h(d, mode, inc, i, j, k, hx, hy, hz, C.hex, C.hey, C.hez);
   if (PML) {
     // Each psi pair belongs to one cell, so all of the cell's pairs are
     // loaded before its first psi store: one memory round trip.
@@ -305,9 +335,9 @@ __device__ __forceinline__ void update_h_cell(const fdtd_dev &d, int mode, const
     if (py >= 0) y = *Y;
     if (px >= 0) x = *X;
     if (pz >= 0) z = *Z;
-    if (py >= 0) h_corr_y(d, py, y, Y, dEz_y, dEx_y, hx, hz);
-    if (px >= 0) h_corr_x(d, px, x, X, dEz_x, dEy_x, hy, hz);
-    if (pz >= 0) h_corr_z(d, pz, z, Z, dEy_z, dEx_z, hx, hy);
+    if (py >= 0) h_corr_y(d, py, y, Y, dEz_y, dEx_y, hx, hz, C.hex, C.hez);
+    if (px >= 0) h_corr_x(d, px, x, X, dEz_x, dEy_x, hy, hz, C.hey, C.hez);
+    if (pz >= 0) h_corr_z(d, pz, z, Z, dEy_z, dEx_z, hx, hy, C.hex, C.hey);
   }
 }
 

@@ -110,6 +110,10 @@ typedef struct sim {
   cudaEvent_t ev[MAX_EVENTS];
   float *d_f[6], *d_ce[6], *d_psi_pool, *d_psi[FDTD_NUM_PSI];
   float *d_den_ex, *d_den_hx, *d_inc[4], *d_src, *d_probes, *d_mu[3];
+  /* per-cell H coefficients (fdtd_set_magnetic): mode 1 arrays, 2 indexed */
+  int32_t hcoef_mode;
+  float *d_hc, *d_htab;
+  uint16_t *d_hmat;
   /* oblique plane wave (TF/SF mode 5) */
   int has_ob;
   double ob_theta, ob_phi, ob_psi;
@@ -377,6 +381,9 @@ int fdtd_destroy(fdtd_handle h) {
   dfree(s->d_ob[0]);
   dfree(s->d_ob[1]);
   for (int a = 0; a < 3; ++a) dfree(s->d_mu[a]);
+  dfree(s->d_hc);
+  dfree(s->d_hmat);
+  dfree(s->d_htab);
   dfree(s->d_psi_pool);
   dfree(s->d_den_ex);
   dfree(s->d_den_hx);
@@ -701,6 +708,10 @@ static void fill_dev_struct(sim *s) {
   d->mat = s->d_mat;
   d->mat_tab = s->d_tab;
   d->n_mat = s->num_mat;
+  d->hcoef_mode = s->hcoef_mode;
+  d->hc = s->d_hc;
+  d->hmat = s->d_hmat;
+  d->hmat_tab = s->d_htab;
   d->err = s->d_err;
   d->zc_h = s->zc_h;
   d->zc_e = s->zc_e;
@@ -1213,15 +1224,99 @@ int fdtd_create_mu(fdtd_handle h, const float *mu_x, const float *mu_y, const fl
   if ((rc = dalloc(s, (void **)&tmp, bytes))) return rc;
   for (int a = 0; a < 3; ++a) {
     if (!s->d_mu[a] && (rc = dalloc(s, (void **)&s->d_mu[a], bytes))) {
-      cudaFree(tmp);
+      dfree(tmp);
       return rc;
     }
     CU(cudaMemcpyAsync(tmp, mu[a], bytes, cudaMemcpyHostToDevice, s->stream));
     KL(fdtdk_compute_mu(s->d_mu[a], tmp, s->d_den_hx, s->IJK, s->I, s->delT, 0.0f, s->stream));
   }
   CU(cudaStreamSynchronize(s->stream));
-  cudaFree(tmp);
+  dfree(tmp);
   s->device_bytes -= bytes;
+  return FDTD_OK;
+}
+
+/* Per-cell magnetic media: createMu's coefficient (src/simulation.h:28-68)
+ * applied everywhere the H update uses Che (curl, CPML corrections, TF/SF
+ * corrections), with a per-cell magnetic conductivity as well.  In double,
+ * rounded once: q = sigma_m delT / 2 / mu0 / mu_r, Chh = (1 - q) / (1 + q),
+ * Che = delT / mu0 / mu_r / (1 + q) / delX -- with mu_r = 1, sigma_m = 0
+ * exactly the scalar pair of src/simulation.h:914-922. */
+int fdtd_set_magnetic(fdtd_handle h, const float *mu_x, const float *mu_y, const float *mu_z,
+                      const float *sm_x, const float *sm_y, const float *sm_z, size_t n) {
+  GET(h);
+  if (!s->init_ready) return fail(FDTD_ERR_STATE, "SetMagnetic requires ReadySimulation");
+  if (!mu_x || !mu_y || !mu_z || n < (size_t)s->IJK)
+    return fail(FDTD_ERR_INVALID_ARG, "mu_x, mu_y, mu_z need Imax*Jmax*Kmax values");
+  if ((sm_x || sm_y || sm_z) && !(sm_x && sm_y && sm_z))
+    return fail(FDTD_ERR_INVALID_ARG, "sigma_m: all three components or none");
+  const float *mu[3] = {mu_x, mu_y, mu_z}, *sm[3] = {sm_x, sm_y, sm_z};
+  const size_t IJK = (size_t)s->IJK;
+  for (int a = 0; a < 3; ++a)
+    for (size_t i = 0; i < IJK; ++i) {
+      if (!(isfinite(mu[a][i]) && mu[a][i] > 0.0f))
+        return fail(FDTD_ERR_INVALID_ARG, "mu_r must be finite and positive (cell %zu)", i);
+      if (sm[a] && !(isfinite(sm[a][i]) && sm[a][i] >= 0.0f))
+        return fail(FDTD_ERR_INVALID_ARG, "sigma_m must be finite and >= 0 (cell %zu)", i);
+    }
+  int rc = flush(s);
+  if (rc) return rc;
+  float *hh = (float *)malloc(2 * IJK * sizeof(float));
+  if (!hh) return fail(FDTD_ERR_OOM, "out of host memory");
+  float *he = hh + IJK;
+  const size_t bytes = 6 * (size_t)s->cells * sizeof(float);
+  if (!s->d_hc) {
+    if ((rc = dalloc(s, (void **)&s->d_hc, bytes))) {
+      free(hh);
+      return rc;
+    }
+    CU(cudaMemsetAsync(s->d_hc, 0, bytes, s->stream));
+  }
+  const double dt = (double)s->delT, dx = (double)s->delX;
+  for (int a = 0; a < 3; ++a) {
+    for (size_t i = 0; i < IJK; ++i) {
+      const double m = (double)mu[a][i];
+      const double q = (sm[a] ? (double)sm[a][i] : 0.0) * dt / 2 / K_MU0 / m;
+      hh[i] = (float)((1 - q) / (1 + q));
+      he[i] = (float)(dt / K_MU0 / m / (1 + q) / dx);
+    }
+    const size_t row = (size_t)s->I * sizeof(float), pitch = (size_t)s->Ip * sizeof(float);
+    cudaError_t e = cudaMemcpy2DAsync(s->d_hc + (size_t)a * s->cells, pitch, hh, row, row,
+                                      (size_t)s->J * s->K, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(s->d_hc + (size_t)(3 + a) * s->cells, pitch, he, row, row,
+                            (size_t)s->J * s->K, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream); /* hh, he are reused */
+    if (e != cudaSuccess) {
+      free(hh);
+      return fail(FDTD_ERR_CUDA, "SetMagnetic upload: %s", cudaGetErrorString(e));
+    }
+  }
+  free(hh);
+  /* 2-byte ids and a table, as for the E coefficients, when the tuples are
+   * few; the per-cell arrays otherwise */
+  s->hcoef_mode = 1;
+  if (s->allow_compress && s->d_hkeys) {
+    if (!s->d_hmat && (rc = dalloc(s, (void **)&s->d_hmat, (size_t)s->cells * sizeof(uint16_t))))
+      return rc;
+    if (!s->d_htab && (rc = dalloc(s, (void **)&s->d_htab, (size_t)MAX_MATERIALS * 6 * sizeof(float))))
+      return rc;
+    CU(cudaMemsetAsync(s->d_hmat, 0, (size_t)s->cells * sizeof(uint16_t), s->stream));
+    const float *cc[6];
+    for (int a = 0; a < 6; ++a) cc[a] = s->d_hc + (size_t)a * s->cells;
+    KL(fdtdk_compress_ce(&s->dev, cc, s->d_hmat, s->d_htab, MAX_MATERIALS, s->d_hkeys, s->d_hrep,
+                         s->d_hid, HASH_CAP, s->d_hcnt, s->stream));
+    int32_t cnt[4];
+    CU(cudaMemcpyAsync(cnt, s->d_hcnt, sizeof(cnt), cudaMemcpyDeviceToHost, s->stream));
+    CU(cudaStreamSynchronize(s->stream));
+    if (!cnt[1] && !cnt[2] && cnt[0] > 0 && cnt[0] <= MAX_MATERIALS) {
+      s->hcoef_mode = 2;
+      dfree(s->d_hc);
+      s->d_hc = NULL;
+      s->device_bytes -= bytes;
+    }
+  }
+  fill_dev_struct(s);
   return FDTD_OK;
 }
 
@@ -1876,6 +1971,7 @@ int fdtd_get_info(fdtd_handle h, fdtd_info *o) {
   o->Che = s->Che;
   o->zchunk_h = s->zc_h;
   o->zchunk_e = s->zc_e;
+  o->hcoef_mode = s->hcoef_mode;
   return FDTD_OK;
 }
 
@@ -2092,6 +2188,8 @@ int fdtd_batch_add(fdtd_batch bh, fdtd_handle h, int32_t first, int32_t count, i
   if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "invalid simulation handle");
   if (!s->init_ready) return fail(FDTD_ERR_STATE, "batch members need ReadySimulation");
   if (!s->maps.valid) return fail(FDTD_ERR_UNSUPPORTED, "batch members need the TMA kernels");
+  if (s->hcoef_mode)
+    return fail(FDTD_ERR_UNSUPPORTED, "batch members need uniform H coefficients (no SetMagnetic)");
   if (first < 0 || count < 0) return fail(FDTD_ERR_INVALID_ARG, "negative step range");
   if (mode < 1 || mode > FDTD_MODE_OBLIQUE) mode = 0;
   const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;

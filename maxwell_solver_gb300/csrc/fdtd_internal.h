@@ -81,7 +81,14 @@ typedef struct {
   int32_t ob_r0[3], ob_w;
   const float *ob_inc[2];
   float ob_rho;
-  int32_t pad_;             /* size: a multiple of 16 bytes (bulk copies) */
+  /* H coefficients: 0 uniform (Chh, Che); per cell (fdtd_set_magnetic):
+   * 1 arrays hc[6 * cells] (Chh x, y, z, then Che x, y, z), 2 indexed
+   * (hmat ids, hmat_tab [n][6] in the same order) */
+  int32_t hcoef_mode;
+  const float *hc;
+  const uint16_t *hmat;
+  const float *hmat_tab;
+  int32_t pad_[2];          /* size: a multiple of 16 bytes (bulk copies) */
 } fdtd_dev;
 
 /* TMA descriptors (CUtensorMap, 128 B each) of one grid: 0..5 = Ex Ey Ez Hx

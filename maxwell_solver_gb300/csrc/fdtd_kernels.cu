@@ -72,7 +72,8 @@ __global__ void __launch_bounds__(TX *TY) k_half_h(const fdtd_dev d, const fdtd_
     const float ez = Ez[n];
     const float ex_k1 = Ex[n + sIJ], ey_k1 = Ey[n + sIJ];
     float hx = Hx[n], hy = Hy[n], hz = Hz[n];
-    update_h_cell<CURL, PML>(d, mode, inc, i, j, k, px, py, pz, hx, hy, hz, Ez[n + sI] - ez,
+    update_h_cell<CURL, PML>(d, hcoef_at(d, n), mode, inc, i, j, k, px, py, pz, hx, hy, hz,
+                             Ez[n + sI] - ez,
                              Ex[n + sI] - ex, Ez[n + 1] - ez, Ey[n + 1] - ey, ey_k1 - ey,
                              ex_k1 - ex);
     Hx[n] = hx;
@@ -221,7 +222,8 @@ __device__ __forceinline__ void face_cell(const fdtd_dev &d, int mode, const flo
   const float v0 = *f;
   float vx = comp == 0 ? v0 : 0.f, vy = comp == 1 ? v0 : 0.f, vz = comp == 2 ? v0 : 0.f;
   if (HFAM) {
-    tfsf_h(d, mode, inc, i, j, k, vx, vy, vz);
+    const HCoef C = hcoef_at(d, n);
+    tfsf_h(d, mode, inc, i, j, k, vx, vy, vz, C.hex, C.hey, C.hez);
   } else {
     const Coef6 C = load_coef(d, n);
     tfsf_e(d, mode, inc, i, j, k, C.exh, C.eyh, C.ezh, vx, vy, vz);
@@ -385,7 +387,7 @@ __device__ __forceinline__ void ob_plane(const fdtd_dev &d, int step, int first,
       x[AXIS] = SIDE ? hi[AXIS] : lo[AXIS] - 1;
       const int64_t n = x[0] + (int64_t)x[1] * d.Ip + (int64_t)x[2] * d.plane;
       float *f = d.f[3 + CH] + n;
-      const float t = d.Che * inc;
+      const float t = hche_at(d, n, CH) * inc;
       *f = (P == 0) == (SIDE == 0) ? *f + t : *f - t;
     } else {
       x[AXIS] = SIDE ? hi[AXIS] : lo[AXIS];
@@ -837,7 +839,9 @@ static int half_oblique(int hfam, const fdtd_dev *d, const fdtd_maps *m, int use
 int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s) {
   if (op->tfsf_mode == FDTD_MODE_OBLIQUE) return half_oblique(1, d, m, use_tma, op, s);
-  if (use_tma && m && m->valid && op->curl) return fdtdk_half_h_tma(d, m, op, s);
+  // per-cell H coefficients (fdtd_set_magnetic) run on the direct kernel
+  if (use_tma && m && m->valid && op->curl && d->hcoef_mode == 0)
+    return fdtdk_half_h_tma(d, m, op, s);
   const int ni = d->I - 1, nj = d->J - 1, nk = d->K - 1;
   if (op->curl && op->pml) return launch_half(k_half_h<true, true>, d, op, s, ni, nj, nk);
   if (op->curl) return launch_half(k_half_h<true, false>, d, op, s, ni, nj, nk);

@@ -578,8 +578,8 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
         const int j = y0 + ty;
         if (oth || (int)ax + (int)ay + (int)az > 1) {
           if (act) {
-            update_h_cell<true, PML>(dp, mode, inc, i, j, k, px, py[c], pz, hx, hy, hz, dEz_y,
-                                     dEx_y, dEz_x, dEy_x, dEy_z, dEx_z);
+            update_h_cell<true, PML>(dp, hcoef_uniform(dp), mode, inc, i, j, k, px, py[c], pz,
+                                     hx, hy, hz, dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z);
           }
         } else {
           hx = Chh * hx + Che * (-dEz_y + dEy_z);
@@ -589,14 +589,14 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
             if (ax) {
               if (px >= 0) {
                 float2 *X = psi_at_x(dp, PSI_HX, px, j, k);
-                h_corr_x(dp, px, *X, X, dEz_x, dEy_x, hy, hz);
+                h_corr_x(dp, px, *X, X, dEz_x, dEy_x, hy, hz, Che, Che);
               }
             } else if (ay) {
               float2 *Y = psi_at_y(dp, PSI_HY, i, py[c], k);
-              h_corr_y(dp, py[c], *Y, Y, dEz_y, dEx_y, hx, hz);
+              h_corr_y(dp, py[c], *Y, Y, dEz_y, dEx_y, hx, hz, Che, Che);
             } else if (az) {
               float2 *Z = psi_at_z(dp, PSI_HZ, i, j, pz);
-              h_corr_z(dp, pz, *Z, Z, dEy_z, dEx_z, hx, hy);
+              h_corr_z(dp, pz, *Z, Z, dEy_z, dEx_z, hx, hy, Che, Che);
             }
           }
         }

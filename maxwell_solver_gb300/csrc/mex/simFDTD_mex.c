@@ -240,6 +240,18 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     free(my);
     free(mz);
     CHECK(rc);
+  } else if (strcmp(o, "setmagnetic") == 0) {
+    /* simFDTD('SetMagnetic', P, mu_x, mu_y, mu_z [, sm_x, sm_y, sm_z]) */
+    if (nrhs != 5 && nrhs != 8)
+      mexErrMsgIdAndTxt("simFDTD:InvalidInput", "mu_x, mu_y, mu_z [, sm_x, sm_y, sm_z] required.");
+    size_t nv[6] = {0, 0, 0, 0, 0, 0};
+    float *v[6] = {NULL, NULL, NULL, NULL, NULL, NULL};
+    for (int a = 0; a < nrhs - 2; ++a) v[a] = as_f32(prhs[2 + a], &nv[a]);
+    size_t n = nv[0];
+    for (int a = 1; a < nrhs - 2; ++a) n = nv[a] < n ? nv[a] : n;
+    int rc = fdtd_set_magnetic(P, v[0], v[1], v[2], v[3], v[4], v[5], n);
+    for (int a = 0; a < 6; ++a) free(v[a]);
+    CHECK(rc);
   } else if (strcmp(o, "init1d") == 0) {
     if (nrhs < 4) mexErrMsgIdAndTxt("simFDTD:InvalidInput", "rate and PW_source required.");
     size_t nr = 0, n = 0;

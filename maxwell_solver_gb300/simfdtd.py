@@ -129,6 +129,13 @@ def simFDTD(op: str, *args):  # noqa: N802 - mirrors the MATLAB entry point
         need(3, "mu_x, mu_y, mu_z required.")
         mx, my, mz = _f32(a[0]), _f32(a[1]), _f32(a[2])
         _check(lib.fdtd_create_mu(P, _ptr(mx), _ptr(my), _ptr(mz), min(mx.size, my.size, mz.size)))
+    elif o == "setmagnetic":
+        if len(a) not in (3, 6):
+            raise SimFDTDError("simFDTD:InvalidInput", "mu_x, mu_y, mu_z [, sm_x, sm_y, sm_z] required.")
+        v = [_f32(x) for x in a]
+        n = min(x.size for x in v)
+        ptrs = [_ptr(x) for x in v] + [None] * (6 - len(v))
+        _check(lib.fdtd_set_magnetic(P, *ptrs, n))
     elif o == "init1d":
         need(2, "rate and PW_source required.")
         rate, pw = _f32(a[0]), _f32(a[1])

@@ -85,6 +85,7 @@ def _load():
                 f("ready_simulation").argtypes = [P]
                 f("init_1d").argtypes = [P, ctypes.c_float, P]
                 f("set_incidence").argtypes = [P] + [ctypes.c_double] * 3
+                f("set_magnetic").argtypes = [P] * 7
                 f("update_cuda").argtypes = [P]
                 f("reset_field_all").argtypes = [P]
                 for n in ("update_h_all", "update_e_all", "update_h_pml", "update_e_pml"):
@@ -168,6 +169,14 @@ class OracleSim:
     def set_incidence(self, theta, phi, psi):
         """TF/SF mode 5 (oblique plane wave); before init_1d."""
         assert self._f("set_incidence")(self._h, float(theta), float(phi), float(psi)) == 0
+
+    def set_magnetic(self, mu, sm=None):
+        """Per-cell mu_r (and magnetic conductivity) of Hx, Hy, Hz: three
+        arrays of I*J*K each; after ready_simulation."""
+        m = [np.ascontiguousarray(x, dtype=np.float32).ravel(order="F") for x in mu]
+        g = [np.ascontiguousarray(x, dtype=np.float32).ravel(order="F") for x in sm] if sm else None
+        ptrs = [_ptr(x) for x in m] + ([_ptr(x) for x in g] if g else [None] * 3)
+        assert self._f("set_magnetic")(self._h, *ptrs) == 0
 
     def init_1d(self, rate, pw):
         a = np.ascontiguousarray(pw, dtype=np.float32)

@@ -90,7 +90,14 @@ typedef struct or_sim {
   long ob_r0[3];
   size_t ob_w;
   real *obE, *obH; /* [T][ob_w] */
+  /* extension: per-cell H coefficients (set_magnetic) -- Chh x, y, z, then
+   * Che x, y, z; NULL: the scalar Chh, Che */
+  real *hc[6];
 } or_sim;
+
+/* H coefficients of component a (0..2) at cell n */
+#define CHH(a, n) (s->hc[a] ? s->hc[a][n] : s->Chh)
+#define CHE(a, n) (s->hc[3 + (a)] ? s->hc[3 + (a)][n] : s->Che)
 
 static void *xcalloc(size_t n, size_t sz) {
   void *p = calloc(n ? n : 1, sz);
@@ -125,6 +132,7 @@ void OR(destroy)(or_sim *s) {
   free(s->Ez1d); free(s->Hy1d); free(s->Einv1d); free(s->Hinv1d);
   free(s->ant_idx); free(s->probes);
   free(s->obE); free(s->obH);
+  for (int a = 0; a < 6; ++a) free(s->hc[a]);
   free(s);
 }
 
@@ -134,6 +142,29 @@ int OR(set_incidence)(or_sim *s, double theta, double phi, double psi) {
   s->ob_theta = theta;
   s->ob_phi = phi;
   s->ob_psi = psi;
+  return 0;
+}
+
+/* Extension: per-cell magnetic media (what createMu, src/simulation.h:28-68,
+ * sets out to do): mu_r and magnetic conductivity sigma_m (sm may be NULL)
+ * per H component; in double, rounded once:
+ * q = sm delT / 2 / mu0 / mu_r, Chh = (1 - q) / (1 + q),
+ * Che = delT / mu0 / mu_r / (1 + q) / delX.  After ready_simulation. */
+int OR(set_magnetic)(or_sim *s, const float *mu_x, const float *mu_y, const float *mu_z,
+                     const float *sm_x, const float *sm_y, const float *sm_z) {
+  if (!s->init_ready) return -1;
+  const float *mu[3] = {mu_x, mu_y, mu_z}, *sm[3] = {sm_x, sm_y, sm_z};
+  const double dt = (double)s->delT, dx = (double)s->delX;
+  for (int a = 0; a < 3; ++a) {
+    if (!s->hc[a]) s->hc[a] = (real *)xcalloc(s->IJK, sizeof(real));
+    if (!s->hc[3 + a]) s->hc[3 + a] = (real *)xcalloc(s->IJK, sizeof(real));
+    for (size_t i = 0; i < s->IJK; ++i) {
+      const double m = (double)mu[a][i];
+      const double q = (sm[a] ? (double)sm[a][i] : 0.0) * dt / 2 / K_MU0 / m;
+      s->hc[a][i] = (real)((1 - q) / (1 + q));
+      s->hc[3 + a][i] = (real)(dt / K_MU0 / m / (1 + q) / dx);
+    }
+  }
   return 0;
 }
 
@@ -547,7 +578,6 @@ int OR(init_1d)(or_sim *s, float rate, const float *pw_source) {
 void OR(update_h_all)(or_sim *s) {
   real *Hx = s->f[F_HX], *Hy = s->f[F_HY], *Hz = s->f[F_HZ];
   const real *Ex = s->f[F_EX], *Ey = s->f[F_EY], *Ez = s->f[F_EZ];
-  const real Chh = s->Chh, Che = s->Che;
   const size_t I = s->I, IJ = s->IJ;
 #pragma omp parallel for schedule(static)
   for (long long kk = 0; kk < (long long)s->K - 1; ++kk)
@@ -555,9 +585,9 @@ void OR(update_h_all)(or_sim *s) {
       for (size_t i = 0; i + 1 < s->I; ++i) {
         size_t n = i + j * I + (size_t)kk * IJ;
         real ez = Ez[n], ey = Ey[n], ex = Ex[n];
-        Hx[n] = Chh * Hx[n] + Che * (-(Ez[n + I] - ez) + (Ey[n + IJ] - ey));
-        Hy[n] = Chh * Hy[n] + Che * (-(Ex[n + IJ] - ex) + (Ez[n + 1] - ez));
-        Hz[n] = Chh * Hz[n] + Che * (-(Ey[n + 1] - ey) + (Ex[n + I] - ex));
+        Hx[n] = CHH(0, n) * Hx[n] + CHE(0, n) * (-(Ez[n + I] - ez) + (Ey[n + IJ] - ey));
+        Hy[n] = CHH(1, n) * Hy[n] + CHE(1, n) * (-(Ex[n + IJ] - ex) + (Ez[n + 1] - ez));
+        Hz[n] = CHH(2, n) * Hz[n] + CHE(2, n) * (-(Ey[n + 1] - ey) + (Ex[n + I] - ex));
       }
 }
 
@@ -588,7 +618,7 @@ void OR(update_h_pml)(or_sim *s) {
   real *Hx = s->f[F_HX], *Hy = s->f[F_HY], *Hz = s->f[F_HZ];
   const real *Ex = s->f[F_EX], *Ey = s->f[F_EY], *Ez = s->f[F_EZ];
   const size_t I = s->I, J = s->J, K = s->K, IJ = s->IJ, p = s->p;
-  const real Che = s->Che, d = s->delX;
+  const real d = s->delX;
   const real *b = s->bH, *c = s->cH;
   /* Y faces: psi layout [k][2p][i] */
   {
@@ -601,9 +631,9 @@ void OR(update_h_pml)(or_sim *s) {
           size_t j = y < p ? y : y + J - 2 * p;
           size_t id = x + j * I + (size_t)kk * IJ;
           pxy[t] = b[y] * pxy[t] + c[y] * (Ez[id + I] - Ez[id]) / d;
-          Hx[id] = Hx[id] - Che * pxy[t] * d;
+          Hx[id] = Hx[id] - CHE(0, id) * pxy[t] * d;
           pzy[t] = b[y] * pzy[t] + c[y] * (Ex[id + I] - Ex[id]) / d;
-          Hz[id] = Hz[id] + Che * pzy[t] * d;
+          Hz[id] = Hz[id] + CHE(2, id) * pzy[t] * d;
         }
   }
   /* X faces: psi layout [k][j][2p] */
@@ -617,9 +647,9 @@ void OR(update_h_pml)(or_sim *s) {
           size_t i = x < p ? x : I - 2 * p + x;
           size_t id = i + j * I + (size_t)kk * IJ;
           pyx[t] = b[x] * pyx[t] + c[x] * (Ez[id + 1] - Ez[id]) / d;
-          Hy[id] = Hy[id] + Che * pyx[t] * d;
+          Hy[id] = Hy[id] + CHE(1, id) * pyx[t] * d;
           pzx[t] = b[x] * pzx[t] + c[x] * (Ey[id + 1] - Ey[id]) / d;
-          Hz[id] = Hz[id] - Che * pzx[t] * d;
+          Hz[id] = Hz[id] - CHE(2, id) * pzx[t] * d;
         }
   }
   /* Z faces: psi layout [2p][j][i] */
@@ -634,9 +664,9 @@ void OR(update_h_pml)(or_sim *s) {
           size_t k = z < p ? z : z + K - 2 * p;
           size_t id = x + j * I + k * IJ;
           pxz[t] = b[z] * pxz[t] + c[z] * (Ey[id + IJ] - Ey[id]) / d;
-          Hx[id] = Hx[id] + Che * pxz[t] * d;
+          Hx[id] = Hx[id] + CHE(0, id) * pxz[t] * d;
           pyz[t] = b[z] * pyz[t] + c[z] * (Ex[id + IJ] - Ex[id]) / d;
-          Hy[id] = Hy[id] - Che * pyz[t] * d;
+          Hy[id] = Hy[id] - CHE(1, id) * pyz[t] * d;
         }
   }
 }
@@ -750,8 +780,9 @@ static void oblique_faces(or_sim *s, int hfam, int n) {
             if (hfam) {
               yee_pos(0, ce, xe, p);
               const real inc = s->ob_e[ce] * ob_interp(rowE, ob_coord(s, p[0], p[1], p[2]), W);
-              real *f = &s->f[F_HX + ch][IDX(xh[0], xh[1], xh[2])];
-              const real val = s->Che * inc;
+              const size_t id = IDX(xh[0], xh[1], xh[2]);
+              real *f = &s->f[F_HX + ch][id];
+              const real val = CHE(ch, id) * inc;
               *f = plus ? *f + val : *f - val;
             } else {
               yee_pos(1, ch, xh, p);
@@ -779,56 +810,56 @@ int OR(update_h_planewave)(or_sim *s, int n, int mode) {
   }
   const size_t I = s->I, IJ = s->IJ, S = s->size1d;
   const size_t i0 = s->i0, i1 = s->i1, j0 = s->j0, j1 = s->j1, k0 = s->k0, k1 = s->k1;
-  const real Ch = s->Che; /* Chxe = Chye = Chze = Che, :920-922 */
+  /* Chxe = Chye = Chze = Che, :920-922 (per cell after set_magnetic) */
   real *Hx = s->f[F_HX], *Hy = s->f[F_HY], *Hz = s->f[F_HZ];
   const real c = 1;
   if (mode == 1) { /* ZY */
     const real *E = s->Ez1d + (size_t)n * S + S - s->K;
     for (size_t y = j0; y <= j1 - 1; ++y)
       for (size_t x = i0; x <= i1; ++x) {
-        Hx[IDX(x, y, k0 - 1)] = Hx[IDX(x, y, k0 - 1)] - Ch * E[k0] * c;
-        Hx[IDX(x, y, k1)] = Hx[IDX(x, y, k1)] + Ch * E[k1] * c;
+        Hx[IDX(x, y, k0 - 1)] = Hx[IDX(x, y, k0 - 1)] - CHE(0, IDX(x, y, k0 - 1)) * E[k0] * c;
+        Hx[IDX(x, y, k1)] = Hx[IDX(x, y, k1)] + CHE(0, IDX(x, y, k1)) * E[k1] * c;
       }
     for (size_t z = k0; z <= k1; ++z)
       for (size_t y = j0; y <= j1 - 1; ++y) {
-        Hz[IDX(i0 - 1, y, z)] = Hz[IDX(i0 - 1, y, z)] + Ch * E[z] * c;
-        Hz[IDX(i1, y, z)] = Hz[IDX(i1, y, z)] - Ch * E[z] * c;
+        Hz[IDX(i0 - 1, y, z)] = Hz[IDX(i0 - 1, y, z)] + CHE(2, IDX(i0 - 1, y, z)) * E[z] * c;
+        Hz[IDX(i1, y, z)] = Hz[IDX(i1, y, z)] - CHE(2, IDX(i1, y, z)) * E[z] * c;
       }
   } else if (mode == 2) { /* ZX */
     const real *E = s->Ez1d + (size_t)n * S + S - s->K;
     for (size_t y = j0; y <= j1; ++y)
       for (size_t x = i0; x <= i1 - 1; ++x) {
-        Hy[IDX(x, y, k0 - 1)] = Hy[IDX(x, y, k0 - 1)] + Ch * E[k0] * c;
-        Hy[IDX(x, y, k1)] = Hy[IDX(x, y, k1)] - Ch * E[k1] * c;
+        Hy[IDX(x, y, k0 - 1)] = Hy[IDX(x, y, k0 - 1)] + CHE(1, IDX(x, y, k0 - 1)) * E[k0] * c;
+        Hy[IDX(x, y, k1)] = Hy[IDX(x, y, k1)] - CHE(1, IDX(x, y, k1)) * E[k1] * c;
       }
     for (size_t z = k0; z <= k1; ++z)
       for (size_t x = i0; x <= i1 - 1; ++x) {
-        Hz[IDX(x, j0 - 1, z)] = Hz[IDX(x, j0 - 1, z)] - Ch * E[z] * c;
-        Hz[IDX(x, j1, z)] = Hz[IDX(x, j1, z)] + Ch * E[z] * c;
+        Hz[IDX(x, j0 - 1, z)] = Hz[IDX(x, j0 - 1, z)] - CHE(2, IDX(x, j0 - 1, z)) * E[z] * c;
+        Hz[IDX(x, j1, z)] = Hz[IDX(x, j1, z)] + CHE(2, IDX(x, j1, z)) * E[z] * c;
       }
   } else if (mode == 3) { /* XZ */
     const real *E = s->Ez1d + (size_t)n * S + S - s->I;
     for (size_t z = k0; z <= k1 - 1; ++z)
       for (size_t x = i0; x <= i1; ++x) {
-        Hx[IDX(x, j0 - 1, z)] = Hx[IDX(x, j0 - 1, z)] + Ch * E[x] * c;
-        Hx[IDX(x, j1, z)] = Hx[IDX(x, j1, z)] - Ch * E[x] * c;
+        Hx[IDX(x, j0 - 1, z)] = Hx[IDX(x, j0 - 1, z)] + CHE(0, IDX(x, j0 - 1, z)) * E[x] * c;
+        Hx[IDX(x, j1, z)] = Hx[IDX(x, j1, z)] - CHE(0, IDX(x, j1, z)) * E[x] * c;
       }
     for (size_t z = k0; z <= k1 - 1; ++z)
       for (size_t y = j0; y <= j1; ++y) {
-        Hy[IDX(i0 - 1, y, z)] = Hy[IDX(i0 - 1, y, z)] - Ch * E[i0] * c;
-        Hy[IDX(i1, y, z)] = Hy[IDX(i1, y, z)] + Ch * E[i1] * c;
+        Hy[IDX(i0 - 1, y, z)] = Hy[IDX(i0 - 1, y, z)] - CHE(1, IDX(i0 - 1, y, z)) * E[i0] * c;
+        Hy[IDX(i1, y, z)] = Hy[IDX(i1, y, z)] + CHE(1, IDX(i1, y, z)) * E[i1] * c;
       }
   } else if (mode == 4) { /* XY, inverse run */
     const real *E = s->Einv1d + (size_t)n * S + S - s->I;
     for (size_t y = j0; y <= j1 - 1; ++y)
       for (size_t x = i0; x <= i1; ++x) {
-        Hx[IDX(x, y, k0 - 1)] = Hx[IDX(x, y, k0 - 1)] - Ch * E[x] * c;
-        Hx[IDX(x, y, k1)] = Hx[IDX(x, y, k1)] + Ch * E[x] * c;
+        Hx[IDX(x, y, k0 - 1)] = Hx[IDX(x, y, k0 - 1)] - CHE(0, IDX(x, y, k0 - 1)) * E[x] * c;
+        Hx[IDX(x, y, k1)] = Hx[IDX(x, y, k1)] + CHE(0, IDX(x, y, k1)) * E[x] * c;
       }
     for (size_t z = k0; z <= k1; ++z)
       for (size_t y = j0; y <= j1 - 1; ++y) {
-        Hz[IDX(i0 - 1, y, z)] = Hz[IDX(i0 - 1, y, z)] + Ch * E[i0] * c;
-        Hz[IDX(i1, y, z)] = Hz[IDX(i1, y, z)] - Ch * E[i1] * c;
+        Hz[IDX(i0 - 1, y, z)] = Hz[IDX(i0 - 1, y, z)] + CHE(2, IDX(i0 - 1, y, z)) * E[i0] * c;
+        Hz[IDX(i1, y, z)] = Hz[IDX(i1, y, z)] - CHE(2, IDX(i1, y, z)) * E[i1] * c;
       }
   }
   (void)I; (void)IJ;
