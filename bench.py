@@ -472,8 +472,8 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4):
     specs = serve_mix(n_req, seed)
     budget = int(budget_gb * (1 << 30))
 
-    def one_run(arrivals, one_at_a_time):
-        with Server(hbm_budget=budget, one_at_a_time=one_at_a_time) as srv:
+    def one_run(arrivals, one_at_a_time, policy="srpt"):
+        with Server(hbm_budget=budget, one_at_a_time=one_at_a_time, policy=policy) as srv:
             t0 = time.perf_counter()
             tickets = []
             for spec, at in zip(specs, arrivals):
@@ -502,10 +502,12 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4):
         rate = load * capacity
         arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
         served, p_s = one_run(arrivals, False)
+        hrrn, p_h = one_run(arrivals, False, "hrrn")
         plain, p_p = one_run(arrivals, True)
         same &= all(np.array_equal(a, b) for a, b in zip(p_s, p_p))
+        same &= all(np.array_equal(a, b) for a, b in zip(p_h, p_p))
         points.append({"load": load, "rate_per_s": round(rate, 3), "served": served,
-                       "one_at_a_time": plain,
+                       "served_hrrn": hrrn, "one_at_a_time": plain,
                        "speedup_solves_per_s": round(served["solves_per_s"] /
                                                      max(plain["solves_per_s"], 1e-9), 2),
                        "p99_ratio_one_at_a_time_over_served": round(
@@ -520,6 +522,8 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4):
         "timing": "wall clock from each request's submission to its result on the host "
                   "(set-up on the device, all steps, probe readout); capacity = every request "
                   "queued at t=0 through the batched server",
+        "policies": "served: least remaining work first; served_hrrn: highest response "
+                    "ratio (waited + remaining) / remaining first",
     }
 
 

@@ -342,7 +342,14 @@ typedef struct {
                              device alone: it runs by itself (fdtd_step_n)
                              when its turn comes, and the batched rounds take
                              only the smaller ones (0: 2^22; -1: never) */
+  int32_t policy;         /* order of the resident requests:
+                             FDTD_SERVE_SRPT (0): least remaining work first;
+                             FDTD_SERVE_HRRN (1): highest response ratio
+                             (waited + remaining) / remaining first, which
+                             bounds how long a large request waits */
 } fdtd_server_config;
+#define FDTD_SERVE_SRPT 0
+#define FDTD_SERVE_HRRN 1
 
 typedef struct {
   double submit_s, admit_s, finish_s; /* server clock, seconds */

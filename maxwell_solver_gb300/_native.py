@@ -60,7 +60,7 @@ class FdtdRequest(ctypes.Structure):
 class FdtdServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_active", I32), ("round_steps", I32),
                 ("one_at_a_time", I32), ("fill_cells", ctypes.c_int64),
-                ("solo_cells", ctypes.c_int64)]
+                ("solo_cells", ctypes.c_int64), ("policy", I32)]
 
 
 class FdtdRequestInfo(ctypes.Structure):

@@ -1236,6 +1236,14 @@ int fdtd_create_mu(fdtd_handle h, const float *mu_x, const float *mu_y, const fl
   return FDTD_OK;
 }
 
+int fdtd_internal_record(fdtd_handle h, cudaEvent_t ev) {
+  GET(h);
+  int rc = flush(s);
+  if (rc) return rc;
+  CU(cudaEventRecord(ev, s->stream));
+  return FDTD_OK;
+}
+
 /* Per-cell magnetic media: createMu's coefficient (src/simulation.h:28-68)
  * applied everywhere the H update uses Che (curl, CPML corrections, TF/SF
  * corrections), with a per-cell magnetic conductivity as well.  In double,
@@ -2055,7 +2063,17 @@ int fdtd_create_signal(double fctr, double delT, double percentage_bw, double nu
  */
 
 #define MAX_BATCHES 256
-#define BATCH_ZRUN 8
+
+/* z-planes per batched work item: 8, or FDTD_BATCH_ZRUN (1..64) */
+static int batch_zrun(void) {
+  static int z = 0;
+  if (!z) {
+    const char *e = getenv("FDTD_BATCH_ZRUN");
+    const int v = e ? atoi(e) : 0;
+    z = v >= 1 && v <= 64 ? v : 8;
+  }
+  return z;
+}
 
 typedef struct {
   fdtd_handle h;
@@ -2254,8 +2272,9 @@ static int ensure_cap(void **d, void **hbuf, int *cap, int need, size_t elem, cu
 }
 
 static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk) {
-  for (int kb = 0; kb < nk; kb += BATCH_ZRUN) {
-    const int np = nk - kb < BATCH_ZRUN ? nk - kb : BATCH_ZRUN;
+  const int zr = batch_zrun();
+  for (int kb = 0; kb < nk; kb += zr) {
+    const int np = nk - kb < zr ? nk - kb : zr;
     for (int y0 = 0; y0 < nj; y0 += FDTD_TILE_Y)
       for (int x0 = 0; x0 < ni; x0 += FDTD_TILE_X) {
         int32_t *e = tab + 4 * (size_t)n;
@@ -2271,7 +2290,7 @@ static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk) {
 
 static int count_items(int ni, int nj, int nk) {
   return ((ni + FDTD_TILE_X - 1) / FDTD_TILE_X) * ((nj + FDTD_TILE_Y - 1) / FDTD_TILE_Y) *
-         ((nk + BATCH_ZRUN - 1) / BATCH_ZRUN);
+         ((nk + batch_zrun() - 1) / batch_zrun());
 }
 
 /* Builds and uploads the device mirrors of the active members. */
@@ -2452,6 +2471,13 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
   left = 0;
   for (int i = 0; i < b->n; ++i) left += b->m[i].done < b->m[i].count;
   if (active_left) *active_left = left;
+  return FDTD_OK;
+}
+
+int fdtd_internal_batch_record(fdtd_batch bh, cudaEvent_t ev) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  CU(cudaEventRecord(ev, b->stream));
   return FDTD_OK;
 }
 

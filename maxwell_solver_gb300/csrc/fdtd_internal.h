@@ -210,6 +210,10 @@ unsigned long long fdtdk_launch_count(void);
 /* Records an error message for the calling thread (fdtd_last_error) and
  * returns code. */
 int fdtd_internal_fail(int code, const char *msg);
+/* Records ev on the stream a simulation's (or a batch's) work runs on, after
+ * the work queued so far (the serving loop paces itself with these). */
+int fdtd_internal_record(fdtd_handle h, cudaEvent_t ev);
+int fdtd_internal_batch_record(fdtd_batch b, cudaEvent_t ev);
 
 /* TF/SF corrections of a split half-step over the face cells (single grid,
  * and every active member of a batch whose op has tfsf_split set;

@@ -68,6 +68,7 @@ typedef struct req {
   /* batched mode: stepping this round, steps completed before its current
    * stretch in the batch, and steps completed now */
   int in_batch, want;
+  double key; /* this round's order (ascending) */
   int32_t done_base, done;
   struct req *next;
 } req;
@@ -90,6 +91,11 @@ typedef struct server {
   req **act;
   int n_act, cap_act;
   fdtd_batch batch;
+  /* pacing: an event after each round; the loop queues a round only once
+   * the round before the last has finished, so that the order it picks
+   * applies on the GPU within two rounds (nothing runs far ahead) */
+  cudaEvent_t ev[2];
+  int ev_used[2], ev_i;
   /* statistics, under mu */
   uint64_t submitted, completed, failed, cell_steps, peak_reserved;
   int peak_active;
@@ -231,14 +237,32 @@ static void fail_active(server *S, int rc) {
 
 static int64_t req_cells(const req *r) { return (int64_t)r->r.I * r->r.J * r->r.K; }
 
-static int by_remaining(const void *a, const void *b) {
+static int by_key(const void *a, const void *b) {
   const req *x = *(req *const *)a, *y = *(req *const *)b;
-  const double wx = (double)req_cells(x) * (x->r.steps - x->done);
-  const double wy = (double)req_cells(y) * (y->r.steps - y->done);
-  return wx < wy ? -1 : wx > wy;
+  return x->key < y->key ? -1 : x->key > y->key;
 }
 
-/* This round's members, in order of least remaining work.  When the first
+/* Approximate cell-steps per second of one GB300 on these kernels: the
+ * scale between waiting time and remaining work in the response ratio. */
+#define SERVE_RATE_EST 3.0e10
+
+static void order_requests(server *S, int policy) {
+  const double now = now_s(S);
+  for (int a = 0; a < S->n_act; ++a) {
+    req *r = S->act[a];
+    const double work = (double)req_cells(r) * (r->r.steps - r->done);
+    if (policy == FDTD_SERVE_HRRN) {
+      const double rem = work / SERVE_RATE_EST + 1e-6;
+      r->key = -((now - r->t_submit) + rem) / rem;
+    } else {
+      r->key = work;
+    }
+  }
+  qsort(S->act, (size_t)S->n_act, sizeof(req *), by_key);
+}
+
+/* This round's members, in the policy's order (least remaining work, or
+ * highest response ratio).  When the first
  * request has at least `solo` cells it runs alone (*solo, through
  * fdtd_step_n, whose kernels are tuned to its shape); otherwise the smaller
  * requests are taken in order until their cells reach `fill`, and the large
@@ -246,7 +270,7 @@ static int by_remaining(const void *a, const void *b) {
  * resident) and rejoin later at the step they reached.  A round of one
  * member also runs alone. */
 static int select_round(server *S, int64_t fill, int64_t solo_cells, req **solo) {
-  qsort(S->act, (size_t)S->n_act, sizeof(req *), by_remaining);
+  order_requests(S, S->cfg.policy);
   for (int a = 0; a < S->n_act; ++a) S->act[a]->want = 0;
   *solo = NULL;
   if (req_cells(S->act[0]) >= solo_cells) {
@@ -379,6 +403,16 @@ static void *serve_loop(void *arg) {
         int32_t left = 0;
         rc = fdtd_batch_step(S->batch, round, &left);
       }
+      if (!rc && S->ev[0]) { /* pace: wait for the previous round */
+        const int e = solo ? fdtd_internal_record(solo->h, S->ev[S->ev_i])
+                           : fdtd_internal_batch_record(S->batch, S->ev[S->ev_i]);
+        S->ev_used[S->ev_i] = e == FDTD_OK;
+        S->ev_i ^= 1;
+        if (S->ev_used[S->ev_i]) {
+          cudaEventSynchronize(S->ev[S->ev_i]);
+          S->ev_used[S->ev_i] = 0;
+        }
+      }
       if (rc) fail_active(S, rc);
     }
 
@@ -413,8 +447,17 @@ static void *serve_loop(void *arg) {
   return NULL;
 }
 
+static void release_gpu(server *S) {
+  if (S->batch) fdtd_batch_destroy(S->batch);
+  S->batch = 0;
+  for (int i = 0; i < 2; ++i)
+    if (S->ev[i]) cudaEventDestroy(S->ev[i]);
+}
+
 int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg) {
   if (!out || !cfg) return FDTD_ERR_INVALID_ARG;
+  if (cfg->policy != FDTD_SERVE_SRPT && cfg->policy != FDTD_SERVE_HRRN)
+    return FDTD_ERR_INVALID_ARG;
   server *S = (server *)calloc(1, sizeof(server));
   if (!S) return FDTD_ERR_OOM;
   S->cfg = *cfg;
@@ -428,10 +471,15 @@ int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg) {
   pthread_cond_init(&S->cv_done, &ca);
   pthread_condattr_destroy(&ca);
   int rc = FDTD_OK;
-  if (!cfg->one_at_a_time) rc = fdtd_batch_create(&S->batch);
+  if (!cfg->one_at_a_time) {
+    rc = fdtd_batch_create(&S->batch);
+    for (int i = 0; i < 2 && !rc; ++i)
+      if (cudaEventCreateWithFlags(&S->ev[i], cudaEventDisableTiming) != cudaSuccess)
+        rc = FDTD_ERR_CUDA;
+  }
   if (!rc && pthread_create(&S->thread, NULL, serve_loop, S) != 0) rc = FDTD_ERR_OOM;
   if (rc) {
-    if (S->batch) fdtd_batch_destroy(S->batch);
+    release_gpu(S);
     free(S);
     return rc;
   }
@@ -455,7 +503,7 @@ int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg) {
     pthread_cond_broadcast(&S->cv_work);
     pthread_mutex_unlock(&S->mu);
     pthread_join(S->thread, NULL);
-    if (S->batch) fdtd_batch_destroy(S->batch);
+    release_gpu(S);
     free(S);
     return FDTD_ERR_OOM;
   }
@@ -658,7 +706,7 @@ int fdtd_server_destroy(fdtd_server h) {
   pthread_cond_broadcast(&S->cv_work);
   pthread_mutex_unlock(&S->mu);
   if (S->thread_started) pthread_join(S->thread, NULL);
-  if (S->batch) fdtd_batch_destroy(S->batch);
+  release_gpu(S);
   for (size_t i = 0; i < S->tab_n; ++i) free_req(S->tab[i]);
   free(S->tab);
   free(S->act);

@@ -24,10 +24,13 @@ from .workloads import GridSpec, grid_probes, grid_shapes, grid_source
 
 class Server:
     def __init__(self, hbm_budget: int = 120 << 30, max_active: int = 0, round_steps: int = 0,
-                 one_at_a_time: bool = False, fill_cells: int = 0, solo_cells: int = 0):
+                 one_at_a_time: bool = False, fill_cells: int = 0, solo_cells: int = 0,
+                 policy: str = "srpt"):
         self._lib = _native.load()
+        pol = {"srpt": 0, "hrrn": 1}[policy]
         cfg = _native.FdtdServerConfig(int(hbm_budget), int(max_active), int(round_steps),
-                                       int(bool(one_at_a_time)), int(fill_cells), int(solo_cells))
+                                       int(bool(one_at_a_time)), int(fill_cells), int(solo_cells),
+                                       pol)
         h = ctypes.c_uint64(0)
         _check(self._lib.fdtd_server_create(ctypes.byref(h), ctypes.byref(cfg)))
         self.handle = h.value

@@ -90,9 +90,11 @@ def _serve(specs, gaps, **cfg):
     return res, st
 
 
-def test_served_results_equal_alone():
+@pytest.mark.parametrize("policy", ["srpt", "hrrn"])
+def test_served_results_equal_alone(policy):
     """Requests arriving while others run are packed into the same batched
-    launches; each ends bit-identical to running alone."""
+    launches (in either order policy); each ends bit-identical to running
+    alone."""
     from maxwell_solver_gb300.serve import estimate_device_bytes
 
     specs = _small_specs(9)
@@ -100,7 +102,7 @@ def test_served_results_equal_alone():
     budget = int(max(est) + 0.6 * (sum(est) - max(est)))  # some requests must queue
     rng = np.random.default_rng(5)
     gaps = rng.exponential(0.01, len(specs))  # Poisson arrivals
-    mixed, st = _serve(specs, gaps, hbm_budget=budget, round_steps=16)
+    mixed, st = _serve(specs, gaps, hbm_budget=budget, round_steps=16, policy=policy)
     alone, st1 = _serve(specs, [0.0] * len(specs), hbm_budget=budget, one_at_a_time=True)
     assert st["completed"] == len(specs) and st["failed"] == 0
     assert st["peak_reserved_bytes"] <= budget
