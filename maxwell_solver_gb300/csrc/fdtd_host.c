@@ -2102,6 +2102,8 @@ typedef struct batch {
   int any_split;   /* some active member's TF/SF runs as the face pass */
   int any_oblique; /* ... in mode 5 */
   int32_t face_max; /* largest face-plane area of those members */
+  int any_xsplit;   /* a member's E CPML X runs as the x-slab pass */
+  int64_t xs_max;   /* the largest member's 2p*J*K */
 } batch;
 
 static batch *g_batches[MAX_BATCHES];
@@ -2344,6 +2346,8 @@ static int batch_rebuild(batch *b) {
   b->any_split = 0;
   b->any_oblique = 0;
   b->face_max = 0;
+  b->any_xsplit = 0;
+  b->xs_max = 0;
   int g = 0;
   nh = ne = 0;
   b->any_probes = 0;
@@ -2365,6 +2369,12 @@ static int batch_rebuild(batch *b) {
       memcpy(op->cur_box, m->cur.box, sizeof(op->cur_box));
     }
     op->tfsf_split = fdtd_tfsf_split(&s->dev, op);
+    op->xsplit = fdtd_xsplit(&s->dev, op);
+    if (op->xsplit) {
+      const int64_t xc = 2 * (int64_t)s->p * s->J * s->K;
+      if (xc > b->xs_max) b->xs_max = xc;
+      b->any_xsplit = 1;
+    }
     if (op->tfsf_split) {
       const int32_t ax = s->I + 2, ay = s->J + 2, az = s->K + 2;
       int32_t f = ax * ay;
@@ -2443,6 +2453,8 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
                                    b->stream));
     KL(fdtdk_batch_half(0, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_e, b->n_e,
                         b->d_work + 2, b->d_err, b->stream));
+    if (b->any_xsplit)
+      KL(fdtdk_batch_e_xslab(b->d_devs, b->d_ops, b->n_act, b->xs_max, b->stream));
     if (b->any_split)
       KL(fdtdk_batch_faces(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
                            b->stream));

@@ -115,7 +115,8 @@ typedef struct {
   int32_t cur_mode;         /* 0 none, 1..3 Ex/Ey/Ez current source */
   int32_t cur_box[6];
   int32_t tfsf_split;       /* TMA kernels: TF/SF applied by the face pass */
-  int32_t pad_[3];
+  int32_t xsplit;           /* TMA E kernel: CPML X applied by the x-slab pass */
+  int32_t pad_[2];
 } fdtd_op;
 
 /* Can the TF/SF corrections of this half-step run as a separate pass over
@@ -150,6 +151,23 @@ static inline int fdtd_tfsf_split(const fdtd_dev *d, const fdtd_op *op) {
   return fdtd_tfsf_faces_clear(d, op);
 }
 
+/* Can the E half-step's CPML X corrections run as a separate pass over the
+ * x-slab cells after the curl kernel?  Per cell the reference applies curl,
+ * TF/SF, CPML Y, Z, X and then the current source (src/simulation.h:386-418,
+ * the source after them), so X is the last step of an x-slab cell unless the
+ * current source reaches that column: E x slabs are i in [1, p) and
+ * [I-p, I-1]. */
+static inline int fdtd_xsplit(const fdtd_dev *d, const fdtd_op *op) {
+  if (!op->pml || !op->curl || d->p < 1) return 0;
+  if (2 * (int64_t)d->p * d->J * d->K > 0x7fffffff) return 0; /* the pass indexes in 32 bits */
+  if (op->cur_mode >= 1 && op->cur_mode <= 3) {
+    const int32_t a = op->cur_box[0], b = op->cur_box[1];
+    if (a <= d->p - 1 && b >= 1) return 0;
+    if (b >= d->I - d->p && a <= d->I - 1) return 0;
+  }
+  return 1;
+}
+
 /* TF/SF mode 5: an oblique plane wave (fdtd_set_incidence), applied only as
  * face passes after the curl / CPML kernels, which needs the faces clear of
  * the CPML and the current source (fdtd_tfsf_faces_clear). */
@@ -166,6 +184,12 @@ int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_
 int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m);
 int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s);
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s);
+/* The E CPML X corrections over the x-slab cells of a grid whose curl kernel
+ * ran with op->xsplit (and of every batch member whose op has it set;
+ * max_cells: the largest 2p*J*K among them). */
+int fdtdk_e_xslab(const fdtd_dev *d, cudaStream_t s);
+int fdtdk_batch_e_xslab(const fdtd_dev *devs, const fdtd_op *ops, int32_t n, int64_t max_cells,
+                        cudaStream_t s);
 /* Material-indexed E coefficients: dedupes the per-cell tuples of ce[6]
  * into mat[] ids and a [n][6] table.  Returns the number of distinct
  * tuples in *n_out, or 0 when they do not fit max_mat / collide. */

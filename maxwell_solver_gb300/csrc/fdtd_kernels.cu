@@ -268,6 +268,50 @@ __global__ void k_batch_faces(const fdtd_dev *devs, const fdtd_op *ops, const in
                          gridDim.x * blockDim.x);
 }
 
+// ------------------------------------------------------- E x-slab pass
+//
+// With fdtd_xsplit the TMA E kernel leaves out CPML X, the last step of an
+// x-slab cell's E update; this pass applies it (e_corr_x, the expression of
+// gpu.h:765-788) to the x-slab cells, one thread per psi pair in the pairs'
+// own order (px fastest, then j, then k; fdtd_xsplit keeps their count
+// below 2^31): i = px below p and px + I - 2p above; px in [1, 2p), j and k
+// inside [1, n-2] (gpu.h:776-777).
+__device__ __forceinline__ void e_xslab_cell(const fdtd_dev &d, int px, int j, int k) {
+  const int p2 = 2 * d.p;
+  if (px < 1 || px >= p2 || j < 1 || j > d.J - 2 || k < 1 || k > d.K - 2) return;
+  const int i = px < d.p ? px : px + d.I - p2;
+  const int64_t n = i + (int64_t)j * d.Ip + (int64_t)k * d.plane;
+  const Coef6 C = load_coef(d, n);
+  const float hz = d.f[5][n], hz_im = d.f[5][n - 1];
+  const float hy = d.f[4][n], hy_im = d.f[4][n - 1];
+  float ey = d.f[1][n], ez = d.f[2][n];
+  float2 *X = psi_at_x(d, PSI_EX, px, j, k);
+  e_corr_x(d, px, *X, X, C, hz, hz_im, hy, hy_im, ey, ez);
+  d.f[1][n] = ey;
+  d.f[2][n] = ez;
+}
+
+__device__ __forceinline__ void e_xslab_range(const fdtd_dev &d, uint32_t first,
+                                              uint32_t stride) {
+  const uint32_t p2 = 2u * (uint32_t)d.p, J = (uint32_t)d.J;
+  const uint32_t total = p2 * J * (uint32_t)d.K;
+  for (uint32_t t = first; t < total; t += stride) {
+    const uint32_t r = t / p2, k = r / J;
+    e_xslab_cell(d, (int)(t - r * p2), (int)(r - k * J), (int)k);
+  }
+}
+
+__global__ void k_e_xslab(const fdtd_dev d) {
+  e_xslab_range(d, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// Batched: blockIdx.y = active member (members without xsplit skip).
+__global__ void k_batch_e_xslab(const fdtd_dev *devs, const fdtd_op *ops) {
+  if (!ops[blockIdx.y].xsplit) return;
+  e_xslab_range(devs[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x,
+                gridDim.x * blockDim.x);
+}
+
 // ---------------------------------------------- oblique plane wave (mode 5)
 //
 // The incident field of an oblique plane wave comes from a 1D FDTD line
@@ -883,6 +927,26 @@ int fdtdk_faces(int hfam, const fdtd_dev *d, const fdtd_op *op, cudaStream_t s) 
   const dim3 grid(bx > 0 ? bx : 1, 4);
   if (hfam) k_faces<true><<<grid, 256, 0, s>>>(*d, *op);
   else k_faces<false><<<grid, 256, 0, s>>>(*d, *op);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_e_xslab(const fdtd_dev *d, cudaStream_t s) {
+  const int64_t total = 2 * (int64_t)d->p * d->J * d->K;
+  if (total <= 0 || total > INT32_MAX) return total > 0 ? (int)cudaErrorInvalidValue : 0;
+  int64_t bx = (total + 255) / 256;
+  if (bx > 152 * 16) bx = 152 * 16;
+  k_e_xslab<<<(unsigned)bx, 256, 0, s>>>(*d);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_batch_e_xslab(const fdtd_dev *devs, const fdtd_op *ops, int32_t n, int64_t max_cells,
+                        cudaStream_t s) {
+  if (n <= 0 || max_cells <= 0) return 0;
+  int64_t bx = (max_cells + 255) / 256;
+  if (bx > 64) bx = 64;
+  k_batch_e_xslab<<<dim3((unsigned)bx, (unsigned)n), 256, 0, s>>>(devs, ops);
   ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -370,8 +370,9 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
       inc = mode ? inc_e_row(d, mode, step) : nullptr;
       cur_src = cm ? d.src[step] : 0.f;
       const bool cur_x = cm && in_range(i, op.cur_box[0], op.cur_box[1]);
-      const bool x_special =
-          (PML && slab_e(i, I, d.p) >= 0) || (mode && (i == d.i0 || i == d.i1)) || i == 0;
+      // with xsplit the x-slab pass applies CPML X afterwards
+      const bool x_special = (PML && !op.xsplit && slab_e(i, I, d.p) >= 0) ||
+                             (mode && (i == d.i0 || i == d.i1)) || i == 0;
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         const int j = y0 + r0 + 4 * c;
@@ -423,6 +424,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
           const int j = y0 + ty;
           int px = -1, py = -1, pz = -1;
           if (PML) e_slabs(d, i, j, k, px, py, pz);
+          if (op.xsplit) px = -1;
           const bool cur = cur_col[c] && in_range(k, op.cur_box[4], op.cur_box[5]);
           update_e_cell<true, PML>(d, mode, inc, cm, cur_src, cur, i, j, k, px, py, pz, C, ex,
                                    ey, ez, hx, hy, hz, hz_jm, hx_jm, hz_im, hy_im, hx_km[c],
@@ -738,15 +740,17 @@ int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) {
   return e;
 }
 
-// The curl kernel, then (when the TF/SF corrections can be split off) the
-// face pass.
+// The curl kernel, then the x-slab pass (CPML X, when it can be split off)
+// and the face pass (TF/SF, when it can): their cells are disjoint.
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
   fdtd_op o = *op;
   o.tfsf_split = fdtd_tfsf_split(d, op);
-  const int e = o.pml ? launch(k_half_e_tma<true, false>, E_SMEM, &g_blocks_e[1], d, m, &o, s,
-                               d->I, d->J, d->K, d->zc_e)
-                      : launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, &o, s,
-                               d->I, d->J, d->K, d->zc_e);
+  o.xsplit = fdtd_xsplit(d, op);
+  int e = o.pml ? launch(k_half_e_tma<true, false>, E_SMEM, &g_blocks_e[1], d, m, &o, s, d->I,
+                         d->J, d->K, d->zc_e)
+                : launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, &o, s,
+                         d->I, d->J, d->K, d->zc_e);
+  if (!e && o.xsplit) e = fdtdk_e_xslab(d, s);
   if (e || !o.tfsf_split) return e;
   return fdtdk_faces(0, d, &o, s);
 }
