@@ -274,16 +274,22 @@ __device__ __forceinline__ void h_corr_y(const fdtd_dev &d, int py, float2 ps, f
   hz = hz + che_z * v1 * dx;
   *dst = make_float2(v0, v1);
 }
-__device__ __forceinline__ void h_corr_x(const fdtd_dev &d, int px, float2 ps, float2 *dst,
-                                         float dEz_x, float dEy_x, float &hy, float &hz,
-                                         float che_y, float che_z) {
+// (b, c: the grading at the cell's slab position px; indexed per lane, so
+// the callers read them from shared memory where they can)
+__device__ __forceinline__ void h_corr_x_bc(const fdtd_dev &d, float b, float c, float2 ps,
+                                            float2 *dst, float dEz_x, float dEy_x, float &hy,
+                                            float &hz, float che_y, float che_z) {
   const float dx = d.dx;  // {psi_Hyx, psi_Hzx}
-  const float b = d.bH[px], c = d.cH[px];
   const float v0 = b * ps.x + div_dx(d, c * dEz_x);
   hy = hy + che_y * v0 * dx;
   const float v1 = b * ps.y + div_dx(d, c * dEy_x);
   hz = hz - che_z * v1 * dx;
   *dst = make_float2(v0, v1);
+}
+__device__ __forceinline__ void h_corr_x(const fdtd_dev &d, int px, float2 ps, float2 *dst,
+                                         float dEz_x, float dEy_x, float &hy, float &hz,
+                                         float che_y, float che_z) {
+  h_corr_x_bc(d, d.bH[px], d.cH[px], ps, dst, dEz_x, dEy_x, hy, hz, che_y, che_z);
 }
 __device__ __forceinline__ void h_corr_z(const fdtd_dev &d, int pz, float2 ps, float2 *dst,
                                          float dEy_z, float dEx_z, float &hx, float &hy,
@@ -311,13 +317,16 @@ __device__ __forceinline__ float2 *psi_at_z(const fdtd_dev &d, int a, int i, int
 // New H of one cell from its old H and the six forward E differences:
 // curl (gpu.h:575-602), TF/SF, CPML Y (gpu.h:644-685), X (:604-642),
 // Z (:687-725).  px/py/pz: H-slab positions (-1 outside).  C: the cell's
-// coefficients (hcoef_uniform: the reference's scalars).
+// coefficients (hcoef_uniform: the reference's scalars).  xb, xc: the H
+// grading tables (d.bH, d.cH, or a shared-memory copy) for the X axis, whose
+// slab position differs between the lanes of a warp.
 template <bool CURL, bool PML>
 __device__ __forceinline__ void update_h_cell(const fdtd_dev &d, const HCoef &C, int mode,
                                               const float *inc, int i, int j, int k, int px,
                                               int py, int pz, float &hx, float &hy, float &hz,
                                               float dEz_y, float dEx_y, float dEz_x,
-                                              float dEy_x, float dEy_z, float dEx_z) {
+                                              float dEy_x, float dEy_z, float dEx_z,
+                                              const float *xb, const float *xc) {
   if (CURL) {
     hx = C.hhx * hx + C.hex * (-dEz_y + dEy_z);
     hy = C.hhy * hy + C.hey * (-dEx_z + dEz_x);
@@ -336,7 +345,7 @@ __device__ __forceinline__ void update_h_cell(const fdtd_dev &d, const HCoef &C,
     if (px >= 0) x = *X;
     if (pz >= 0) z = *Z;
     if (py >= 0) h_corr_y(d, py, y, Y, dEz_y, dEx_y, hx, hz, C.hex, C.hez);
-    if (px >= 0) h_corr_x(d, px, x, X, dEz_x, dEy_x, hy, hz, C.hey, C.hez);
+    if (px >= 0) h_corr_x_bc(d, xb[px], xc[px], x, X, dEz_x, dEy_x, hy, hz, C.hey, C.hez);
     if (pz >= 0) h_corr_z(d, pz, z, Z, dEy_z, dEx_z, hx, hy, C.hex, C.hey);
   }
 }
@@ -377,16 +386,21 @@ __device__ __forceinline__ void e_corr_z(const fdtd_dev &d, int pz, float2 ps, f
   ey = ey + C.eyh * v1 * dx;
   *dst = make_float2(v0, v1);
 }
-__device__ __forceinline__ void e_corr_x(const fdtd_dev &d, int px, float2 ps, float2 *dst,
-                                         const Coef6 &C, float hz, float hz_im, float hy,
-                                         float hy_im, float &ey, float &ez) {
+// (b, c: the grading at the cell's slab position px)
+__device__ __forceinline__ void e_corr_x_bc(const fdtd_dev &d, float b, float c, float2 ps,
+                                            float2 *dst, const Coef6 &C, float hz, float hz_im,
+                                            float hy, float hy_im, float &ey, float &ez) {
   const float dx = d.dx;  // {psi_Eyx, psi_Ezx}
-  const float b = d.bE[px], c = d.cE[px];
   const float v0 = b * ps.x + div_dx(d, c * (hz - hz_im));
   ey = ey - C.eyh * v0 * dx;
   const float v1 = b * ps.y + div_dx(d, c * (hy - hy_im));
   ez = ez + C.ezh * v1 * dx;
   *dst = make_float2(v0, v1);
+}
+__device__ __forceinline__ void e_corr_x(const fdtd_dev &d, int px, float2 ps, float2 *dst,
+                                         const Coef6 &C, float hz, float hz_im, float hy,
+                                         float hy_im, float &ey, float &ez) {
+  e_corr_x_bc(d, d.bE[px], d.cE[px], ps, dst, C, hz, hz_im, hy, hy_im, ey, ez);
 }
 
 // New E of one cell: curl with the reference's guards (gpu.h:727-763),

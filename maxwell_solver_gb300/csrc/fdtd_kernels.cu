@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(TX *TY) k_half_h(const fdtd_dev d, const fdtd_
     update_h_cell<CURL, PML>(d, hcoef_at(d, n), mode, inc, i, j, k, px, py, pz, hx, hy, hz,
                              Ez[n + sI] - ez,
                              Ex[n + sI] - ex, Ez[n + 1] - ez, Ey[n + 1] - ey, ey_k1 - ey,
-                             ex_k1 - ex);
+                             ex_k1 - ex, d.bH, d.cH);
     Hx[n] = hx;
     Hy[n] = hy;
     Hz[n] = hz;
@@ -276,7 +276,8 @@ __global__ void k_batch_faces(const fdtd_dev *devs, const fdtd_op *ops, const in
 // own order (px fastest, then j, then k; fdtd_xsplit keeps their count
 // below 2^31): i = px below p and px + I - 2p above; px in [1, 2p), j and k
 // inside [1, n-2] (gpu.h:776-777).
-__device__ __forceinline__ void e_xslab_cell(const fdtd_dev &d, int px, int j, int k) {
+__device__ __forceinline__ void e_xslab_cell(const fdtd_dev &d, const float *sb, const float *sc,
+                                             int px, int j, int k) {
   const int p2 = 2 * d.p;
   if (px < 1 || px >= p2 || j < 1 || j > d.J - 2 || k < 1 || k > d.K - 2) return;
   const int i = px < d.p ? px : px + d.I - p2;
@@ -286,18 +287,26 @@ __device__ __forceinline__ void e_xslab_cell(const fdtd_dev &d, int px, int j, i
   const float hy = d.f[4][n], hy_im = d.f[4][n - 1];
   float ey = d.f[1][n], ez = d.f[2][n];
   float2 *X = psi_at_x(d, PSI_EX, px, j, k);
-  e_corr_x(d, px, *X, X, C, hz, hz_im, hy, hy_im, ey, ez);
+  e_corr_x_bc(d, sb[px], sc[px], *X, X, C, hz, hz_im, hy, hy_im, ey, ez);
   d.f[1][n] = ey;
   d.f[2][n] = ez;
 }
 
+// The CPML grading is staged in shared memory: indexed per lane from the
+// by-value descriptor it would be a divergent constant-bank load.
 __device__ __forceinline__ void e_xslab_range(const fdtd_dev &d, uint32_t first,
                                               uint32_t stride) {
+  __shared__ float sb[2 * FDTD_MAX_PML], sc[2 * FDTD_MAX_PML];
+  for (int t = threadIdx.x; t < 2 * d.p && t < 2 * FDTD_MAX_PML; t += blockDim.x) {
+    sb[t] = d.bE[t];
+    sc[t] = d.cE[t];
+  }
+  __syncthreads();
   const uint32_t p2 = 2u * (uint32_t)d.p, J = (uint32_t)d.J;
   const uint32_t total = p2 * J * (uint32_t)d.K;
   for (uint32_t t = first; t < total; t += stride) {
     const uint32_t r = t / p2, k = r / J;
-    e_xslab_cell(d, (int)(t - r * p2), (int)(r - k * J), (int)k);
+    e_xslab_cell(d, sb, sc, (int)(t - r * p2), (int)(r - k * J), (int)k);
   }
 }
 

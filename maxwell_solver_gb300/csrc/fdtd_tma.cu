@@ -462,6 +462,15 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
   int4 *meta = reinterpret_cast<int4 *>(empty + NS);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
+  // the X-axis CPML grading, read per lane below: a shared-memory copy
+  // (indexed loads from the by-value descriptor would be divergent
+  // constant-bank loads); in batch mode the staged descriptor has it
+  __shared__ float s_xbc[2][2 * FDTD_MAX_PML];
+  if (!BATCH && PML)
+    for (int t = tid; t < 2 * FDTD_MAX_PML; t += NT) {
+      s_xbc[0][t] = d0.bH[t];
+      s_xbc[1][t] = d0.cH[t];
+    }
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
@@ -581,7 +590,8 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
         if (oth || (int)ax + (int)ay + (int)az > 1) {
           if (act) {
             update_h_cell<true, PML>(dp, hcoef_uniform(dp), mode, inc, i, j, k, px, py[c], pz,
-                                     hx, hy, hz, dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z);
+                                     hx, hy, hz, dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z,
+                                     BATCH ? dp.bH : s_xbc[0], BATCH ? dp.cH : s_xbc[1]);
           }
         } else {
           hx = Chh * hx + Che * (-dEz_y + dEy_z);
@@ -591,7 +601,9 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
             if (ax) {
               if (px >= 0) {
                 float2 *X = psi_at_x(dp, PSI_HX, px, j, k);
-                h_corr_x(dp, px, *X, X, dEz_x, dEy_x, hy, hz, Che, Che);
+                const float xb = BATCH ? dp.bH[px] : s_xbc[0][px];
+                const float xc = BATCH ? dp.cH[px] : s_xbc[1][px];
+                h_corr_x_bc(dp, xb, xc, *X, X, dEz_x, dEy_x, hy, hz, Che, Che);
               }
             } else if (ay) {
               float2 *Y = psi_at_y(dp, PSI_HY, i, py[c], k);
