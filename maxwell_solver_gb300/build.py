@@ -48,9 +48,22 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _defines() -> str:
+    return " ".join(os.environ.get("FDTD_NVCC_DEFINES", "").split())
+
+
+def _stamp_ok() -> bool:
+    """The library was built with the current FDTD_NVCC_DEFINES."""
+    try:
+        with open(LIB + ".defines") as f:
+            return f.read() == _defines()
+    except OSError:
+        return _defines() == ""
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     cu, c, hdr = _sources()
-    if not force and not _stale(LIB, cu + c + hdr + [__file__]):
+    if not force and _stamp_ok() and not _stale(LIB, cu + c + hdr + [__file__]):
         return LIB
     home = cuda_home()
     nvcc = os.path.join(home, "bin", "nvcc")
@@ -63,8 +76,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(obj)
         jobs.append([nvcc, ARCH, "-lineinfo", "-O3", "--fmad=false", "-std=c++17",
                      "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",
-                     *inc, *os.environ.get("FDTD_NVCC_DEFINES", "").split(),
-                     "-c", src, "-o", obj])
+                     *inc, *_defines().split(), "-c", src, "-o", obj])
     for src in c:
         obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
         objs.append(obj)
@@ -86,6 +98,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + f".tmp{os.getpid()}"
     run([nvcc, ARCH, "-shared", "-o", tmp, *objs, "-lpthread", "-lm"])
     os.replace(tmp, LIB)
+    with open(LIB + ".defines", "w") as f:
+        f.write(_defines())
     return LIB
 
 

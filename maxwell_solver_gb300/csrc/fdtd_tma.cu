@@ -49,7 +49,19 @@ namespace {
 constexpr int BX = 64, BY = 8;
 constexpr int NCW = 8;                       // consumer warps
 constexpr int NT = (NCW + 1) * 32;           // + one producer warp
-constexpr int NSE = 4, NSH = 5;              // ring stages (E, H)
+#ifndef FDTD_NSE
+#define FDTD_NSE 4
+#endif
+#ifndef FDTD_NSH
+#define FDTD_NSH 5
+#endif
+#ifndef FDTD_MIN_BLOCKS_E
+#define FDTD_MIN_BLOCKS_E 3
+#endif
+#ifndef FDTD_MIN_BLOCKS_H
+#define FDTD_MIN_BLOCKS_H 3
+#endif
+constexpr int NSE = FDTD_NSE, NSH = FDTD_NSH;  // ring stages (E, H)
 // Batch kernels: resident blocks per SM the register budget is sized for,
 // and their ring depth (build-time tunables).
 #ifndef FDTD_BATCH_MIN_BLOCKS
@@ -263,7 +275,7 @@ __device__ __forceinline__ void cell_map(int tid, int &xo, int &r0) {
 // ----------------------------------------------------------------- E half
 
 template <bool PML, bool BATCH>
-__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
+__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_E)
     k_half_e_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -451,7 +463,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
 // ----------------------------------------------------------------- H half
 
 template <bool PML, bool BATCH>
-__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : 3)
+__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_H)
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
