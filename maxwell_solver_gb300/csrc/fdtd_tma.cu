@@ -53,13 +53,16 @@ constexpr int NT = (NCW + 1) * 32;           // + one producer warp
 #define FDTD_NSE 4
 #endif
 #ifndef FDTD_NSH
-#define FDTD_NSH 5
+#define FDTD_NSH 4
 #endif
+// blocks per SM the single-grid kernels are compiled for (registers): the
+// H kernel fits 4 (56 registers, 4 stages of 13.3 KB), the E kernel 3
+// (72 registers; at 4 it spills)
 #ifndef FDTD_MIN_BLOCKS_E
 #define FDTD_MIN_BLOCKS_E 3
 #endif
 #ifndef FDTD_MIN_BLOCKS_H
-#define FDTD_MIN_BLOCKS_H 3
+#define FDTD_MIN_BLOCKS_H 4
 #endif
 constexpr int NSE = FDTD_NSE, NSH = FDTD_NSH;  // ring stages (E, H)
 // Batch kernels: resident blocks per SM the register budget is sized for,
