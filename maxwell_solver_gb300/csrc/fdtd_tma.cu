@@ -67,14 +67,22 @@ constexpr int NT = (NCW + 1) * 32;           // + one producer warp
 constexpr int NSE = FDTD_NSE, NSH = FDTD_NSH;  // ring stages (E, H)
 // Batch kernels: resident blocks per SM the register budget is sized for,
 // and their ring depth (build-time tunables).
+#ifndef FDTD_BATCH_MIN_BLOCKS_H
+#define FDTD_BATCH_MIN_BLOCKS_H 3
+#endif
+#ifndef FDTD_BATCH_NS_H
+#define FDTD_BATCH_NS_H 4
+#endif
 #ifndef FDTD_BATCH_MIN_BLOCKS
 #define FDTD_BATCH_MIN_BLOCKS 3
 #endif
 #ifndef FDTD_BATCH_NS
 #define FDTD_BATCH_NS 4
 #endif
-constexpr int kBatchMinBlocks = FDTD_BATCH_MIN_BLOCKS;
+constexpr int kBatchMinBlocks = FDTD_BATCH_MIN_BLOCKS;  // E (and the default for H)
 constexpr int kBatchNS = FDTD_BATCH_NS;
+constexpr int kBatchMinBlocksH = FDTD_BATCH_MIN_BLOCKS_H;
+constexpr int kBatchNSH = FDTD_BATCH_NS_H;
 constexpr int HW = BX + 4;                   // halo box row (floats)
 constexpr int HH = BY + 1;                   // halo box rows
 constexpr int TILE_B = BX * BY * 4;          // 2048 B
@@ -106,7 +114,7 @@ struct EG {
 };
 template <bool BATCH>
 struct HG {
-  static constexpr int NS = BATCH ? kBatchNS : NSH;
+  static constexpr int NS = BATCH ? kBatchNSH : NSH;
   static constexpr int STAGE = BATCH ? H_STAGE + DESC_B + OPSLOT_B : H_STAGE;
   static constexpr int SMEM = NS * STAGE + CTRL_B;
 };
@@ -114,14 +122,14 @@ constexpr int E_SMEM = EG<false>::SMEM;
 constexpr int H_SMEM = HG<false>::SMEM;
 static_assert(EG<true>::STAGE % 128 == 0 && HG<true>::STAGE % 128 == 0, "batch stage alignment");
 static_assert(kBatchMinBlocks * (EG<true>::SMEM + 1024) <= 228 * 1024 &&
-                  kBatchMinBlocks * (HG<true>::SMEM + 1024) <= 228 * 1024,
+                  kBatchMinBlocksH * (HG<true>::SMEM + 1024) <= 228 * 1024,
               "batch blocks per SM");
 constexpr unsigned kSpinLimit = 1u << 22;    // bounded mbarrier waits
 static_assert(E_STAGE % 128 == 0 && H_STAGE % 128 == 0, "stage alignment");
 static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
               "TMA inner box extents must be multiples of 16 bytes");
 static_assert(NSH * (8 + 8 + 32) <= CTRL_B && NSE * (8 + 8 + 32) <= CTRL_B &&
-                  kBatchNS * (8 + 8 + 32) <= CTRL_B,
+                  kBatchNS * (8 + 8 + 32) <= CTRL_B && kBatchNSH * (8 + 8 + 32) <= CTRL_B,
               "control block");
 
 struct Maps {
@@ -466,7 +474,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
 // ----------------------------------------------------------------- H half
 
 template <bool PML, bool BATCH>
-__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_H)
+__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : FDTD_MIN_BLOCKS_H)
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
