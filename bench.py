@@ -149,14 +149,15 @@ def ncu_traffic(workload: str):
 
 # ----------------------------------------------------------------- CPU arm
 
-def cpu_oracle_rate(w, target_s: float, max_steps: int):
+def cpu_oracle_rate(w, target_s: float, max_steps: int, warmup: int = 3):
     """Times the FP32 oracle (OpenMP, all host threads) on the workload's grid
-    for a bounded number of steps; returns (Mcell-steps/s, steps, seconds)."""
+    for a bounded number of steps after `warmup` untimed ones; returns
+    (Mcell-steps/s, steps, seconds)."""
     import oracle
     from maxwell_solver_gb300.workloads import materials, probe_locations, sources
 
     oracle.build()
-    T = max_steps + 2
+    T = max_steps + warmup + 1
     o = oracle.OracleSim("f32")
     o.set_params(pml=w.pml, tfsf_width=w.pml + 5)
     I, J, K = w.dims
@@ -171,15 +172,16 @@ def cpu_oracle_rate(w, target_s: float, max_steps: int):
     if w.mode == 5:
         o.set_incidence(*w.angles)
     o.init_1d(1.0, pw)
-    o.step(0, w.mode)  # warm-up
-    n, t0 = 1, time.perf_counter()
-    while n <= max_steps:
+    for n in range(warmup):
+        o.step(n, w.mode)
+    n, t0 = warmup, time.perf_counter()
+    while n < warmup + max_steps:
         o.step(n, w.mode)
         n += 1
         if time.perf_counter() - t0 >= target_s:
             break
     dt = time.perf_counter() - t0
-    steps = n - 1
+    steps = n - warmup
     o.close()
     return w.cells * steps / dt / 1e6, steps, dt
 
@@ -192,12 +194,13 @@ def run_reference(args, ranks):
     w = WORKLOADS[args.workload]
     cores = os.cpu_count()
     steps = max(1, min(args.steps, 200))
-    rate, done, secs = cpu_oracle_rate(w, target_s=10.0, max_steps=steps)
+    warmup = max(3, args.warmup)
+    rate, done, secs = cpu_oracle_rate(w, target_s=10.0, max_steps=steps, warmup=warmup)
     sample = (f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} grid of workload {w.name}, {done} FDTD "
               f"steps ({secs:.1f} s) of the FP32 CPU restatement, OpenMP {cores} threads")
     return {
         "impl": "reference", "metric": "Mcell-steps/s", "value": round(rate, 3),
-        "unit": "Mcell-steps/s", "n_gpus": args.gpus, "steps": done, "warmup": 1,
+        "unit": "Mcell-steps/s", "n_gpus": args.gpus, "steps": done, "warmup": warmup,
         "ms_per_step": round(secs / done * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(w),
