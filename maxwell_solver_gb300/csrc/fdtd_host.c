@@ -2381,8 +2381,9 @@ static int batch_rebuild(batch *b) {
       if (ay * az > f) f = ay * az;
       if (ax * az > f) f = ax * az;
       if (f > b->face_max) b->face_max = f;
-      b->any_split = 1;
+      /* the axis-mode face pass and the oblique one serve different members */
       if (op->tfsf_mode == FDTD_MODE_OBLIQUE) b->any_oblique = 1;
+      else b->any_split = 1;
     }
     b->h_steps[g] = m->first + m->done;
     if (s->dev.num_ant > 0) b->any_probes = 1;
