@@ -972,12 +972,17 @@ int fdtdk_batch_faces(int hfam, const fdtd_dev *devs, const fdtd_op *ops, const 
   return (int)cudaGetLastError();
 }
 
+// blocks per face plane and member of the batched oblique face pass
+#ifndef FDTD_BATCH_FACE_BLOCKS
+#define FDTD_BATCH_FACE_BLOCKS 4
+#endif
+
 int fdtdk_batch_faces_oblique(int hfam, const fdtd_dev *devs, const fdtd_op *ops,
                               const int32_t *steps, int32_t n, int32_t max_cells_per_face,
                               cudaStream_t s) {
   if (n <= 0) return 0;
   int bx = (max_cells_per_face + 255) / 256;
-  bx = bx < 1 ? 1 : (bx > 4 ? 4 : bx);
+  bx = bx < 1 ? 1 : (bx > FDTD_BATCH_FACE_BLOCKS ? FDTD_BATCH_FACE_BLOCKS : bx);
   if (hfam) k_batch_faces_oblique<true><<<dim3(bx, 12, n), 256, 0, s>>>(devs, ops, steps);
   else k_batch_faces_oblique<false><<<dim3(bx, 12, n), 256, 0, s>>>(devs, ops, steps);
   ++g_launches;
