@@ -94,7 +94,9 @@ typedef struct sim {
   int32_t i0, i1, j0, j1, k0, k1;
   int64_t size_x, size_y, size_z;
   /* host copies (reference: pinned arrays of setConst / setSource) */
-  float *h_mat[6];      /* sigma_x,y,z, eps_x,y,z; allocated on first use */
+  float *h_mat[6];      /* sigma_x,y,z, eps_x,y,z; each allocated when
+                           UpdateMaterial first sets it (unset: defaults) */
+  int has_mat;          /* UpdateMaterial was called */
   /* media as shapes (fdtd_set_shapes): rasterised on the device instead */
   fdtd_shape *shapes;
   int32_t n_shapes;
@@ -135,6 +137,13 @@ typedef struct sim {
   uint64_t device_bytes;
   fdtd_dev dev;
   pending_t pend;
+  /* per-op steps in the reference order, held so that whole steps go to the
+   * device as graph replays (like fdtd_step_n): UpdateH_All's probe gather
+   * (belongs to the next H half-step), an H half-step waiting for the E
+   * half-step of its step, and a run of complete steps */
+  int gather_pending, held_h;
+  fdtd_op held_op;
+  int32_t run_first, run_n, run_mode;
   /* graph cache for fdtd_step_n */
   cudaGraphExec_t gexec;
   int g_mode, g_cur_mode, g_cur_box[6], g_probes;
@@ -493,16 +502,29 @@ int fdtd_set_const(fdtd_handle h, const float freqRes[3], const int32_t timeDim[
   return FDTD_OK;
 }
 
-/* The host material arrays (sigma 0, eps 1 until UpdateMaterial sets
- * them), allocated when first needed. */
-static int host_materials(sim *s) {
-  for (int a = 0; a < 6; ++a) {
-    if (s->h_mat[a]) continue;
-    s->h_mat[a] = (float *)malloc((size_t)s->IJK * sizeof(float));
-    if (!s->h_mat[a]) return fail(FDTD_ERR_OOM, "out of host memory");
-    const float v = a < 3 ? 0.0f : 1.0f;
-    for (int64_t n = 0; n < s->IJK; ++n) s->h_mat[a][n] = v;
+/* Value of a material array (0..2 sigma, 3..5 eps) that UpdateMaterial
+ * never set: sigma 0, eps 1. */
+static float material_default(int a) { return a < 3 ? 0.0f : 1.0f; }
+
+/* Host <-> device copies of one logical IJK array and its pitched device
+ * copy: one contiguous transfer (rows of I floats at a pitch of Ip), through
+ * a packed device scratch and a device-side 2D copy when the rows are
+ * padded; a host-side 2D copy of J*K short rows is far slower. */
+static int upload_pitched(sim *s, float *dst, const float *src, float *scratch) {
+  const size_t row = (size_t)s->I * sizeof(float);
+  if (s->Ip == s->I || !scratch) {
+    if (s->Ip == s->I)
+      CU(cudaMemcpyAsync(dst, src, (size_t)s->IJK * sizeof(float), cudaMemcpyHostToDevice,
+                         s->stream));
+    else
+      CU(cudaMemcpy2DAsync(dst, (size_t)s->Ip * sizeof(float), src, row, row,
+                           (size_t)s->J * s->K, cudaMemcpyHostToDevice, s->stream));
+    return FDTD_OK;
   }
+  CU(cudaMemcpyAsync(scratch, src, (size_t)s->IJK * sizeof(float), cudaMemcpyHostToDevice,
+                     s->stream));
+  CU(cudaMemcpy2DAsync(dst, (size_t)s->Ip * sizeof(float), scratch, row, row,
+                       (size_t)s->J * s->K, cudaMemcpyDeviceToDevice, s->stream));
   return FDTD_OK;
 }
 
@@ -553,9 +575,12 @@ int fdtd_update_material(fdtd_handle h, int32_t flag, const float *values, size_
                 (long long)s->IJK);
   if (s->shapes)
     return fail(FDTD_ERR_STATE, "UpdateMaterial after SetShapes: the media are the shapes");
-  int rc = host_materials(s);
-  if (rc) return rc;
+  if (!s->h_mat[flag - 1]) {
+    s->h_mat[flag - 1] = (float *)malloc((size_t)s->IJK * sizeof(float));
+    if (!s->h_mat[flag - 1]) return fail(FDTD_ERR_OOM, "out of host memory");
+  }
   memcpy(s->h_mat[flag - 1], values, (size_t)s->IJK * sizeof(float));
+  s->has_mat = 1;
   return FDTD_OK;
 }
 
@@ -563,7 +588,7 @@ int fdtd_set_shapes(fdtd_handle h, float bg_eps_r, float bg_sigma, const fdtd_sh
                     int32_t n) {
   GET(h);
   if (!s->init_const) return fail(FDTD_ERR_STATE, "SetShapes requires SetConst");
-  if (s->h_mat[0]) return fail(FDTD_ERR_STATE, "SetShapes after UpdateMaterial");
+  if (s->has_mat) return fail(FDTD_ERR_STATE, "SetShapes after UpdateMaterial");
   if (n < 0 || (n > 0 && !shapes) || n > FDTD_MAX_SHAPES)
     return fail(FDTD_ERR_INVALID_ARG, "SetShapes takes 0..%d shapes", FDTD_MAX_SHAPES);
   for (int a = 0; a < n; ++a)
@@ -775,7 +800,7 @@ static void shape_material(const sim *s, int i, int j, int k, float *eps, float 
  * per-cell arrays (the kernels then read the 2-byte ids only). */
 static int upload_coefficients(sim *s) {
   const size_t bytes = (size_t)s->cells * sizeof(float);
-  int rc;
+  int rc = FDTD_OK;
   for (int a = 0; a < 6; ++a)
     if (!s->d_ce[a] && (rc = dalloc(s, (void **)&s->d_ce[a], bytes))) return rc;
   fill_dev_struct(s);
@@ -795,11 +820,17 @@ static int upload_coefficients(sim *s) {
     dfree(d_shapes);
     KL(e);
   } else {
-    if ((rc = host_materials(s))) return rc;
-    for (int a = 0; a < 6; ++a)
-      CU(cudaMemcpy2DAsync(s->d_ce[a], (size_t)s->Ip * sizeof(float), s->h_mat[a],
-                           (size_t)s->I * sizeof(float), (size_t)s->I * sizeof(float),
-                           (size_t)s->J * s->K, cudaMemcpyHostToDevice, s->stream));
+    float *scratch = NULL;
+    if (s->Ip != s->I && pool_alloc((void **)&scratch, (size_t)s->IJK * sizeof(float),
+                                    s->stream) != cudaSuccess)
+      scratch = NULL; /* the slower host-side 2D copy instead */
+    for (int a = 0; a < 6 && !rc; ++a) {
+      if (s->h_mat[a]) rc = upload_pitched(s, s->d_ce[a], s->h_mat[a], scratch);
+      else if (fdtdk_fill_f32(s->d_ce[a], material_default(a), s->cells, s->stream))
+        rc = fail(FDTD_ERR_CUDA, "material default fill failed");
+    }
+    dfree(scratch);
+    if (rc) return rc;
   }
   float *ce[6];
   const float *eps[3], *sig[3];
@@ -1529,10 +1560,79 @@ static int check_device_error(sim *s) {
   return FDTD_OK;
 }
 
-static int flush(sim *s) {
+static int run_steps(sim *s, int32_t first, int32_t count, int32_t mode,
+                     const fdtd_current *cur);
+
+/* A half-step that is part of a plain step: curl, CPML and the step's
+ * TF/SF (if any), no current source. */
+static int plain_half(const fdtd_op *o) {
+  return o->curl && o->pml && !o->cur_mode && !o->step_from_dev;
+}
+
+static int issue_gather(sim *s) {
+  s->gather_pending = 0;
+  if (s->dev.num_ant > 0) KL(fdtdk_probe_gather(&s->dev, s->stream));
+  return FDTD_OK;
+}
+
+/* The held run of complete steps goes to the device. */
+static int issue_run(sim *s) {
+  if (!s->run_n) return FDTD_OK;
+  const int32_t first = s->run_first, n = s->run_n;
+  s->run_n = 0;
+  return run_steps(s, first, n, s->run_mode, NULL);
+}
+
+/* The held H half-step (with its probe gather) goes to the device. */
+static int issue_held(sim *s) {
+  if (!s->held_h) return FDTD_OK;
+  s->held_h = 0;
+  int rc = issue_gather(s);
+  if (rc) return rc;
+  return issue(s, 1, &s->held_op);
+}
+
+/* The pending half-step leaves the queue: a plain H half-step after its
+ * probe gather is held; the plain E half-step of the same step and mode
+ * then joins it as one more step of the held run (issued every GRAPH_CHUNK
+ * steps); anything else goes to the device after what is held, in order. */
+static int retire(sim *s) {
   if (!s->pend.active) return FDTD_OK;
   s->pend.active = 0;
-  return issue(s, s->pend.h, &s->pend.op);
+  const fdtd_op *o = &s->pend.op;
+  int rc;
+  if (s->pend.h == 1 && s->gather_pending && !s->held_h && plain_half(o)) {
+    s->held_h = 1;
+    s->held_op = *o;
+    s->gather_pending = 0;
+    return FDTD_OK;
+  }
+  if (s->pend.h == 0 && s->held_h && plain_half(o) && o->tfsf_mode == s->held_op.tfsf_mode &&
+      (!o->tfsf_mode || o->step == s->held_op.step)) {
+    const int32_t n = s->held_op.step, m = o->tfsf_mode;
+    s->held_h = 0;
+    if (s->run_n && (s->run_mode != m || (m && s->run_first + s->run_n != n)) &&
+        (rc = issue_run(s)))
+      return rc;
+    if (!s->run_n) {
+      s->run_first = n;
+      s->run_mode = m;
+    }
+    if (++s->run_n >= GRAPH_CHUNK) return issue_run(s);
+    return FDTD_OK;
+  }
+  if ((rc = issue_run(s)) || (rc = issue_held(s))) return rc;
+  if (s->pend.h == 1 && s->gather_pending && (rc = issue_gather(s))) return rc;
+  return issue(s, s->pend.h, o);
+}
+
+/* Everything queued or held goes to the device, in the call order. */
+static int flush(sim *s) {
+  int rc = retire(s);
+  if (!rc) rc = issue_run(s);
+  if (!rc) rc = issue_held(s);
+  if (!rc && s->gather_pending) rc = issue_gather(s);
+  return rc;
 }
 
 static int need_ready(sim *s) {
@@ -1579,7 +1679,7 @@ static int enqueue(sim *s, int hfam, int rank, const fdtd_op *stage) {
                          (s->pend.op.tfsf_mode || s->pend.op.cur_mode);
   if (s->pend.active &&
       (s->pend.h != hfam || pend_rank(&s->pend.op) >= rank || step_clash)) {
-    int rc = flush(s);
+    int rc = retire(s);
     if (rc) return rc;
   }
   if (!s->pend.active) {
@@ -1607,8 +1707,9 @@ int fdtd_update_h_all(fdtd_handle h) {
   GET(h);
   int rc = need_ready(s);
   if (rc) return rc;
-  if ((rc = flush(s))) return rc;
-  if (s->dev.num_ant > 0) KL(fdtdk_probe_gather(&s->dev, s->stream));
+  if ((rc = retire(s))) return rc;
+  if (s->gather_pending && (rc = issue_gather(s))) return rc;
+  s->gather_pending = 1; /* issued with the H half-step this call starts */
   fdtd_op st;
   memset(&st, 0, sizeof(st));
   return enqueue(s, 1, 1, &st);
@@ -1733,6 +1834,15 @@ int fdtd_step_n(fdtd_handle h, int32_t first, int32_t count, int32_t mode,
   if (mode && (rc = tfsf_check(s, first, mode))) return rc;
   if (use_cur && !s->init_src) return fail(FDTD_ERR_STATE, "current source requires SetSource");
   if ((rc = flush(s))) return rc;
+  return run_steps(s, first, count, mode, cur);
+}
+
+/* Steps first..first+count-1 as GRAPH_CHUNK-step graph replays and single
+ * steps (the arguments already checked). */
+static int run_steps(sim *s, int32_t first, int32_t count, int32_t mode,
+                     const fdtd_current *cur) {
+  int rc;
+  const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
   const int probes = s->dev.num_ant > 0;
   int32_t done = 0;
   if (count >= GRAPH_CHUNK) {
@@ -1901,21 +2011,40 @@ int fdtd_output_vis(fdtd_handle h, float *out, size_t n, int32_t flag) {
       }
       return FDTD_OK;
     }
-    int rc = host_materials(s);
-    if (rc) return rc;
-    memcpy(out, s->h_mat[idx], cnt * sizeof(float));
+    if (s->h_mat[idx]) {
+      memcpy(out, s->h_mat[idx], cnt * sizeof(float));
+    } else {
+      const float v = material_default(idx);
+      for (size_t n2 = 0; n2 < cnt; ++n2) out[n2] = v;
+    }
     return FDTD_OK;
   }
   if (flag >= 1 && flag <= 6) {
     if (!s->init_ready) return fail(FDTD_ERR_STATE, "OutputVis of fields requires ReadySimulation");
     int rc = flush(s);
     if (rc) return rc;
-    /* device rows are pitched: whole rows by a 2D copy, then the tail */
+    /* device rows are pitched: whole rows packed on the device (a 2D
+     * device copy) and read back in one transfer, then the tail */
     const size_t rows = cnt / (size_t)s->I, tail = cnt % (size_t)s->I;
+    const size_t row = (size_t)s->I * sizeof(float);
     const float *src = s->d_f[flag - 1];
-    if (rows)
-      CU(cudaMemcpy2DAsync(out, (size_t)s->I * sizeof(float), src, (size_t)s->Ip * sizeof(float),
-                           (size_t)s->I * sizeof(float), rows, cudaMemcpyDeviceToHost, s->stream));
+    float *scratch = NULL;
+    if (rows && s->Ip != s->I &&
+        pool_alloc((void **)&scratch, rows * row, s->stream) != cudaSuccess)
+      scratch = NULL;
+    if (rows && s->Ip == s->I) {
+      CU(cudaMemcpyAsync(out, src, rows * row, cudaMemcpyDeviceToHost, s->stream));
+    } else if (rows && scratch) {
+      cudaError_t e = cudaMemcpy2DAsync(scratch, row, src, (size_t)s->Ip * sizeof(float), row,
+                                        rows, cudaMemcpyDeviceToDevice, s->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, scratch, rows * row, cudaMemcpyDeviceToHost, s->stream);
+      dfree(scratch);
+      CU(e);
+    } else if (rows) {
+      CU(cudaMemcpy2DAsync(out, row, src, (size_t)s->Ip * sizeof(float), row, rows,
+                           cudaMemcpyDeviceToHost, s->stream));
+    }
     if (tail)
       CU(cudaMemcpyAsync(out + rows * s->I, src + rows * s->Ip, tail * sizeof(float),
                          cudaMemcpyDeviceToHost, s->stream));

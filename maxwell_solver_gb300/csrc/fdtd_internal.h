@@ -201,6 +201,7 @@ int fdtdk_compress_ce(const fdtd_dev *d, const float *const ce[6], uint16_t *mat
  * [2] collision. */
 int fdtdk_probe_gather(const fdtd_dev *d, cudaStream_t s);
 int fdtdk_set_i32(int32_t *dst, int32_t v, cudaStream_t s);
+int fdtdk_fill_f32(float *dst, float v, int64_t n, cudaStream_t s);
 int fdtdk_add_i32(int32_t *dst, int32_t v, cudaStream_t s);
 /* Per-cell E coefficients from device eps/sigma (src/simulation.h:924-938). */
 int fdtdk_compute_ce(const fdtd_dev *d, float *const ce[6],

@@ -551,6 +551,12 @@ __global__ void k_check_division(fdtd_div_plan p, uint64_t first, uint64_t count
 }
 __global__ void k_set_i32(int32_t *p, int32_t v) { *p = v; }
 
+__global__ void k_fill_f32(float *p, float v, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    p[t] = v;
+}
+
 // ------------------------------------------------------ coefficients (setup)
 
 // src/simulation.h:924-938 in the reference's precision: 2*eps0*eps and the
@@ -1011,6 +1017,15 @@ int fdtdk_probe_gather(const fdtd_dev *d, cudaStream_t s) {
   k_probe_gather<<<(nt + 255) / 256, 256, 0, s>>>(*d);
   k_add_i32<<<1, 1, 0, s>>>(d->probe_row, 1);
   g_launches += 2;
+  return (int)cudaGetLastError();
+}
+
+int fdtdk_fill_f32(float *dst, float v, int64_t n, cudaStream_t s) {
+  if (n <= 0) return 0;
+  int64_t bx = (n + 255) / 256;
+  if (bx > 152 * 16) bx = 152 * 16;
+  k_fill_f32<<<(unsigned)bx, 256, 0, s>>>(dst, v, n);
+  ++g_launches;
   return (int)cudaGetLastError();
 }
 
