@@ -155,6 +155,9 @@ SIGNATURES = {
                                                   ctypes.POINTER(ctypes.c_uint64)]),
     "fdtd_division_plan": (ctypes.c_int, [ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
     "fdtd_check_division": (ctypes.c_int, [ctypes.c_float, ctypes.POINTER(ctypes.c_uint64)]),
+    "fdtd_check_bounded_wait": (ctypes.c_int, [ctypes.POINTER(I32), ctypes.POINTER(I32),
+                                               ctypes.POINTER(ctypes.c_double),
+                                               ctypes.POINTER(ctypes.c_double)]),
     "fdtd_launch_count": (ctypes.c_uint64, []),
     "fdtd_last_error": (ctypes.c_char_p, []),
     "fdtd_create_signal": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double,

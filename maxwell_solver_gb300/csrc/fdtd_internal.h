@@ -269,6 +269,11 @@ fdtd_div_plan fdtd_make_div_plan(float dx);
 /* Adds to *out (device) the number of float bit patterns in
  * [first, first + count) whose plan quotient differs bitwise from the IEEE
  * division on the GPU. */
+/* Bounded-wait self-check (fdtd_tma.cu): out[0] = 1 when the wait gave up,
+ * out[1] = clock cycles it took; the production limit and the check's. */
+int fdtdk_check_wait(int arrive, long long out[2]);
+unsigned fdtdk_wait_polls(void);
+unsigned fdtdk_check_polls(void);
 int fdtdk_check_division(fdtd_div_plan p, uint64_t first, uint64_t count,
                          unsigned long long *out, cudaStream_t s);
 

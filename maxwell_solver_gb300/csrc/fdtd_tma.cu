@@ -124,7 +124,9 @@ static_assert(EG<true>::STAGE % 128 == 0 && HG<true>::STAGE % 128 == 0, "batch s
 static_assert(kBatchMinBlocks * (EG<true>::SMEM + 1024) <= 228 * 1024 &&
                   kBatchMinBlocksH * (HG<true>::SMEM + 1024) <= 228 * 1024,
               "batch blocks per SM");
-constexpr unsigned kSpinLimit = 1u << 22;    // bounded mbarrier waits
+// Bounded mbarrier waits: about 1 s, since a poll of a phase that has not
+// completed suspends the thread for ~3.8 us (fdtd_check_bounded_wait).
+constexpr unsigned kSpinLimit = 1u << 18;
 static_assert(E_STAGE % 128 == 0 && H_STAGE % 128 == 0, "stage alignment");
 static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
               "TMA inner box extents must be multiples of 16 bytes");
@@ -184,10 +186,37 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 // Bounded wait for phase `parity` of an mbarrier; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (unsigned it = 0; it < kSpinLimit; ++it)
+// Waits for the phase with the given parity, at most LIMIT polls; false
+// when it gave up (the caller reports the timeout and leaves).
+template <unsigned LIMIT>
+__device__ __forceinline__ bool mbar_wait_n(uint64_t *bar, uint32_t parity) {
+  for (unsigned it = 0; it < LIMIT; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  return mbar_wait_n<kSpinLimit>(bar, parity);
+}
+
+// Self-check of the bounded wait: one thread waits, at most kCheckPolls
+// polls, on a barrier that nothing completes (arrive = 0: it must give up
+// and report it) or that it completes itself first (arrive = 1: it must
+// succeed); out[0] = 1 when it gave up, out[1] = clock cycles spent.
+constexpr unsigned kCheckPolls = 1024;
+__global__ void k_check_wait(long long *out, int arrive) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (arrive) mbar_arrive(&bar);
+    const long long t0 = clock64();
+    const bool ok = mbar_wait_n<kCheckPolls>(&bar, 0);
+    out[1] = clock64() - t0;
+    out[0] = ok ? 0 : 1;
+  }
 }
 // Plain bulk copy global -> shared (16-byte aligned, size a multiple of 16).
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
@@ -836,3 +865,21 @@ int fdtdk_batch_half(int hfam, const fdtd_dev *devs, const void *maps, const fdt
 }
 
 }  // extern "C"
+
+extern "C" int fdtdk_check_wait(int arrive, long long out[2]) {
+  long long *d = nullptr;
+  cudaError_t e = cudaMalloc((void **)&d, 2 * sizeof(long long));
+  if (e != cudaSuccess) return (int)e;
+  e = cudaMemset(d, 0, 2 * sizeof(long long));
+  if (e == cudaSuccess) {
+    k_check_wait<<<1, 32>>>(d, arrive);
+    fdtdk_count_launches(1);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, 2 * sizeof(long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return (int)e;
+}
+
+extern "C" unsigned fdtdk_wait_polls(void) { return kSpinLimit; }
+extern "C" unsigned fdtdk_check_polls(void) { return kCheckPolls; }
