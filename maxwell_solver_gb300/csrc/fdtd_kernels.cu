@@ -898,9 +898,7 @@ static int half_oblique(int hfam, const fdtd_dev *d, const fdtd_maps *m, int use
 int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s) {
   if (op->tfsf_mode == FDTD_MODE_OBLIQUE) return half_oblique(1, d, m, use_tma, op, s);
-  // per-cell H coefficients (fdtd_set_magnetic) run on the direct kernel
-  if (use_tma && m && m->valid && op->curl && d->hcoef_mode == 0)
-    return fdtdk_half_h_tma(d, m, op, s);
+  if (use_tma && m && m->valid && op->curl) return fdtdk_half_h_tma(d, m, op, s);
   const int ni = d->I - 1, nj = d->J - 1, nk = d->K - 1;
   if (op->curl && op->pml) return launch_half(k_half_h<true, true>, d, op, s, ni, nj, nk);
   if (op->curl) return launch_half(k_half_h<true, false>, d, op, s, ni, nj, nk);

@@ -502,8 +502,10 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
 
 // ----------------------------------------------------------------- H half
 
-template <bool PML, bool BATCH>
-__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : FDTD_MIN_BLOCKS_H)
+// MU: per-cell H coefficients (fdtd_set_magnetic), read per cell from the
+// material ids and table (or the arrays); compiled for 3 blocks per SM.
+template <bool PML, bool BATCH, bool MU = false>
+__global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_MIN_BLOCKS_H))
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -639,30 +641,31 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : FDTD_MIN_BLOCKS
         const bool ax = PML && __any_sync(0xffffffffu, act && px >= 0);
         const bool ay = PML && py[c] >= 0, az = PML && pz >= 0;
         const int j = y0 + ty;
+        const HCoef C = MU ? hcoef_at(dp, act ? n0[c] + off : 0) : HCoef{Chh, Chh, Chh, Che, Che, Che};
         if (oth || (int)ax + (int)ay + (int)az > 1) {
           if (act) {
-            update_h_cell<true, PML>(dp, hcoef_uniform(dp), mode, inc, i, j, k, px, py[c], pz,
+            update_h_cell<true, PML>(dp, C, mode, inc, i, j, k, px, py[c], pz,
                                      hx, hy, hz, dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z,
                                      BATCH ? dp.bH : s_xbc[0], BATCH ? dp.cH : s_xbc[1]);
           }
         } else {
-          hx = Chh * hx + Che * (-dEz_y + dEy_z);
-          hy = Chh * hy + Che * (-dEx_z + dEz_x);
-          hz = Chh * hz + Che * (-dEy_x + dEx_y);
+          hx = C.hhx * hx + C.hex * (-dEz_y + dEy_z);
+          hy = C.hhy * hy + C.hey * (-dEx_z + dEz_x);
+          hz = C.hhz * hz + C.hez * (-dEy_x + dEx_y);
           if (PML && act) {
             if (ax) {
               if (px >= 0) {
                 float2 *X = psi_at_x(dp, PSI_HX, px, j, k);
                 const float xb = BATCH ? dp.bH[px] : s_xbc[0][px];
                 const float xc = BATCH ? dp.cH[px] : s_xbc[1][px];
-                h_corr_x_bc(dp, xb, xc, *X, X, dEz_x, dEy_x, hy, hz, Che, Che);
+                h_corr_x_bc(dp, xb, xc, *X, X, dEz_x, dEy_x, hy, hz, C.hey, C.hez);
               }
             } else if (ay) {
               float2 *Y = psi_at_y(dp, PSI_HY, i, py[c], k);
-              h_corr_y(dp, py[c], *Y, Y, dEz_y, dEx_y, hx, hz, Che, Che);
+              h_corr_y(dp, py[c], *Y, Y, dEz_y, dEx_y, hx, hz, C.hex, C.hez);
             } else if (az) {
               float2 *Z = psi_at_z(dp, PSI_HZ, i, j, pz);
-              h_corr_z(dp, pz, *Z, Z, dEy_z, dEx_z, hx, hy, Che, Che);
+              h_corr_z(dp, pz, *Z, Z, dEy_z, dEx_z, hx, hy, C.hex, C.hey);
             }
           }
         }
@@ -759,7 +762,7 @@ int encode(CUtensorMap *out, void *base, CUtensorMapDataType dt, int esize, cons
   return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
 }
 
-int g_blocks_e[2] = {0, 0}, g_blocks_h[2] = {0, 0}, g_blocks_b[2] = {0, 0};
+int g_blocks_e[2] = {0, 0}, g_blocks_h[4] = {0, 0, 0, 0}, g_blocks_b[2] = {0, 0};
 
 // Resident blocks of a kernel on the current device (cached per kernel).
 template <class KH>
@@ -822,10 +825,18 @@ int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
 int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
   fdtd_op o = *op;
   o.tfsf_split = fdtd_tfsf_split(d, op);
-  const int e = o.pml ? launch(k_half_h_tma<true, false>, H_SMEM, &g_blocks_h[1], d, m, &o, s,
-                               d->I - 1, d->J - 1, d->K - 1, d->zc_h)
-                      : launch(k_half_h_tma<false, false>, H_SMEM, &g_blocks_h[0], d, m, &o, s,
-                               d->I - 1, d->J - 1, d->K - 1, d->zc_h);
+  const int ni = d->I - 1, nj = d->J - 1, nk = d->K - 1;
+  int e;
+  if (d->hcoef_mode)  // per-cell H coefficients
+    e = o.pml ? launch(k_half_h_tma<true, false, true>, H_SMEM, &g_blocks_h[3], d, m, &o, s, ni,
+                       nj, nk, d->zc_h)
+              : launch(k_half_h_tma<false, false, true>, H_SMEM, &g_blocks_h[2], d, m, &o, s,
+                       ni, nj, nk, d->zc_h);
+  else
+    e = o.pml ? launch(k_half_h_tma<true, false>, H_SMEM, &g_blocks_h[1], d, m, &o, s, ni, nj,
+                       nk, d->zc_h)
+              : launch(k_half_h_tma<false, false>, H_SMEM, &g_blocks_h[0], d, m, &o, s, ni, nj,
+                       nk, d->zc_h);
   if (e || !o.tfsf_split) return e;
   return fdtdk_faces(1, d, &o, s);
 }
