@@ -132,7 +132,7 @@ typedef struct sim {
   int32_t *d_hid, *d_hcnt;
   int32_t coef_mode, num_mat;
   int use_tma, allow_compress;
-  fdtd_maps maps;
+  fdtd_maps maps, maps_b; /* single-grid and batched kernels' tiles */
   int32_t zc_h, zc_e; /* tuned z-planes per TMA work item (0: heuristic) */
   uint64_t device_bytes;
   fdtd_dev dev;
@@ -1107,6 +1107,7 @@ int fdtd_ready_simulation(fdtd_handle h) {
   if (s->use_tma) {
     int e = fdtdk_make_maps(&s->dev, &s->maps);
     if (e) s->maps.valid = 0; /* the direct kernels take over */
+    if (e || fdtdk_make_maps_batch(&s->dev, &s->maps_b)) s->maps_b.valid = 0;
   }
   if ((rc = autotune_zero_state(s))) return rc;
   CU(cudaStreamSynchronize(s->stream));
@@ -2355,7 +2356,7 @@ int fdtd_batch_add(fdtd_batch bh, fdtd_handle h, int32_t first, int32_t count, i
   sim *s = lookup(h);
   if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "invalid simulation handle");
   if (!s->init_ready) return fail(FDTD_ERR_STATE, "batch members need ReadySimulation");
-  if (!s->maps.valid) return fail(FDTD_ERR_UNSUPPORTED, "batch members need the TMA kernels");
+  if (!s->maps_b.valid) return fail(FDTD_ERR_UNSUPPORTED, "batch members need the TMA kernels");
   if (s->hcoef_mode)
     return fail(FDTD_ERR_UNSUPPORTED, "batch members need uniform H coefficients (no SetMagnetic)");
   if (first < 0 || count < 0) return fail(FDTD_ERR_INVALID_ARG, "negative step range");
@@ -2425,8 +2426,8 @@ static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk) {
   const int zr = batch_zrun();
   for (int kb = 0; kb < nk; kb += zr) {
     const int np = nk - kb < zr ? nk - kb : zr;
-    for (int y0 = 0; y0 < nj; y0 += FDTD_TILE_Y)
-      for (int x0 = 0; x0 < ni; x0 += FDTD_TILE_X) {
+    for (int y0 = 0; y0 < nj; y0 += FDTD_BTILE_Y)
+      for (int x0 = 0; x0 < ni; x0 += FDTD_BTILE_X) {
         int32_t *e = tab + 4 * (size_t)n;
         e[0] = g;
         e[1] = x0;
@@ -2439,7 +2440,7 @@ static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk) {
 }
 
 static int count_items(int ni, int nj, int nk) {
-  return ((ni + FDTD_TILE_X - 1) / FDTD_TILE_X) * ((nj + FDTD_TILE_Y - 1) / FDTD_TILE_Y) *
+  return ((ni + FDTD_BTILE_X - 1) / FDTD_BTILE_X) * ((nj + FDTD_BTILE_Y - 1) / FDTD_BTILE_Y) *
          ((nk + batch_zrun() - 1) / batch_zrun());
 }
 
@@ -2506,7 +2507,7 @@ static int batch_rebuild(batch *b) {
     sim *s = lookup(m->h);
     b->act[g] = i;
     b->h_devs[g] = s->dev;
-    memcpy(b->h_maps + (size_t)g * mapsz, s->maps.bytes, mapsz);
+    memcpy(b->h_maps + (size_t)g * mapsz, s->maps_b.bytes, mapsz);
     fdtd_op *op = &b->h_ops[g];
     memset(op, 0, sizeof(*op));
     op->curl = 1;

@@ -180,8 +180,11 @@ int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_
                  cudaStream_t s);
 int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s);
-/* Encodes the TMA descriptors for the current device pointers (fdtd_tma.cu). */
+/* Encodes the TMA descriptors for the current device pointers (fdtd_tma.cu):
+ * the single-grid kernels' boxes (FDTD_TILE_X x FDTD_TILE_Y tiles) and the
+ * batched kernels' (FDTD_BTILE_X x FDTD_BTILE_Y). */
 int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m);
+int fdtdk_make_maps_batch(const fdtd_dev *d, fdtd_maps *m);
 int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s);
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s);
 /* The E CPML X corrections over the x-slab cells of a grid whose curl kernel
@@ -226,6 +229,8 @@ int fdtdk_batch_advance(int32_t *steps, int32_t n, cudaStream_t s);
 /* Batched-tile geometry of the TMA kernels. */
 #define FDTD_TILE_X 64
 #define FDTD_TILE_Y 8
+#define FDTD_BTILE_X 32
+#define FDTD_BTILE_Y 16
 
 /* Per-cell mu coefficients (src/simulation.h:43-63). */
 int fdtdk_compute_mu(float *out, const float *mu, const float *den_hx,

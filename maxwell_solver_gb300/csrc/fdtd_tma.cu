@@ -37,6 +37,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <type_traits>
+
 #include "fdtd_device.cuh"
 #include "fdtd_internal.h"
 
@@ -46,7 +48,6 @@ extern "C" void fdtdk_count_launches(unsigned long long n);
 
 namespace {
 
-constexpr int BX = 64, BY = 8;
 constexpr int NCW = 8;                       // consumer warps
 constexpr int NT = (NCW + 1) * 32;           // + one producer warp
 #ifndef FDTD_NSE
@@ -83,17 +84,35 @@ constexpr int kBatchMinBlocks = FDTD_BATCH_MIN_BLOCKS;  // E (and the default fo
 constexpr int kBatchNS = FDTD_BATCH_NS;
 constexpr int kBatchMinBlocksH = FDTD_BATCH_MIN_BLOCKS_H;
 constexpr int kBatchNSH = FDTD_BATCH_NS_H;
-constexpr int HW = BX + 4;                   // halo box row (floats)
-constexpr int HH = BY + 1;                   // halo box rows
-constexpr int TILE_B = BX * BY * 4;          // 2048 B
-constexpr int HALO_B = HW * HH * 4;          // 2448 B transferred
-constexpr int HALO_SLOT = 2560;              // 128-byte aligned slot
-constexpr int MAT_B = BX * BY * 2;           // 1024 B
-constexpr int E_OFF_H = 3 * TILE_B;
-constexpr int E_OFF_M = E_OFF_H + 3 * HALO_SLOT;
-constexpr int E_STAGE = E_OFF_M + MAT_B;     // 14848 B
-constexpr int H_OFF_H = 3 * HALO_SLOT;
-constexpr int H_STAGE = H_OFF_H + 3 * TILE_B;  // 13824 B
+// Tile geometry: a work item is a BX x BY tile of cells over a run of
+// z-planes.  The single-grid kernels use 64 x 8; the batched ones 32 x 16,
+// since their grids are narrow (32..128 cells in x) and a 64-wide tile of a
+// 70-cell axis leaves most lanes of its second tile idle.  Both have the
+// same stage byte sizes.
+template <int BX_, int BY_>
+struct Geo {
+  static constexpr int BX = BX_, BY = BY_;
+  static constexpr int HW = BX + 4;                   // halo box row (floats)
+  static constexpr int HH = BY + 1;                   // halo box rows
+  static constexpr int TILE_B = BX * BY * 4;          // 2048 B
+  static constexpr int HALO_B = HW * HH * 4;          // bytes transferred
+  static constexpr int HALO_SLOT = (HALO_B + 127) / 128 * 128;  // 128-byte aligned slot
+  static constexpr int MAT_B = BX * BY * 2;           // 1024 B
+  static constexpr int E_OFF_H = 3 * TILE_B;
+  static constexpr int E_OFF_M = E_OFF_H + 3 * HALO_SLOT;
+  static constexpr int E_STAGE = E_OFF_M + MAT_B;
+  static constexpr int H_OFF_H = 3 * HALO_SLOT;
+  static constexpr int H_STAGE = H_OFF_H + 3 * TILE_B;
+  static_assert(BX % 32 == 0 && (256 / 32) % (BX / 32) == 0 && BX * BY == 512,
+                "8 consumer warps, two cells per thread");
+  static_assert(E_STAGE % 128 == 0 && H_STAGE % 128 == 0, "stage alignment");
+  static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
+                "TMA inner box extents must be multiples of 16 bytes");
+};
+using GS = Geo<64, 8>;   // single-grid kernels
+using GB = Geo<32, 16>;  // batched kernels
+template <bool BATCH>
+using GeoOf = typename std::conditional<BATCH, GB, GS>::type;
 constexpr int kSmemTabMax = 512;             // coefficient ids staged in shared memory
 constexpr int CTRL_B = 512;                  // barriers + stage metadata
 // Batch mode: every stage also carries its grid's descriptor and op (bulk
@@ -109,13 +128,14 @@ static_assert(sizeof(fdtd_op) <= OPSLOT_B && sizeof(fdtd_op) % 16 == 0, "op slot
 template <bool BATCH>
 struct EG {
   static constexpr int NS = BATCH ? kBatchNS : NSE;
-  static constexpr int STAGE = BATCH ? E_STAGE + DESC_B + OPSLOT_B + TAB_B : E_STAGE;
+  static constexpr int STAGE =
+      BATCH ? GB::E_STAGE + DESC_B + OPSLOT_B + TAB_B : GS::E_STAGE;
   static constexpr int SMEM = NS * STAGE + CTRL_B + (BATCH ? 0 : kSmemTabMax * 6 * 4);
 };
 template <bool BATCH>
 struct HG {
   static constexpr int NS = BATCH ? kBatchNSH : NSH;
-  static constexpr int STAGE = BATCH ? H_STAGE + DESC_B + OPSLOT_B : H_STAGE;
+  static constexpr int STAGE = BATCH ? GB::H_STAGE + DESC_B + OPSLOT_B : GS::H_STAGE;
   static constexpr int SMEM = NS * STAGE + CTRL_B;
 };
 constexpr int E_SMEM = EG<false>::SMEM;
@@ -127,9 +147,6 @@ static_assert(kBatchMinBlocks * (EG<true>::SMEM + 1024) <= 228 * 1024 &&
 // Bounded mbarrier waits: about 1 s, since a poll of a phase that has not
 // completed suspends the thread for ~3.8 us (fdtd_check_bounded_wait).
 constexpr unsigned kSpinLimit = 1u << 18;
-static_assert(E_STAGE % 128 == 0 && H_STAGE % 128 == 0, "stage alignment");
-static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
-              "TMA inner box extents must be multiples of 16 bytes");
 static_assert(NSH * (8 + 8 + 32) <= CTRL_B && NSE * (8 + 8 + 32) <= CTRL_B &&
                   kBatchNS * (8 + 8 + 32) <= CTRL_B && kBatchNSH * (8 + 8 + 32) <= CTRL_B,
               "control block");
@@ -250,8 +267,8 @@ __device__ __forceinline__ void decode_item(const Items &it, int w, int &g, int 
     const int nt = it.tiles_x * it.tiles_y;
     const int chunk = w / nt, tile = w - chunk * nt;
     g = 0;
-    x0 = (tile % it.tiles_x) * BX;
-    y0 = (tile / it.tiles_x) * BY;
+    x0 = (tile % it.tiles_x) * GS::BX;
+    y0 = (tile / it.tiles_x) * GS::BY;
     kb = chunk * it.zchunk;
     np = min(it.zchunk, it.nk - kb);
   }
@@ -304,12 +321,15 @@ __device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *em
 }
 
 // Thread -> cell map of the consumer warps: warp w covers one 32-cell x run
-// (half w & 1 of the 64-wide tile) of rows w >> 1 and (w >> 1) + 4, so that
-// whole warps fall inside or outside the CPML x slabs and TF/SF x faces.
+// (run w % (BX/32) of the tile's row) of rows r0 = w / (BX/32) and
+// r0 + BY/2, so that whole warps fall inside or outside the CPML x slabs and
+// TF/SF x faces.
+template <class G>
 __device__ __forceinline__ void cell_map(int tid, int &xo, int &r0) {
+  constexpr int WPR = G::BX / 32;  // warps per tile row
   const int w = tid >> 5;
-  xo = 32 * (w & 1) + (tid & 31);
-  r0 = w >> 1;
+  xo = 32 * (w % WPR) + (tid & 31);
+  r0 = w / WPR;
 }
 
 // ----------------------------------------------------------------- E half
@@ -319,6 +339,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
     k_half_e_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
+  using G = GeoOf<BATCH>;
   constexpr int ST = EG<BATCH>::STAGE;
   constexpr int NS = EG<BATCH>::NS;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * ST);
@@ -363,18 +384,18 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
         const uint32_t desc_b = BATCH ? (uint32_t)(sizeof(fdtd_dev) + sizeof(fdtd_op)) : 0u;
         proxy_fence();
         // one arrive per phase: the stage's whole byte count at once
-        mbar_expect_tx(&full[s], desc_b + 3 * TILE_B + 3 * HALO_B + (um ? MAT_B : 0) +
+        mbar_expect_tx(&full[s], desc_b + 3 * G::TILE_B + 3 * G::HALO_B + (um ? G::MAT_B : 0) +
                                      (BATCH ? tab_b : 0u));
         if (BATCH) {
-          bulk_g2s(st + E_STAGE, &it.devs[g], sizeof(fdtd_dev), &full[s]);
-          bulk_g2s(st + E_STAGE + DESC_B, &it.ops[g], sizeof(fdtd_op), &full[s]);
+          bulk_g2s(st + G::E_STAGE, &it.devs[g], sizeof(fdtd_dev), &full[s]);
+          bulk_g2s(st + G::E_STAGE + DESC_B, &it.ops[g], sizeof(fdtd_op), &full[s]);
           if (tab_b)
-            bulk_g2s(st + E_STAGE + DESC_B + OPSLOT_B, it.devs[g].mat_tab, tab_b, &full[s]);
+            bulk_g2s(st + G::E_STAGE + DESC_B + OPSLOT_B, it.devs[g].mat_tab, tab_b, &full[s]);
         }
-        for (int c = 0; c < 3; ++c) tma_load_3d(st + c * TILE_B, &mm[c], &full[s], x0, y0, k);
+        for (int c = 0; c < 3; ++c) tma_load_3d(st + c * G::TILE_B, &mm[c], &full[s], x0, y0, k);
         for (int c = 0; c < 3; ++c)
-          tma_load_3d(st + E_OFF_H + c * HALO_SLOT, &mm[3 + c], &full[s], x0 - 4, y0 - 1, k);
-        if (um) tma_load_3d(st + E_OFF_M, &mm[12], &full[s], x0, y0, k);
+          tma_load_3d(st + G::E_OFF_H + c * G::HALO_SLOT, &mm[3 + c], &full[s], x0 - 4, y0 - 1, k);
+        if (um) tma_load_3d(st + G::E_OFF_M, &mm[12], &full[s], x0, y0, k);
       });
     }
     return;
@@ -382,7 +403,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
 
   // ------------------------------------------------------------ consumers
   int xo, r0;
-  cell_map(tid, xo, r0);
+  cell_map<G>(tid, xo, r0);
   // per-item state
   int i = 0, y0 = 0, kb = 0, mode = 0, cm = 0;
   bool use_mat = false, tab_local = false;
@@ -401,14 +422,14 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
     const int4 m = meta[2 * s];
     if (m.x < 0) return;  // sentinel
     const unsigned char *st = smem + s * ST;
-    const fdtd_dev &d = BATCH ? *reinterpret_cast<const fdtd_dev *>(st + E_STAGE) : d0;
-    const fdtd_op &op = BATCH ? *reinterpret_cast<const fdtd_op *>(st + E_STAGE + DESC_B) : op0;
-    const float *ttab = BATCH ? reinterpret_cast<const float *>(st + E_STAGE + DESC_B + OPSLOT_B)
+    const fdtd_dev &d = BATCH ? *reinterpret_cast<const fdtd_dev *>(st + G::E_STAGE) : d0;
+    const fdtd_op &op = BATCH ? *reinterpret_cast<const fdtd_op *>(st + G::E_STAGE + DESC_B) : op0;
+    const float *ttab = BATCH ? reinterpret_cast<const float *>(st + G::E_STAGE + DESC_B + OPSLOT_B)
                               : stab;
     const int I = d.I, J = d.J, K = d.K;
-    const float *sHx = reinterpret_cast<const float *>(st + E_OFF_H);
-    const float *sHy = sHx + HALO_SLOT / 4;
-    const float *sHz = sHy + HALO_SLOT / 4;
+    const float *sHx = reinterpret_cast<const float *>(st + G::E_OFF_H);
+    const float *sHy = sHx + G::HALO_SLOT / 4;
+    const float *sHz = sHy + G::HALO_SLOT / 4;
     if (m.y == 0) {  // first plane of a new item: column constants
       const int4 m1 = meta[2 * s + 1];
       kb = m.w;
@@ -427,7 +448,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
                              (mode && (i == d.i0 || i == d.i1)) || i == 0;
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
-        const int j = y0 + r0 + 4 * c;
+        const int j = y0 + r0 + (G::BY / 2) * c;
         valid[c] = i < I && j < J;
         cur_col[c] = cur_x && in_range(j, op.cur_box[2], op.cur_box[3]);
         col_special[c] = x_special || (PML && slab_e(j, J, d.p) >= 0) ||
@@ -442,19 +463,19 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
     }
     const int k = kb + m.y;
     const float *sEx = reinterpret_cast<const float *>(st);
-    const float *sEy = sEx + BX * BY;
-    const float *sEz = sEy + BX * BY;
-    const uint16_t *sM = reinterpret_cast<const uint16_t *>(st + E_OFF_M);
+    const float *sEy = sEx + G::BX * G::BY;
+    const float *sEz = sEy + G::BX * G::BY;
+    const uint16_t *sM = reinterpret_cast<const uint16_t *>(st + G::E_OFF_M);
     const bool plane_special = (PML && slab_e(k, K, d.p) >= 0) ||
                                (mode && (k == d.k0 || k == d.k1)) || k == 0 ||
                                (cm && in_range(k, op.cur_box[4], op.cur_box[5]));
     const int64_t off = (int64_t)m.y * d.plane;
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-      const int ty = r0 + 4 * c;
+      const int ty = r0 + (G::BY / 2) * c;
       const bool act = valid[c];
-      const int hb = (ty + 1) * HW + xo + 4;  // own cell in the halo tile
-      const int eb = ty * BX + xo;            // own cell in the plain tile
+      const int hb = (ty + 1) * G::HW + xo + 4;  // own cell in the halo tile
+      const int eb = ty * G::BX + xo;            // own cell in the plain tile
       Coef6 C = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       if (use_mat) {
         const int mi = sM[eb];
@@ -468,7 +489,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
         C = coef_from_arrays(d, n0[c] + off);
       }
       const float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
-      const float hz_jm = sHz[hb - HW], hx_jm = sHx[hb - HW];
+      const float hz_jm = sHz[hb - G::HW], hx_jm = sHx[hb - G::HW];
       const float hz_im = sHz[hb - 1], hy_im = sHy[hb - 1];
       float ex = sEx[eb], ey = sEy[eb], ez = sEz[eb];
       if (__any_sync(0xffffffffu, act && (col_special[c] || plane_special))) {
@@ -509,6 +530,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   extern __shared__ __align__(128) unsigned char smem[];
+  using G = GeoOf<BATCH>;
   constexpr int ST = HG<BATCH>::STAGE;
   constexpr int NS = HG<BATCH>::NS;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * ST);
@@ -536,7 +558,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
 
   if (warp == NCW) {  // ------------------------------------- producer
     if (lane == 0) {
-      const uint32_t tx_bytes = 3 * HALO_B + 3 * TILE_B;
+      const uint32_t tx_bytes = 3 * G::HALO_B + 3 * G::TILE_B;
       const auto step_of = [&](int g) {
         return (BATCH ? it.steps[g] + it.ops[g].step : op_step(d0, op0));
       };
@@ -548,13 +570,13 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
         mbar_expect_tx(&full[s], tx_bytes + (BATCH ? (uint32_t)(sizeof(fdtd_dev) +
                                                                 sizeof(fdtd_op)) : 0u));
         if (BATCH) {
-          bulk_g2s(st + H_STAGE, &it.devs[g], sizeof(fdtd_dev), &full[s]);
-          bulk_g2s(st + H_STAGE + DESC_B, &it.ops[g], sizeof(fdtd_op), &full[s]);
+          bulk_g2s(st + G::H_STAGE, &it.devs[g], sizeof(fdtd_dev), &full[s]);
+          bulk_g2s(st + G::H_STAGE + DESC_B, &it.ops[g], sizeof(fdtd_op), &full[s]);
         }
         for (int c = 0; c < 3; ++c)
-          tma_load_3d(st + c * HALO_SLOT, &mm[6 + c], &full[s], x0, y0, k);
+          tma_load_3d(st + c * G::HALO_SLOT, &mm[6 + c], &full[s], x0, y0, k);
         for (int c = 0; c < 3; ++c)
-          tma_load_3d(st + H_OFF_H + c * TILE_B, &mm[9 + c], &full[s], x0, y0, k);
+          tma_load_3d(st + G::H_OFF_H + c * G::TILE_B, &mm[9 + c], &full[s], x0, y0, k);
       });
     }
     return;
@@ -562,7 +584,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
 
   // ------------------------------------------------------------ consumers
   int xo, r0;
-  cell_map(tid, xo, r0);
+  cell_map<G>(tid, xo, r0);
 
   int q = 0;
   for (;;) {
@@ -578,9 +600,9 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
     // the item's descriptor and op: the first load's copies (every load of
     // the item carries the same ones)
     const unsigned char *st_item = smem + s * ST;
-    const fdtd_dev &d = BATCH ? *reinterpret_cast<const fdtd_dev *>(st_item + H_STAGE) : d0;
+    const fdtd_dev &d = BATCH ? *reinterpret_cast<const fdtd_dev *>(st_item + G::H_STAGE) : d0;
     const fdtd_op &op =
-        BATCH ? *reinterpret_cast<const fdtd_op *>(st_item + H_STAGE + DESC_B) : op0;
+        BATCH ? *reinterpret_cast<const fdtd_op *>(st_item + G::H_STAGE + DESC_B) : op0;
     const int I = d.I, J = d.J, K = d.K, p = d.p;
     const int mode = op.tfsf_split ? 0 : op.tfsf_mode;  // split: the face pass applies it
     const float *inc = mode ? inc_h_row(d, mode, m1.w) : nullptr;
@@ -593,7 +615,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
     int64_t n0[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-      const int j = y0 + r0 + 4 * c;
+      const int j = y0 + r0 + (G::BY / 2) * c;
       valid[c] = i < I - 1 && j < J - 1;
       py[c] = PML ? slab_h(j, J, p) : -1;
       col_face[c] = x_face || (mode && (j == d.j0 - 1 || j == d.j1));
@@ -611,27 +633,27 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
       const unsigned char *st0 = smem + prev * ST;
       // descriptor of the stage in use (the item's first stage may already
       // have been handed back to the producer)
-      const fdtd_dev &dp = BATCH ? *reinterpret_cast<const fdtd_dev *>(st0 + H_STAGE) : d0;
+      const fdtd_dev &dp = BATCH ? *reinterpret_cast<const fdtd_dev *>(st0 + G::H_STAGE) : d0;
       const unsigned char *st1 = smem + s * ST;
       const float *sEx = reinterpret_cast<const float *>(st0);
-      const float *sEy = sEx + HALO_SLOT / 4;
-      const float *sEz = sEy + HALO_SLOT / 4;
+      const float *sEy = sEx + G::HALO_SLOT / 4;
+      const float *sEz = sEy + G::HALO_SLOT / 4;
       const float *sEx1 = reinterpret_cast<const float *>(st1);
-      const float *sEy1 = sEx1 + HALO_SLOT / 4;
-      const float *sHx = reinterpret_cast<const float *>(st0 + H_OFF_H);
-      const float *sHy = sHx + BX * BY;
-      const float *sHz = sHy + BX * BY;
+      const float *sEy1 = sEx1 + G::HALO_SLOT / 4;
+      const float *sHx = reinterpret_cast<const float *>(st0 + G::H_OFF_H);
+      const float *sHy = sHx + G::BX * G::BY;
+      const float *sHz = sHy + G::BX * G::BY;
       const int pz = PML ? slab_h(k, K, p) : -1;
       const bool plane_face = mode && (k == dp.k0 - 1 || k == dp.k1);
       const int64_t off = (int64_t)t * dp.plane;
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
-        const int ty = r0 + 4 * c;
+        const int ty = r0 + (G::BY / 2) * c;
         const bool act = valid[c];
-        const int eb = ty * HW + xo;  // own cell in the halo tile
-        const int hb = ty * BX + xo;  // own cell in the plain tile
+        const int eb = ty * G::HW + xo;  // own cell in the halo tile
+        const int hb = ty * G::BX + xo;  // own cell in the plain tile
         const float ex = sEx[eb], ey = sEy[eb], ez = sEz[eb];
-        const float dEz_y = sEz[eb + HW] - ez, dEx_y = sEx[eb + HW] - ex;
+        const float dEz_y = sEz[eb + G::HW] - ez, dEx_y = sEx[eb + G::HW] - ex;
         const float dEz_x = sEz[eb + 1] - ez, dEy_x = sEy[eb + 1] - ey;
         const float dEy_z = sEy1[eb] - ey, dEx_z = sEx1[eb] - ex;
         float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
@@ -723,8 +745,8 @@ int launch(KH kern, int smem, int *cached_blocks, const fdtd_dev *d, const fdtd_
   memset(&it, 0, sizeof(it));
   it.work = d->work;
   it.err = d->err;
-  it.tiles_x = (ni + BX - 1) / BX;
-  it.tiles_y = (nj + BY - 1) / BY;
+  it.tiles_x = (ni + GS::BX - 1) / GS::BX;
+  it.tiles_y = (nj + GS::BY - 1) / GS::BY;
   it.nk = nk;
   it.zchunk = pick_zchunk(it.tiles_x * it.tiles_y, nk, *cached_blocks);
   if (zc_tuned > 0 && !getenv("FDTD_TMA_ZCHUNK")) it.zchunk = zc_tuned < nk ? zc_tuned : nk;
@@ -779,11 +801,9 @@ int resident_blocks(KH kern, int smem, int *cached) {
   return 0;
 }
 
-}  // namespace
-
-extern "C" {
-
-int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) {
+template <class G>
+int make_maps(const fdtd_dev *d, fdtd_maps *m) {
+  constexpr int BX = G::BX, BY = G::BY, HW = G::HW, HH = G::HH;
   m->valid = 0;
   // TMA: 16-byte aligned base and strides; the pitch guarantees the strides
   if (((d->Ip * 4) % 16) || ((d->Ip * 2) % 16)) return (int)cudaErrorInvalidValue;
@@ -806,6 +826,14 @@ int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) {
   if (!e) m->valid = 1;
   return e;
 }
+
+
+}  // namespace
+
+extern "C" {
+
+int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) { return make_maps<GS>(d, m); }
+int fdtdk_make_maps_batch(const fdtd_dev *d, fdtd_maps *m) { return make_maps<GB>(d, m); }
 
 // The curl kernel, then the x-slab pass (CPML X, when it can be split off)
 // and the face pass (TF/SF, when it can): their cells are disjoint.
