@@ -2213,13 +2213,13 @@ int fdtd_create_signal(double fctr, double delT, double percentage_bw, double nu
 
 #define MAX_BATCHES 256
 
-/* z-planes per batched work item: 8, or FDTD_BATCH_ZRUN (1..64) */
+/* z-planes per batched work item: 16, or FDTD_BATCH_ZRUN (1..64) */
 static int batch_zrun(void) {
   static int z = 0;
   if (!z) {
     const char *e = getenv("FDTD_BATCH_ZRUN");
     const int v = e ? atoi(e) : 0;
-    z = v >= 1 && v <= 64 ? v : 8;
+    z = v >= 1 && v <= 64 ? v : 16;
   }
   return z;
 }
