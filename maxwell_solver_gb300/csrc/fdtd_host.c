@@ -94,8 +94,8 @@ typedef struct sim {
   int32_t i0, i1, j0, j1, k0, k1;
   int64_t size_x, size_y, size_z;
   /* host copies (reference: pinned arrays of setConst / setSource) */
-  float *h_mat[6];      /* sigma_x,y,z, eps_x,y,z; each allocated when
-                           UpdateMaterial first sets it (unset: defaults) */
+  float *d_raw[6];      /* sigma_x,y,z, eps_x,y,z as UpdateMaterial gave them
+                           (device, packed I*J*K); unset: the defaults */
   int has_mat;          /* UpdateMaterial was called */
   /* media as shapes (fdtd_set_shapes): rasterised on the device instead */
   fdtd_shape *shapes;
@@ -383,7 +383,7 @@ int fdtd_destroy(fdtd_handle h) {
   for (int a = 0; a < 6; ++a) {
     dfree(s->d_f[a]);
     dfree(s->d_ce[a]);
-    free(s->h_mat[a]);
+    dfree(s->d_raw[a]);
   }
   free(s->shapes);
   for (int a = 0; a < 4; ++a) dfree(s->d_inc[a]);
@@ -506,28 +506,6 @@ int fdtd_set_const(fdtd_handle h, const float freqRes[3], const int32_t timeDim[
  * never set: sigma 0, eps 1. */
 static float material_default(int a) { return a < 3 ? 0.0f : 1.0f; }
 
-/* Host <-> device copies of one logical IJK array and its pitched device
- * copy: one contiguous transfer (rows of I floats at a pitch of Ip), through
- * a packed device scratch and a device-side 2D copy when the rows are
- * padded; a host-side 2D copy of J*K short rows is far slower. */
-static int upload_pitched(sim *s, float *dst, const float *src, float *scratch) {
-  const size_t row = (size_t)s->I * sizeof(float);
-  if (s->Ip == s->I || !scratch) {
-    if (s->Ip == s->I)
-      CU(cudaMemcpyAsync(dst, src, (size_t)s->IJK * sizeof(float), cudaMemcpyHostToDevice,
-                         s->stream));
-    else
-      CU(cudaMemcpy2DAsync(dst, (size_t)s->Ip * sizeof(float), src, row, row,
-                           (size_t)s->J * s->K, cudaMemcpyHostToDevice, s->stream));
-    return FDTD_OK;
-  }
-  CU(cudaMemcpyAsync(scratch, src, (size_t)s->IJK * sizeof(float), cudaMemcpyHostToDevice,
-                     s->stream));
-  CU(cudaMemcpy2DAsync(dst, (size_t)s->Ip * sizeof(float), scratch, row, row,
-                       (size_t)s->J * s->K, cudaMemcpyDeviceToDevice, s->stream));
-  return FDTD_OK;
-}
-
 /* src/simulation.h:1068-1082 */
 int fdtd_set_source(fdtd_handle h, const float *src, size_t n) {
   GET(h);
@@ -575,11 +553,12 @@ int fdtd_update_material(fdtd_handle h, int32_t flag, const float *values, size_
                 (long long)s->IJK);
   if (s->shapes)
     return fail(FDTD_ERR_STATE, "UpdateMaterial after SetShapes: the media are the shapes");
-  if (!s->h_mat[flag - 1]) {
-    s->h_mat[flag - 1] = (float *)malloc((size_t)s->IJK * sizeof(float));
-    if (!s->h_mat[flag - 1]) return fail(FDTD_ERR_OOM, "out of host memory");
-  }
-  memcpy(s->h_mat[flag - 1], values, (size_t)s->IJK * sizeof(float));
+  /* kept on the device as given; the copy is complete when this returns */
+  const size_t bytes = (size_t)s->IJK * sizeof(float);
+  int rc;
+  if (!s->d_raw[flag - 1] && (rc = dalloc(s, (void **)&s->d_raw[flag - 1], bytes))) return rc;
+  CU(cudaMemcpyAsync(s->d_raw[flag - 1], values, bytes, cudaMemcpyHostToDevice, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
   s->has_mat = 1;
   return FDTD_OK;
 }
@@ -820,17 +799,18 @@ static int upload_coefficients(sim *s) {
     dfree(d_shapes);
     KL(e);
   } else {
-    float *scratch = NULL;
-    if (s->Ip != s->I && pool_alloc((void **)&scratch, (size_t)s->IJK * sizeof(float),
-                                    s->stream) != cudaSuccess)
-      scratch = NULL; /* the slower host-side 2D copy instead */
-    for (int a = 0; a < 6 && !rc; ++a) {
-      if (s->h_mat[a]) rc = upload_pitched(s, s->d_ce[a], s->h_mat[a], scratch);
-      else if (fdtdk_fill_f32(s->d_ce[a], material_default(a), s->cells, s->stream))
-        rc = fail(FDTD_ERR_CUDA, "material default fill failed");
+    const size_t row = (size_t)s->I * sizeof(float);
+    for (int a = 0; a < 6; ++a) {
+      if (!s->d_raw[a]) {
+        KL(fdtdk_fill_f32(s->d_ce[a], material_default(a), s->cells, s->stream));
+      } else if (s->Ip == s->I) {
+        CU(cudaMemcpyAsync(s->d_ce[a], s->d_raw[a], (size_t)s->IJK * sizeof(float),
+                           cudaMemcpyDeviceToDevice, s->stream));
+      } else { /* packed rows to pitched rows */
+        CU(cudaMemcpy2DAsync(s->d_ce[a], (size_t)s->Ip * sizeof(float), s->d_raw[a], row, row,
+                             (size_t)s->J * s->K, cudaMemcpyDeviceToDevice, s->stream));
+      }
     }
-    dfree(scratch);
-    if (rc) return rc;
   }
   float *ce[6];
   const float *eps[3], *sig[3];
@@ -2031,8 +2011,10 @@ int fdtd_output_vis(fdtd_handle h, float *out, size_t n, int32_t flag) {
       }
       return FDTD_OK;
     }
-    if (s->h_mat[idx]) {
-      memcpy(out, s->h_mat[idx], cnt * sizeof(float));
+    if (s->d_raw[idx]) {
+      CU(cudaMemcpyAsync(out, s->d_raw[idx], cnt * sizeof(float), cudaMemcpyDeviceToHost,
+                         s->stream));
+      CU(cudaStreamSynchronize(s->stream));
     } else {
       const float v = material_default(idx);
       for (size_t n2 = 0; n2 < cnt; ++n2) out[n2] = v;
