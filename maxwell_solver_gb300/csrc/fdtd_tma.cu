@@ -2,7 +2,8 @@
  * fdtd_tma.cu -- persistent, warp-specialised TMA kernels of the two
  * half-steps for sm_103a.
  *
- * Work: the grid is cut into items of one 64 x 8 (x, y) tile and a run of
+ * Work: the grid is cut into items of one (x, y) tile -- 64 x 8 in the
+ * single-grid kernels, 32 x 16 in the batched ones -- and a run of
  * z-planes.  A launch is persistent (as many blocks as fit, at most one
  * per item): in every block one producer warp takes items from a global
  * atomic counter and streams every z-plane the item needs into a
@@ -14,11 +15,13 @@
  * the blocks busy to the end of the launch.  The producer that finishes
  * last rewinds the counter for the next launch.
  *
- *   E half-step, plane k: E tile (64x8) + H tile with the x-1 / y-1 halo
- *     (68x9, box origin (x0-4, y0-1): the x origin stays 16-byte aligned)
- *     + the material-id tile; Hx, Hy of plane k-1 are carried in registers.
- *   H half-step, plane k: E tile with the x+1 / y+1 halo (68x9 at (x0, y0))
- *     + H tile; Ex, Ey of plane k+1 come from the item's next load.
+ *   E half-step, plane k: E tile (BX x BY) + H tile with the x-1 / y-1
+ *     halo ((BX+4) x (BY+1), box origin (x0-4, y0-1): the x origin stays
+ *     16-byte aligned) + the material-id tile; Hx, Hy of plane k-1 are
+ *     carried in registers.
+ *   H half-step, plane k: E tile with the x+1 / y+1 halo ((BX+4) x (BY+1)
+ *     at (x0, y0)) + H tile; Ex, Ey of plane k+1 come from the item's next
+ *     load.
  *
  * Cells with no CPML, TF/SF face or source in their warp take a lean
  * curl-only path; the others go through fdtd_device.cuh's full per-cell
