@@ -495,16 +495,19 @@ __global__ void k_batch_faces_oblique(const fdtd_dev *devs, const fdtd_op *ops,
 
 // --------------------------------------------------------------- probes
 
-// Records the six components at every probe into row *probe_row (one thread
-// per probe and component); the row advances in k_add_i32 afterwards.
+// Records the six components at every probe into row *probe_row and
+// advances the row: one block, every thread reads the row before the
+// barrier, then thread 0 advances it (one launch per step).
 __global__ void k_probe_gather(const fdtd_dev d) {
   const int row = *d.probe_row;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (row < d.T && t < d.num_ant * 6) {
-    const int a = t / 6, c = t - a * 6;
-    const int64_t id = d.probe_idx[a];
-    d.probes[((int64_t)row * d.num_ant + a) * 6 + c] = id >= 0 ? d.f[c][id] : 0.f;
-  }
+  if (row < d.T)
+    for (int t = threadIdx.x; t < d.num_ant * 6; t += blockDim.x) {
+      const int a = t / 6, c = t - a * 6;
+      const int64_t id = d.probe_idx[a];
+      d.probes[((int64_t)row * d.num_ant + a) * 6 + c] = id >= 0 ? d.f[c][id] : 0.f;
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) *d.probe_row = row + 1;
 }
 
 // Batched probe gather: block g records grid g's probes into its current
@@ -1011,10 +1014,8 @@ int fdtdk_init_1d_oblique(int n1, int m_src, int mb, int w, int T, float cE, flo
 
 int fdtdk_probe_gather(const fdtd_dev *d, cudaStream_t s) {
   if (d->num_ant <= 0 || !d->probes) return 0;
-  const int nt = d->num_ant * 6;
-  k_probe_gather<<<(nt + 255) / 256, 256, 0, s>>>(*d);
-  k_add_i32<<<1, 1, 0, s>>>(d->probe_row, 1);
-  g_launches += 2;
+  k_probe_gather<<<1, 1024, 0, s>>>(*d);
+  ++g_launches;
   return (int)cudaGetLastError();
 }
 
