@@ -369,7 +369,10 @@ def run_e2e(w, K, simFDTD, materials, probe_locations, sources):
     simFDTD("DeleteSimulation", P)
     dt = time.perf_counter() - t0
     assert np.isfinite(ez).all() and np.isfinite(probes).all()
-    h2d = 2 * 6 * ijk * 4 + 2 * T * 4 + loc.size * 4
+    # host -> device: the six material arrays (UpdateMaterial copies each once;
+    # UpdateCuda recomputes from the device copies), the two waveforms, the
+    # probe locations
+    h2d = 6 * ijk * 4 + 2 * T * 4 + loc.size * 4
     d2h = ijk * 4 + probes.size * 4
     return {"value": round(ijk * K / dt / 1e6, 2), "unit": "Mcell-steps/s",
             "h2d_bytes_per_step": int(round(h2d / K)), "d2h_bytes_per_step": int(round(d2h / K)),
