@@ -2195,6 +2195,17 @@ int fdtd_create_signal(double fctr, double delT, double percentage_bw, double nu
 
 #define MAX_BATCHES 256
 
+/* FDTD_XSPLIT=0 keeps the batched E kernels' CPML X inline (the x-slab
+ * pass is the default) */
+static int xsplit_enabled(void) {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("FDTD_XSPLIT");
+    v = !(e && strcmp(e, "0") == 0);
+  }
+  return v;
+}
+
 /* z-planes per batched work item: 16, or FDTD_BATCH_ZRUN (1..64) */
 static int batch_zrun(void) {
   static int z = 0;
@@ -2500,7 +2511,7 @@ static int batch_rebuild(batch *b) {
       memcpy(op->cur_box, m->cur.box, sizeof(op->cur_box));
     }
     op->tfsf_split = fdtd_tfsf_split(&s->dev, op);
-    op->xsplit = fdtd_xsplit(&s->dev, op);
+    op->xsplit = xsplit_enabled() && fdtd_xsplit(&s->dev, op);
     if (op->xsplit) {
       const int64_t xc = 2 * (int64_t)s->p * s->J * s->K;
       if (xc > b->xs_max) b->xs_max = xc;
