@@ -330,7 +330,8 @@ typedef struct {
 
 typedef struct {
   uint64_t hbm_budget;    /* device bytes the admitted solves may hold at their
-                             peak (fdtd_estimate_device_bytes) */
+                             peak (fdtd_estimate_device_bytes); 0: 90 % of the
+                             device memory free when the server is created */
   int32_t max_active;     /* solves on the device at once (0: no limit) */
   int32_t round_steps;    /* most steps per batch round between admissions
                              (0: 32) */
@@ -369,6 +370,7 @@ typedef struct {
   double elapsed_s;             /* first submission to last completion */
   double latency_p50_s, latency_p90_s, latency_p99_s, latency_mean_s;
   double solves_per_s;          /* completed / elapsed_s */
+  uint64_t hbm_budget;          /* the budget in use */
 } fdtd_server_stats;
 
 int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg);

@@ -76,7 +76,7 @@ class FdtdServerStats(ctypes.Structure):
                 ("queued", I32), ("active", I32), ("elapsed_s", ctypes.c_double),
                 ("latency_p50_s", ctypes.c_double), ("latency_p90_s", ctypes.c_double),
                 ("latency_p99_s", ctypes.c_double), ("latency_mean_s", ctypes.c_double),
-                ("solves_per_s", ctypes.c_double)]
+                ("solves_per_s", ctypes.c_double), ("hbm_budget", ctypes.c_uint64)]
 
 
 class FdtdInfo(ctypes.Structure):

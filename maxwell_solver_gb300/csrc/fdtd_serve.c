@@ -461,6 +461,14 @@ int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg) {
   server *S = (server *)calloc(1, sizeof(server));
   if (!S) return FDTD_ERR_OOM;
   S->cfg = *cfg;
+  if (!S->cfg.hbm_budget) { /* admit by the device memory free now */
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      free(S);
+      return FDTD_ERR_CUDA;
+    }
+    S->cfg.hbm_budget = (uint64_t)((double)free_b * 0.9);
+  }
   clock_gettime(CLOCK_MONOTONIC, &S->t0);
   S->first_submit = -1.0;
   pthread_mutex_init(&S->mu, NULL);
@@ -672,6 +680,7 @@ int fdtd_server_get_stats(fdtd_server h, fdtd_server_stats *out) {
   out->peak_active = S->peak_active;
   out->queued = S->queued;
   out->active = S->active;
+  out->hbm_budget = S->cfg.hbm_budget;
   out->elapsed_s = S->first_submit >= 0 && S->last_finish > S->first_submit
                        ? S->last_finish - S->first_submit
                        : 0.0;

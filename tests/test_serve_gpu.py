@@ -184,3 +184,21 @@ def test_request_over_budget_fails_alone():
         assert srv.result(ts)["info"]["status"] == 0
         st = srv.stats()
     assert st["failed"] == 1 and st["completed"] == 1
+
+
+def test_budget_from_free_device_memory():
+    """hbm_budget 0: the server admits by the device memory free when it was
+    created (90 % of it)."""
+    import torch
+
+    from maxwell_solver_gb300.serve import Server
+
+    spec = _small_specs(1, seed=41)[0]
+    with Server(hbm_budget=0) as srv:
+        t = srv.submit(spec, n_probes=6)
+        res = srv.result(t)
+        st = srv.stats()
+    free, total = torch.cuda.mem_get_info()
+    assert 0 < st["hbm_budget"] <= total
+    assert st["hbm_budget"] >= 0.5 * free  # most of what is free now
+    assert res["info"]["status"] == 0 and st["completed"] == 1
