@@ -105,7 +105,11 @@ def test_mex_dispatcher_errors(mex):
                      ("SetConst", (np.float32([1, 2, 3]),)), ("Init1D", (np.float32([1]),)),
                      ("OutputVis", (np.uint32(8),)), ("CreateMu", ()),
                      ("UpdateMaterial", (np.int32(1),)), ("SetSource", ()),
-                     ("SetAntennaLocations", ()), ("OutputAnt", ())):
+                     ("SetAntennaLocations", ()), ("OutputAnt", ()),
+                     ("SetMagnetic", (np.float32([1]), np.float32([1]))),
+                     ("SetIncidence", ()), ("SetShapes", (np.float32([1, 0]),)),
+                     ("LoadCheckpoint", ()), ("LoadCheckpoint", (np.float32([1]),)),
+                     ("StepN", ())):
         with pytest.raises(MexError) as e:
             mex(op, bogus, *args)
         assert e.value.identifier == "simFDTD:InvalidInput", op
