@@ -44,12 +44,12 @@ def log(*a):
 # ----------------------------------------------------------------- ranks
 
 class Ranks:
-    def __init__(self):
+    def __init__(self, join: bool = True):
         self.rank = int(os.environ.get("RANK", "0"))
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = None
-        if self.world > 1:
+        if self.world > 1 and join:
             import torch.distributed as dist
 
             os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
@@ -152,11 +152,12 @@ def ncu_traffic(workload: str):
 def cpu_oracle_rate(w, target_s: float, max_steps: int, warmup: int = 3):
     """Times the FP32 oracle (OpenMP, all host threads) on the workload's grid
     for a bounded number of steps after `warmup` untimed ones; returns
-    (Mcell-steps/s, steps, seconds)."""
+    (Mcell-steps/s, steps, seconds, OpenMP threads used)."""
     import oracle
     from maxwell_solver_gb300.workloads import materials, probe_locations, sources
 
     oracle.build()
+    oracle.set_threads(os.cpu_count() or 1)  # torchrun sets OMP_NUM_THREADS=1
     T = max_steps + warmup + 1
     o = oracle.OracleSim("f32")
     o.set_params(pml=w.pml, tfsf_width=w.pml + 5)
@@ -183,7 +184,7 @@ def cpu_oracle_rate(w, target_s: float, max_steps: int, warmup: int = 3):
     dt = time.perf_counter() - t0
     steps = n - warmup
     o.close()
-    return w.cells * steps / dt / 1e6, steps, dt
+    return w.cells * steps / dt / 1e6, steps, dt, oracle.threads()
 
 
 def run_reference(args, ranks):
@@ -192,10 +193,9 @@ def run_reference(args, ranks):
     if ranks.rank != 0:
         return None
     w = WORKLOADS[args.workload]
-    cores = os.cpu_count()
     steps = max(1, min(args.steps, 200))
     warmup = max(3, args.warmup)
-    rate, done, secs = cpu_oracle_rate(w, target_s=10.0, max_steps=steps, warmup=warmup)
+    rate, done, secs, cores = cpu_oracle_rate(w, target_s=10.0, max_steps=steps, warmup=warmup)
     sample = (f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} grid of workload {w.name}, {done} FDTD "
               f"steps ({secs:.1f} s) of the FP32 CPU restatement, OpenMP {cores} threads")
     return {
@@ -293,11 +293,11 @@ def run_ours(args, ranks):
 
     cpu = None
     if ranks.rank == 0 and not args.no_cpu:
-        rate, done, secs = cpu_oracle_rate(w, target_s=args.cpu_seconds, max_steps=200)
-        cpu = {"value": round(rate, 3), "unit": "Mcell-steps/s", "cores": os.cpu_count(),
+        rate, done, secs, cores = cpu_oracle_rate(w, target_s=args.cpu_seconds, max_steps=200)
+        cpu = {"value": round(rate, 3), "unit": "Mcell-steps/s", "cores": cores,
                "kind": "port",
                "sample": f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} grid, {done} steps "
-                         f"({secs:.1f} s) of the FP32 oracle, OpenMP all host threads"}
+                         f"({secs:.1f} s) of the FP32 oracle, OpenMP {cores} threads"}
     ranks.close()
     if ranks.rank != 0:
         return None
@@ -555,7 +555,10 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    ranks = Ranks()
+    # the reference arm runs on rank 0 alone; the other ranks leave at once
+    # (a rank waiting in the process group would spin on a core the OpenMP
+    # oracle's threads need)
+    ranks = Ranks(join=args.impl != "reference")
     if args.batch_only:
         print(json.dumps({"batched": run_batched(args.batch_grids, batched_only=True)}), flush=True)
         return

@@ -76,6 +76,9 @@ def _load():
                 P = ctypes.c_void_p
                 f = lambda n: getattr(lib, f"ora_{sfx}_{n}")  # noqa: E731
                 f("create").restype = P
+                f("set_threads").argtypes = [ctypes.c_int]
+                f("set_threads").restype = None
+                f("threads").restype = ctypes.c_int
                 f("destroy").argtypes = [P]
                 f("set_params").argtypes = [P, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6
                 f("set_const").argtypes = [P, P, P]
@@ -108,6 +111,20 @@ def _load():
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_threads(n: int) -> int:
+    """Runs the oracle's OpenMP loops on n host threads; returns the count
+    in use."""
+    lib = _load()
+    lib.ora_f32_set_threads(int(n))
+    lib.ora_f64_set_threads(int(n))
+    return int(lib.ora_f32_threads())
+
+
+def threads() -> int:
+    """OpenMP threads the oracle's loops use."""
+    return int(_load().ora_f32_threads())
 
 
 class OracleSim:

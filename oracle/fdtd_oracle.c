@@ -33,6 +33,9 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #ifndef OR_REAL
 #define OR_REAL float
@@ -106,6 +109,22 @@ static void *xcalloc(size_t n, size_t sz) {
     abort();
   }
   return p;
+}
+
+/* OpenMP threads of the oracle's loops: set (n >= 1) and read back. */
+void OR(set_threads)(int n) {
+#ifdef _OPENMP
+  if (n >= 1) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int OR(threads)(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
 }
 
 or_sim *OR(create)(void) {
