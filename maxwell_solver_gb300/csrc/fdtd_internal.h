@@ -168,6 +168,13 @@ static inline int fdtd_xsplit(const fdtd_dev *d, const fdtd_op *op) {
   return 1;
 }
 
+/* The lean E curl kernel serves an op (tfsf_split and xsplit already set)
+ * whose TF/SF corrections run in the face pass or are absent, whose CPML X
+ * runs in the x-slab pass or is absent, and which has no current source. */
+static inline int fdtd_e_lean(const fdtd_op *op) {
+  return (!op->tfsf_mode || op->tfsf_split) && !op->cur_mode && (!op->pml || op->xsplit);
+}
+
 /* TF/SF mode 5: an oblique plane wave (fdtd_set_incidence), applied only as
  * face passes after the curl / CPML kernels, which needs the faces clear of
  * the CPML and the current source (fdtd_tfsf_faces_clear). */
@@ -217,11 +224,12 @@ size_t fdtdk_init_1d_smem_limit(void);
 /* Batched half-step over many grids (fdtd_tma.cu): table holds n_items
  * int4 {grid, x0, y0, kb | np << 16}; devs / maps (FDTD_NUM_MAPS x 128 B per
  * grid, 64-byte aligned) / ops / steps are per-grid device arrays; work is
- * a zeroed counter pair.  Every grid runs curl + CPML (+ its TF/SF mode and
+ * a zeroed counter pair; lean (E only) when fdtd_e_lean holds for every
+ * grid's op.  Every grid runs curl + CPML (+ its TF/SF mode and
  * current source) at step steps[g] + ops[g].step. */
-int fdtdk_batch_half(int hfam, const fdtd_dev *devs, const void *maps, const fdtd_op *ops,
-                     const int32_t *steps, const int32_t *table, int32_t n_items, int32_t *work,
-                     int32_t *err, cudaStream_t s);
+int fdtdk_batch_half(int hfam, int lean, const fdtd_dev *devs, const void *maps,
+                     const fdtd_op *ops, const int32_t *steps, const int32_t *table,
+                     int32_t n_items, int32_t *work, int32_t *err, cudaStream_t s);
 /* Probe rows of every grid of a batch, then +1 on each grid's probe row
  * and step (fdtd_kernels.cu). */
 int fdtdk_batch_probes(const fdtd_dev *devs, int32_t n, cudaStream_t s);

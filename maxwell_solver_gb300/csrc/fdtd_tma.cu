@@ -337,7 +337,11 @@ __device__ __forceinline__ void cell_map(int tid, int &xo, int &r0) {
 
 // ----------------------------------------------------------------- E half
 
-template <bool PML, bool BATCH>
+// LEAN: every grid the launch serves has its TF/SF corrections in the face
+// pass (or none), CPML X in the x-slab pass (or no CPML) and no current
+// source, so the consumer drops those per-cell paths (fewer registers and
+// branches; the cells it updates and their arithmetic are the same).
+template <bool PML, bool BATCH, bool LEAN = false>
 __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_E)
     k_half_e_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
@@ -438,8 +442,8 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
       kb = m.w;
       y0 = m1.z;
       i = m1.y + xo;
-      mode = op.tfsf_split ? 0 : op.tfsf_mode;  // split: the face pass applies it
-      cm = op.cur_mode;
+      mode = (LEAN || op.tfsf_split) ? 0 : op.tfsf_mode;  // split: the face pass applies it
+      cm = LEAN ? 0 : op.cur_mode;
       use_mat = d.coef_mode == 1;
       tab_local = BATCH ? (use_mat && d.n_mat <= kStageTabMax) : tab_in_smem;
       const int step = m1.w;
@@ -447,7 +451,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
       cur_src = cm ? d.src[step] : 0.f;
       const bool cur_x = cm && in_range(i, op.cur_box[0], op.cur_box[1]);
       // with xsplit the x-slab pass applies CPML X afterwards
-      const bool x_special = (PML && !op.xsplit && slab_e(i, I, d.p) >= 0) ||
+      const bool x_special = (PML && !LEAN && !op.xsplit && slab_e(i, I, d.p) >= 0) ||
                              (mode && (i == d.i0 || i == d.i1)) || i == 0;
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
@@ -500,7 +504,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
           const int j = y0 + ty;
           int px = -1, py = -1, pz = -1;
           if (PML) e_slabs(d, i, j, k, px, py, pz);
-          if (op.xsplit) px = -1;
+          if (LEAN || op.xsplit) px = -1;
           const bool cur = cur_col[c] && in_range(k, op.cur_box[4], op.cur_box[5]);
           update_e_cell<true, PML>(d, mode, inc, cm, cur_src, cur, i, j, k, px, py, pz, C, ex,
                                    ey, ez, hx, hy, hz, hz_jm, hx_jm, hz_im, hy_im, hx_km[c],
@@ -787,7 +791,7 @@ int encode(CUtensorMap *out, void *base, CUtensorMapDataType dt, int esize, cons
   return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
 }
 
-int g_blocks_e[2] = {0, 0}, g_blocks_h[4] = {0, 0, 0, 0}, g_blocks_b[2] = {0, 0};
+int g_blocks_e[4] = {0, 0, 0, 0}, g_blocks_h[4] = {0, 0, 0, 0}, g_blocks_b[3] = {0, 0, 0};
 
 // Resident blocks of a kernel on the current device (cached per kernel).
 template <class KH>
@@ -844,10 +848,18 @@ int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
   fdtd_op o = *op;
   o.tfsf_split = fdtd_tfsf_split(d, op);
   o.xsplit = fdtd_xsplit(d, op);
-  int e = o.pml ? launch(k_half_e_tma<true, false>, E_SMEM, &g_blocks_e[1], d, m, &o, s, d->I,
-                         d->J, d->K, d->zc_e)
-                : launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, &o, s,
-                         d->I, d->J, d->K, d->zc_e);
+  const int I = d->I, J = d->J, K = d->K;
+  int e;
+  if (fdtd_e_lean(&o))
+    e = o.pml ? launch(k_half_e_tma<true, false, true>, E_SMEM, &g_blocks_e[3], d, m, &o, s, I,
+                       J, K, d->zc_e)
+              : launch(k_half_e_tma<false, false, true>, E_SMEM, &g_blocks_e[2], d, m, &o, s, I,
+                       J, K, d->zc_e);
+  else
+    e = o.pml ? launch(k_half_e_tma<true, false>, E_SMEM, &g_blocks_e[1], d, m, &o, s, I, J, K,
+                       d->zc_e)
+              : launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, &o, s, I, J, K,
+                       d->zc_e);
   if (!e && o.xsplit) e = fdtdk_e_xslab(d, s);
   if (e || !o.tfsf_split) return e;
   return fdtdk_faces(0, d, &o, s);
@@ -872,9 +884,9 @@ int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
   return fdtdk_faces(1, d, &o, s);
 }
 
-int fdtdk_batch_half(int hfam, const fdtd_dev *devs, const void *maps, const fdtd_op *ops,
-                     const int32_t *steps, const int32_t *table, int32_t n_items, int32_t *work,
-                     int32_t *err, cudaStream_t s) {
+int fdtdk_batch_half(int hfam, int lean, const fdtd_dev *devs, const void *maps,
+                     const fdtd_op *ops, const int32_t *steps, const int32_t *table,
+                     int32_t n_items, int32_t *work, int32_t *err, cudaStream_t s) {
   if (n_items <= 0) return 0;
   Items it;
   memset(&it, 0, sizeof(it));
@@ -896,6 +908,11 @@ int fdtdk_batch_half(int hfam, const fdtd_dev *devs, const void *maps, const fdt
     if (e) return e;
     const int blocks = n_items < g_blocks_b[0] ? n_items : g_blocks_b[0];
     k_half_h_tma<true, true><<<blocks, NT, HG<true>::SMEM, s>>>(d0, op0, mp0, it);
+  } else if (lean) {
+    e = resident_blocks(k_half_e_tma<true, true, true>, EG<true>::SMEM, &g_blocks_b[2]);
+    if (e) return e;
+    const int blocks = n_items < g_blocks_b[2] ? n_items : g_blocks_b[2];
+    k_half_e_tma<true, true, true><<<blocks, NT, EG<true>::SMEM, s>>>(d0, op0, mp0, it);
   } else {
     e = resident_blocks(k_half_e_tma<true, true>, EG<true>::SMEM, &g_blocks_b[1]);
     if (e) return e;
