@@ -2246,6 +2246,7 @@ typedef struct batch {
   int32_t face_max; /* largest face-plane area of those members */
   int any_xsplit;   /* a member's E CPML X runs as the x-slab pass */
   int all_lean;     /* every member's E op satisfies fdtd_e_lean */
+  int all_lean_h;   /* every member's op satisfies fdtd_h_lean */
   int64_t xs_max;   /* the largest member's 2p*J*K */
 } batch;
 
@@ -2491,6 +2492,7 @@ static int batch_rebuild(batch *b) {
   b->face_max = 0;
   b->any_xsplit = 0;
   b->all_lean = 1;
+  b->all_lean_h = 1;
   b->xs_max = 0;
   int g = 0;
   nh = ne = 0;
@@ -2520,6 +2522,7 @@ static int batch_rebuild(batch *b) {
       b->any_xsplit = 1;
     }
     if (!fdtd_e_lean(op)) b->all_lean = 0;
+    if (!fdtd_h_lean(op)) b->all_lean_h = 0;
     if (op->tfsf_split) {
       const int32_t ax = s->I + 2, ay = s->J + 2, az = s->K + 2;
       int32_t f = ax * ay;
@@ -2589,7 +2592,7 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
   }
   for (int32_t t = 0; t < nsteps; ++t) {
     if (b->any_probes) KL(fdtdk_batch_probes(b->d_devs, b->n_act, b->stream));
-    KL(fdtdk_batch_half(1, 0, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_h,
+    KL(fdtdk_batch_half(1, b->all_lean_h, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_h,
                         b->n_h, b->d_work, b->d_err, b->stream));
     if (b->any_split)
       KL(fdtdk_batch_faces(1, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,

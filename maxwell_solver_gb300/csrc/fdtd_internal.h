@@ -175,6 +175,9 @@ static inline int fdtd_e_lean(const fdtd_op *op) {
   return (!op->tfsf_mode || op->tfsf_split) && !op->cur_mode && (!op->pml || op->xsplit);
 }
 
+/* The lean H curl kernel: TF/SF corrections in the face pass or absent. */
+static inline int fdtd_h_lean(const fdtd_op *op) { return !op->tfsf_mode || op->tfsf_split; }
+
 /* TF/SF mode 5: an oblique plane wave (fdtd_set_incidence), applied only as
  * face passes after the curl / CPML kernels, which needs the faces clear of
  * the CPML and the current source (fdtd_tfsf_faces_clear). */
@@ -224,8 +227,8 @@ size_t fdtdk_init_1d_smem_limit(void);
 /* Batched half-step over many grids (fdtd_tma.cu): table holds n_items
  * int4 {grid, x0, y0, kb | np << 16}; devs / maps (FDTD_NUM_MAPS x 128 B per
  * grid, 64-byte aligned) / ops / steps are per-grid device arrays; work is
- * a zeroed counter pair; lean (E only) when fdtd_e_lean holds for every
- * grid's op.  Every grid runs curl + CPML (+ its TF/SF mode and
+ * a zeroed counter pair; lean when fdtd_e_lean (E) or fdtd_h_lean (H)
+ * holds for every grid's op.  Every grid runs curl + CPML (+ its TF/SF mode and
  * current source) at step steps[g] + ops[g].step. */
 int fdtdk_batch_half(int hfam, int lean, const fdtd_dev *devs, const void *maps,
                      const fdtd_op *ops, const int32_t *steps, const int32_t *table,

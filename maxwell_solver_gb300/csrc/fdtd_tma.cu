@@ -532,7 +532,9 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
 
 // MU: per-cell H coefficients (fdtd_set_magnetic), read per cell from the
 // material ids and table (or the arrays); compiled for 3 blocks per SM.
-template <bool PML, bool BATCH, bool MU = false>
+// LEAN: every grid the launch serves has its TF/SF corrections in the face
+// pass (or none), so the consumer drops the inline TF/SF path.
+template <bool PML, bool BATCH, bool MU = false, bool LEAN = false>
 __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_MIN_BLOCKS_H))
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
@@ -611,7 +613,8 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
     const fdtd_op &op =
         BATCH ? *reinterpret_cast<const fdtd_op *>(st_item + G::H_STAGE + DESC_B) : op0;
     const int I = d.I, J = d.J, K = d.K, p = d.p;
-    const int mode = op.tfsf_split ? 0 : op.tfsf_mode;  // split: the face pass applies it
+    // split: the face pass applies it
+    const int mode = (LEAN || op.tfsf_split) ? 0 : op.tfsf_mode;
     const float *inc = mode ? inc_h_row(d, mode, m1.w) : nullptr;
     const float Chh = d.Chh, Che = d.Che;
     const int i = x0 + xo;
@@ -791,7 +794,8 @@ int encode(CUtensorMap *out, void *base, CUtensorMapDataType dt, int esize, cons
   return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
 }
 
-int g_blocks_e[4] = {0, 0, 0, 0}, g_blocks_h[4] = {0, 0, 0, 0}, g_blocks_b[3] = {0, 0, 0};
+int g_blocks_e[4] = {0, 0, 0, 0}, g_blocks_h[6] = {0, 0, 0, 0, 0, 0};
+int g_blocks_b[4] = {0, 0, 0, 0};
 
 // Resident blocks of a kernel on the current device (cached per kernel).
 template <class KH>
@@ -875,6 +879,11 @@ int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
                        nj, nk, d->zc_h)
               : launch(k_half_h_tma<false, false, true>, H_SMEM, &g_blocks_h[2], d, m, &o, s,
                        ni, nj, nk, d->zc_h);
+  else if (fdtd_h_lean(&o))
+    e = o.pml ? launch(k_half_h_tma<true, false, false, true>, H_SMEM, &g_blocks_h[5], d, m, &o,
+                       s, ni, nj, nk, d->zc_h)
+              : launch(k_half_h_tma<false, false, false, true>, H_SMEM, &g_blocks_h[4], d, m, &o,
+                       s, ni, nj, nk, d->zc_h);
   else
     e = o.pml ? launch(k_half_h_tma<true, false>, H_SMEM, &g_blocks_h[1], d, m, &o, s, ni, nj,
                        nk, d->zc_h)
@@ -903,7 +912,12 @@ int fdtdk_batch_half(int hfam, int lean, const fdtd_dev *devs, const void *maps,
   static fdtd_op op0;
   static Maps mp0;
   int e;
-  if (hfam) {
+  if (hfam && lean) {
+    e = resident_blocks(k_half_h_tma<true, true, false, true>, HG<true>::SMEM, &g_blocks_b[3]);
+    if (e) return e;
+    const int blocks = n_items < g_blocks_b[3] ? n_items : g_blocks_b[3];
+    k_half_h_tma<true, true, false, true><<<blocks, NT, HG<true>::SMEM, s>>>(d0, op0, mp0, it);
+  } else if (hfam) {
     e = resident_blocks(k_half_h_tma<true, true>, HG<true>::SMEM, &g_blocks_b[0]);
     if (e) return e;
     const int blocks = n_items < g_blocks_b[0] ? n_items : g_blocks_b[0];
