@@ -19,6 +19,7 @@
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "fdtd_device.cuh"
 #include "fdtd_internal.h"
@@ -957,11 +958,20 @@ int fdtdk_e_xslab(const fdtd_dev *d, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
+// Blocks per member of the batched x-slab and face passes (environment
+// FDTD_BATCH_XSLAB_BLOCKS, FDTD_BATCH_FACE_BLOCKS; read once).
+static int batch_blocks(const char *name, int def) {
+  const char *e = getenv(name);
+  const int v = e ? atoi(e) : def;
+  return v >= 1 && v <= 4096 ? v : def;
+}
+
 int fdtdk_batch_e_xslab(const fdtd_dev *devs, const fdtd_op *ops, int32_t n, int64_t max_cells,
                         cudaStream_t s) {
+  static const int cap = batch_blocks("FDTD_BATCH_XSLAB_BLOCKS", 64);
   if (n <= 0 || max_cells <= 0) return 0;
   int64_t bx = (max_cells + 255) / 256;
-  if (bx > 64) bx = 64;
+  if (bx > cap) bx = cap;
   k_batch_e_xslab<<<dim3((unsigned)bx, (unsigned)n), 256, 0, s>>>(devs, ops);
   ++g_launches;
   return (int)cudaGetLastError();
@@ -969,9 +979,10 @@ int fdtdk_batch_e_xslab(const fdtd_dev *devs, const fdtd_op *ops, int32_t n, int
 
 int fdtdk_batch_faces(int hfam, const fdtd_dev *devs, const fdtd_op *ops, const int32_t *steps,
                       int32_t n, int32_t max_cells_per_face, cudaStream_t s) {
+  static const int cap = batch_blocks("FDTD_BATCH_FACE_BLOCKS", 4);
   if (n <= 0) return 0;
   int bx = (max_cells_per_face + 255) / 256;
-  if (bx > 4) bx = 4;
+  if (bx > cap) bx = cap;
   const dim3 grid(bx > 0 ? bx : 1, 4, (unsigned)n);
   if (hfam) k_batch_faces<true><<<grid, 256, 0, s>>>(devs, ops, steps);
   else k_batch_faces<false><<<grid, 256, 0, s>>>(devs, ops, steps);
@@ -979,17 +990,13 @@ int fdtdk_batch_faces(int hfam, const fdtd_dev *devs, const fdtd_op *ops, const 
   return (int)cudaGetLastError();
 }
 
-// blocks per face plane and member of the batched oblique face pass
-#ifndef FDTD_BATCH_FACE_BLOCKS
-#define FDTD_BATCH_FACE_BLOCKS 4
-#endif
-
 int fdtdk_batch_faces_oblique(int hfam, const fdtd_dev *devs, const fdtd_op *ops,
                               const int32_t *steps, int32_t n, int32_t max_cells_per_face,
                               cudaStream_t s) {
+  static const int cap = batch_blocks("FDTD_BATCH_FACE_BLOCKS", 4);
   if (n <= 0) return 0;
   int bx = (max_cells_per_face + 255) / 256;
-  bx = bx < 1 ? 1 : (bx > FDTD_BATCH_FACE_BLOCKS ? FDTD_BATCH_FACE_BLOCKS : bx);
+  bx = bx < 1 ? 1 : (bx > cap ? cap : bx);
   if (hfam) k_batch_faces_oblique<true><<<dim3(bx, 12, n), 256, 0, s>>>(devs, ops, steps);
   else k_batch_faces_oblique<false><<<dim3(bx, 12, n), 256, 0, s>>>(devs, ops, steps);
   ++g_launches;
