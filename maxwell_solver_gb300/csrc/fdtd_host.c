@@ -2248,6 +2248,9 @@ typedef struct batch {
   int all_lean;     /* every member's E op satisfies fdtd_e_lean */
   int all_lean_h;   /* every member's op satisfies fdtd_h_lean */
   int64_t xs_max;   /* the largest member's 2p*J*K */
+  /* GRAPH_CHUNK steps of the active set, captured after each rebuild */
+  cudaGraphExec_t gexec;
+  unsigned long long g_kernels;
 } batch;
 
 static batch *g_batches[MAX_BATCHES];
@@ -2333,6 +2336,7 @@ int fdtd_batch_destroy(fdtd_batch h) {
   g_batches[slot - 1] = NULL;
   pthread_mutex_unlock(&g_reg_lock);
   cudaStreamSynchronize(b->stream);
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
   batch_free_mirrors(b);
   dfree_on(b->stream, b->d_work);
   dfree_on(b->stream, b->d_err);
@@ -2562,6 +2566,32 @@ static int batch_rebuild(batch *b) {
   return FDTD_OK;
 }
 
+/* One step of every active member: the probe rows, H (+ faces), E (+ x-slab
+ * pass, faces) and the step counters. */
+static int batch_step_ops(batch *b) {
+  if (b->any_probes) KL(fdtdk_batch_probes(b->d_devs, b->n_act, b->stream));
+  KL(fdtdk_batch_half(1, b->all_lean_h, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_h,
+                      b->n_h, b->d_work, b->d_err, b->stream));
+  if (b->any_split)
+    KL(fdtdk_batch_faces(1, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
+                         b->stream));
+  if (b->any_oblique)
+    KL(fdtdk_batch_faces_oblique(1, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
+                                 b->stream));
+  KL(fdtdk_batch_half(0, b->all_lean, b->d_devs, b->d_maps, b->d_ops, b->d_steps,
+                      b->d_tab_e, b->n_e, b->d_work + 2, b->d_err, b->stream));
+  if (b->any_xsplit)
+    KL(fdtdk_batch_e_xslab(b->d_devs, b->d_ops, b->n_act, b->xs_max, b->stream));
+  if (b->any_split)
+    KL(fdtdk_batch_faces(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
+                         b->stream));
+  if (b->any_oblique)
+    KL(fdtdk_batch_faces_oblique(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
+                                 b->stream));
+  KL(fdtdk_batch_advance(b->d_steps, b->n_act, b->stream));
+  return FDTD_OK;
+}
+
 /* Advances every active member by up to max_steps steps (all by the same
  * number: the fewest remaining steps of any active member, capped by
  * max_steps).  *active_left receives the number of members still running. */
@@ -2583,6 +2613,10 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
       CU(cudaEventRecord(s->ev[15], s->stream));
       CU(cudaStreamWaitEvent(b->stream, s->ev[15], 0));
     }
+    if (b->gexec) { /* the mirrors and item tables change */
+      cudaGraphExecDestroy(b->gexec);
+      b->gexec = NULL;
+    }
     if ((rc = batch_rebuild(b))) return rc;
   }
   int32_t nsteps = max_steps;
@@ -2590,28 +2624,33 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
     const bmember *m = &b->m[b->act[g]];
     if (m->count - m->done < nsteps) nsteps = m->count - m->done;
   }
-  for (int32_t t = 0; t < nsteps; ++t) {
-    if (b->any_probes) KL(fdtdk_batch_probes(b->d_devs, b->n_act, b->stream));
-    KL(fdtdk_batch_half(1, b->all_lean_h, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_h,
-                        b->n_h, b->d_work, b->d_err, b->stream));
-    if (b->any_split)
-      KL(fdtdk_batch_faces(1, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
-                           b->stream));
-    if (b->any_oblique)
-      KL(fdtdk_batch_faces_oblique(1, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
-                                   b->stream));
-    KL(fdtdk_batch_half(0, b->all_lean, b->d_devs, b->d_maps, b->d_ops, b->d_steps,
-                        b->d_tab_e, b->n_e, b->d_work + 2, b->d_err, b->stream));
-    if (b->any_xsplit)
-      KL(fdtdk_batch_e_xslab(b->d_devs, b->d_ops, b->n_act, b->xs_max, b->stream));
-    if (b->any_split)
-      KL(fdtdk_batch_faces(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
-                           b->stream));
-    if (b->any_oblique)
-      KL(fdtdk_batch_faces_oblique(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,
-                                   b->stream));
-    KL(fdtdk_batch_advance(b->d_steps, b->n_act, b->stream));
+  int32_t t = 0;
+  if (nsteps >= GRAPH_CHUNK) {
+    if (!b->gexec) {
+      cudaGraph_t g;
+      const unsigned long long before = fdtdk_launch_count();
+      CU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      int crc = FDTD_OK;
+      for (int c = 0; c < GRAPH_CHUNK && !crc; ++c) crc = batch_step_ops(b);
+      cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+      if (crc) return crc;
+      if (ce != cudaSuccess) return fail(FDTD_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&b->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) {
+        b->gexec = NULL;
+        return fail(FDTD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+      }
+      b->g_kernels = fdtdk_launch_count() - before;
+      g_captured_kernels += b->g_kernels;
+    }
+    for (; nsteps - t >= GRAPH_CHUNK; t += GRAPH_CHUNK) {
+      CU(cudaGraphLaunch(b->gexec, b->stream));
+      g_graph_kernels += b->g_kernels;
+    }
   }
+  for (; t < nsteps; ++t)
+    if ((rc = batch_step_ops(b))) return rc;
   int finished = 0;
   for (int g = 0; g < b->n_act; ++g) {
     bmember *m = &b->m[b->act[g]];
