@@ -280,11 +280,13 @@ __device__ __forceinline__ void decode_item(const Items &it, int w, int &g, int 
 // Stage metadata, written by the producer before it arms the stage:
 // meta[2s] = {item, plane of the item, planes, first plane},
 // meta[2s+1] = {grid, x0, y0, absolute step of the grid's op}.
-// Producer side of one launch (lane 0 of the producer warp).  `extra` more
-// loads follow each item's np planes (the H half-step reads plane k+1).
+// Producer side of one launch (lane 0 of the producer warp).  Up: the
+// item's np planes from kb.  DOWN: `extra` more planes above the item come
+// first (the H half-step reads plane k+1), then the item's planes from the
+// top down; issue() is told which loads are such extra planes.
 // Ends with a sentinel stage, rewinds the work counter when it is the last
 // producer, and waits for its own copies before returning.
-template <int NS, bool BATCH, class StepFn, class IssueFn>
+template <int NS, bool BATCH, bool DOWN, class StepFn, class IssueFn>
 __device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *empty, int4 *meta,
                         StepFn step_of, IssueFn issue) {
   int q = 0;
@@ -301,7 +303,10 @@ __device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *em
       if (!ok) break;
       meta[2 * s] = make_int4(w, t, np, kb);
       meta[2 * s + 1] = make_int4(g, x0, y0, step);
-      issue(s, g, x0, y0, kb + t);
+      if (DOWN)
+        issue(s, g, x0, y0, kb + np + extra - 1 - t, t < extra);
+      else
+        issue(s, g, x0, y0, kb + t, false);
     }
     if (!ok) break;
   }
@@ -377,8 +382,8 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
       const auto step_of = [&](int g) {
         return (BATCH ? it.steps[g] + it.ops[g].step : op_step(d0, op0));
       };
-      produce<NS, BATCH>(it, 0, full, empty, meta, step_of, [&](int s, int g, int x0, int y0,
-                                                                  int k) {
+      produce<NS, BATCH, false>(it, 0, full, empty, meta, step_of, [&](int s, int g, int x0,
+                                                                         int y0, int k, bool) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
         if (BATCH && g != g_um) {
           g_um = g;
@@ -571,21 +576,26 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
       const auto step_of = [&](int g) {
         return (BATCH ? it.steps[g] + it.ops[g].step : op_step(d0, op0));
       };
-      produce<NS, BATCH>(it, 1, full, empty, meta, step_of, [&](int s, int g, int x0, int y0,
-                                                                 int k) {
+      // planes from the top down; the item's first load is plane kb + np,
+      // of which the consumers read Ex and Ey of their own cells
+      produce<NS, BATCH, true>(it, 1, full, empty, meta, step_of, [&](int s, int g, int x0,
+                                                                       int y0, int k,
+                                                                       bool above) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
         unsigned char *st = smem + s * ST;
         proxy_fence();
-        mbar_expect_tx(&full[s], tx_bytes + (BATCH ? (uint32_t)(sizeof(fdtd_dev) +
-                                                                sizeof(fdtd_op)) : 0u));
+        mbar_expect_tx(&full[s], (above ? 2 * G::HALO_B : tx_bytes) +
+                                     (BATCH ? (uint32_t)(sizeof(fdtd_dev) + sizeof(fdtd_op))
+                                            : 0u));
         if (BATCH) {
           bulk_g2s(st + G::H_STAGE, &it.devs[g], sizeof(fdtd_dev), &full[s]);
           bulk_g2s(st + G::H_STAGE + DESC_B, &it.ops[g], sizeof(fdtd_op), &full[s]);
         }
-        for (int c = 0; c < 3; ++c)
+        for (int c = 0; c < (above ? 2 : 3); ++c)
           tma_load_3d(st + c * G::HALO_SLOT, &mm[6 + c], &full[s], x0, y0, k);
-        for (int c = 0; c < 3; ++c)
-          tma_load_3d(st + G::H_OFF_H + c * G::TILE_B, &mm[9 + c], &full[s], x0, y0, k);
+        if (!above)
+          for (int c = 0; c < 3; ++c)
+            tma_load_3d(st + G::H_OFF_H + c * G::TILE_B, &mm[9 + c], &full[s], x0, y0, k);
       });
     }
     return;
@@ -631,25 +641,37 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
       col_face[c] = x_face || (mode && (j == d.j0 - 1 || j == d.j1));
       n0[c] = valid[c] ? i + (int64_t)j * d.Ip + (int64_t)kb * d.plane : 0;
     }
-    int prev = s;
+    // the item's first load is plane kb + np: Ex, Ey of the own cells, the
+    // upper ends of plane kb + np - 1's z differences; then the planes from
+    // the top down, each carrying its own Ex, Ey to the plane below
+    float ex1[2], ey1[2];
+    {
+      const float *sEx = reinterpret_cast<const float *>(st_item);
+      const float *sEy = sEx + G::HALO_SLOT / 4;
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int eb = (r0 + (G::BY / 2) * c) * G::HW + xo;
+        ex1[c] = sEx[eb];
+        ey1[c] = sEy[eb];
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
     ++q;
-    for (int t = 0; t < np; ++t, ++q) {
+    for (int t = np - 1; t >= 0; --t, ++q) {
       s = q % NS;
       if (!mbar_wait(&full[s], (uint32_t)((q / NS) & 1))) {
         if (it.err) atomicExch(it.err, 2);
         return;
       }
       const int k = kb + t;
-      const unsigned char *st0 = smem + prev * ST;
-      // descriptor of the stage in use (the item's first stage may already
-      // have been handed back to the producer)
+      const unsigned char *st0 = smem + s * ST;
+      // descriptor of the stage in use (the item's first stage has been
+      // handed back to the producer)
       const fdtd_dev &dp = BATCH ? *reinterpret_cast<const fdtd_dev *>(st0 + G::H_STAGE) : d0;
-      const unsigned char *st1 = smem + s * ST;
       const float *sEx = reinterpret_cast<const float *>(st0);
       const float *sEy = sEx + G::HALO_SLOT / 4;
       const float *sEz = sEy + G::HALO_SLOT / 4;
-      const float *sEx1 = reinterpret_cast<const float *>(st1);
-      const float *sEy1 = sEx1 + G::HALO_SLOT / 4;
       const float *sHx = reinterpret_cast<const float *>(st0 + G::H_OFF_H);
       const float *sHy = sHx + G::BX * G::BY;
       const float *sHz = sHy + G::BX * G::BY;
@@ -665,7 +687,9 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
         const float ex = sEx[eb], ey = sEy[eb], ez = sEz[eb];
         const float dEz_y = sEz[eb + G::HW] - ez, dEx_y = sEx[eb + G::HW] - ex;
         const float dEz_x = sEz[eb + 1] - ez, dEy_x = sEy[eb + 1] - ey;
-        const float dEy_z = sEy1[eb] - ey, dEx_z = sEx1[eb] - ex;
+        const float dEy_z = ey1[c] - ey, dEx_z = ex1[c] - ex;
+        ex1[c] = ex;
+        ey1[c] = ey;
         float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
         // lean path (curl, then at most one CPML axis) unless a cell is on
         // a TF/SF face or in two slabs
@@ -708,11 +732,8 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
         }
       }
       __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[prev]);
-      prev = s;
+      if (lane == 0) mbar_arrive(&empty[s]);
     }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[prev]);  // the item's extra plane
   }
 }
 
