@@ -20,8 +20,9 @@
  *     16-byte aligned) + the material-id tile; Hx, Hy of plane k-1 are
  *     carried in registers.
  *   H half-step, plane k: E tile with the x+1 / y+1 halo ((BX+4) x (BY+1)
- *     at (x0, y0)) + H tile; Ex, Ey of plane k+1 come from the item's next
- *     load.
+ *     at (x0, y0)) + H tile.  Items march down in z: their first load is
+ *     plane kb + np (Ex, Ey only), and Ex, Ey of plane k+1 are carried in
+ *     registers.
  *
  * Cells with no CPML, TF/SF face or source in their warp take a lean
  * curl-only path; the others go through fdtd_device.cuh's full per-cell
