@@ -517,11 +517,13 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4):
         arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
         served, p_s = one_run(arrivals, False)
         hrrn, p_h = one_run(arrivals, False, "hrrn")
+        bounded, p_b = one_run(arrivals, False, "bounded")
         plain, p_p = one_run(arrivals, True)
         same &= all(np.array_equal(a, b) for a, b in zip(p_s, p_p))
         same &= all(np.array_equal(a, b) for a, b in zip(p_h, p_p))
+        same &= all(np.array_equal(a, b) for a, b in zip(p_b, p_p))
         points.append({"load": load, "rate_per_s": round(rate, 3), "served": served,
-                       "served_hrrn": hrrn, "one_at_a_time": plain,
+                       "served_hrrn": hrrn, "served_bounded": bounded, "one_at_a_time": plain,
                        "speedup_solves_per_s": round(served["solves_per_s"] /
                                                      max(plain["solves_per_s"], 1e-9), 2),
                        "p99_ratio_one_at_a_time_over_served": round(
@@ -537,7 +539,8 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4):
                   "(set-up on the device, all steps, probe readout); capacity = every request "
                   "queued at t=0 through the batched server",
         "policies": "served: least remaining work first; served_hrrn: highest response "
-                    "ratio (waited + remaining) / remaining first",
+                    "ratio (waited + remaining) / remaining first; served_bounded: least "
+                    "remaining work first, requests whose response ratio reached 3 ahead",
     }
 
 

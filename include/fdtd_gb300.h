@@ -347,10 +347,15 @@ typedef struct {
                              FDTD_SERVE_SRPT (0): least remaining work first;
                              FDTD_SERVE_HRRN (1): highest response ratio
                              (waited + remaining) / remaining first, which
-                             bounds how long a large request waits */
+                             bounds how long a large request waits;
+                             FDTD_SERVE_BOUNDED (2): least remaining work
+                             first, except that requests whose response
+                             ratio reached 3 go ahead of the others, highest
+                             ratio first */
 } fdtd_server_config;
 #define FDTD_SERVE_SRPT 0
 #define FDTD_SERVE_HRRN 1
+#define FDTD_SERVE_BOUNDED 2
 
 typedef struct {
   double submit_s, admit_s, finish_s; /* server clock, seconds */

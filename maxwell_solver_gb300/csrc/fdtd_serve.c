@@ -245,24 +245,38 @@ static int by_key(const void *a, const void *b) {
 /* Approximate cell-steps per second of one GB300 on these kernels: the
  * scale between waiting time and remaining work in the response ratio. */
 #define SERVE_RATE_EST 3.0e10
+/* FDTD_SERVE_BOUNDED: the response ratio at which a request goes ahead
+ * (3, or FDTD_SERVE_MAX_RATIO > 1; read once) */
+static double serve_max_ratio(void) {
+  static double v = 0.0;
+  if (v <= 0.0) {
+    const char *e = getenv("FDTD_SERVE_MAX_RATIO");
+    const double x = e ? atof(e) : 0.0;
+    v = x > 1.0 ? x : 3.0;
+  }
+  return v;
+}
 
 static void order_requests(server *S, int policy) {
   const double now = now_s(S);
   for (int a = 0; a < S->n_act; ++a) {
     req *r = S->act[a];
     const double work = (double)req_cells(r) * (r->r.steps - r->done);
-    if (policy == FDTD_SERVE_HRRN) {
-      const double rem = work / SERVE_RATE_EST + 1e-6;
-      r->key = -((now - r->t_submit) + rem) / rem;
-    } else {
+    const double rem = work / SERVE_RATE_EST + 1e-6;
+    const double ratio = ((now - r->t_submit) + rem) / rem;
+    if (policy == FDTD_SERVE_HRRN)
+      r->key = -ratio;
+    else if (policy == FDTD_SERVE_BOUNDED && ratio >= serve_max_ratio())
+      r->key = -ratio; /* ahead of every key >= 0 below */
+    else
       r->key = work;
-    }
   }
   qsort(S->act, (size_t)S->n_act, sizeof(req *), by_key);
 }
 
-/* This round's members, in the policy's order (least remaining work, or
- * highest response ratio).  When the first
+/* This round's members, in the policy's order (least remaining work,
+ * highest response ratio, or least remaining work with the requests past
+ * the ratio bound first).  When the first
  * request has at least `solo` cells it runs alone (*solo, through
  * fdtd_step_n, whose kernels are tuned to its shape); otherwise the smaller
  * requests are taken in order until their cells reach `fill`, and the large
@@ -456,7 +470,8 @@ static void release_gpu(server *S) {
 
 int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg) {
   if (!out || !cfg) return FDTD_ERR_INVALID_ARG;
-  if (cfg->policy != FDTD_SERVE_SRPT && cfg->policy != FDTD_SERVE_HRRN)
+  if (cfg->policy != FDTD_SERVE_SRPT && cfg->policy != FDTD_SERVE_HRRN &&
+      cfg->policy != FDTD_SERVE_BOUNDED)
     return FDTD_ERR_INVALID_ARG;
   server *S = (server *)calloc(1, sizeof(server));
   if (!S) return FDTD_ERR_OOM;
