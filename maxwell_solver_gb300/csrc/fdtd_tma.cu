@@ -632,6 +632,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
     const int px = PML ? slab_h(i, I, p) : -1;
     const bool x_face = mode && (i == d.i0 - 1 || i == d.i1);
     bool valid[2], col_face[2];  // col_face: a TF/SF face cell (not split off)
+    bool ax[2];                  // a cell of the warp row is in an x slab
     int py[2];
     int64_t n0[2];
 #pragma unroll
@@ -641,6 +642,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
       py[c] = PML ? slab_h(j, J, p) : -1;
       col_face[c] = x_face || (mode && (j == d.j0 - 1 || j == d.j1));
       n0[c] = valid[c] ? i + (int64_t)j * d.Ip + (int64_t)kb * d.plane : 0;
+      ax[c] = PML && __any_sync(0xffffffffu, valid[c] && px >= 0);
     }
     // the item's first load is plane kb + np: Ex, Ey of the own cells, the
     // upper ends of plane kb + np - 1's z differences; then the planes from
@@ -694,12 +696,11 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
         float hx = sHx[hb], hy = sHy[hb], hz = sHz[hb];
         // lean path (curl, then at most one CPML axis) unless a cell is on
         // a TF/SF face or in two slabs
-        const bool oth = __any_sync(0xffffffffu, act && (col_face[c] || plane_face));
-        const bool ax = PML && __any_sync(0xffffffffu, act && px >= 0);
+        const bool oth = !LEAN && __any_sync(0xffffffffu, act && (col_face[c] || plane_face));
         const bool ay = PML && py[c] >= 0, az = PML && pz >= 0;
         const int j = y0 + ty;
         const HCoef C = MU ? hcoef_at(dp, act ? n0[c] + off : 0) : HCoef{Chh, Chh, Chh, Che, Che, Che};
-        if (oth || (int)ax + (int)ay + (int)az > 1) {
+        if (oth || (int)ax[c] + (int)ay + (int)az > 1) {
           if (act) {
             update_h_cell<true, PML>(dp, C, mode, inc, i, j, k, px, py[c], pz,
                                      hx, hy, hz, dEz_y, dEx_y, dEz_x, dEy_x, dEy_z, dEx_z,
@@ -710,7 +711,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
           hy = C.hhy * hy + C.hey * (-dEx_z + dEz_x);
           hz = C.hhz * hz + C.hez * (-dEy_x + dEx_y);
           if (PML && act) {
-            if (ax) {
+            if (ax[c]) {
               if (px >= 0) {
                 float2 *X = psi_at_x(dp, PSI_HX, px, j, k);
                 const float xb = BATCH ? dp.bH[px] : s_xbc[0][px];
