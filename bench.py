@@ -3,10 +3,10 @@
 
 One bench step = one FDTD time step (H and E half-steps with CPML, TF/SF
 plane wave and probe recording) over the whole grid of the workload.
-Default workload: the 256^3 single-grid scattering configuration (c2: 12-cell
-CPML, 40 dielectric/lossy spheres, TF/SF plane wave, 64 probes), synthetic
-seeded inputs; the fields and coefficients (~0.8 GB) exceed the 129 MB L2, so
-no L2 flush is needed between steps.
+Default workload: the 512x512x448 layered-earth configuration (c3: 16-cell
+CPML, 6 conductive layers below air, vertically incident TF/SF plane wave,
+256-cell surface probe line), synthetic seeded inputs; the state (~3.4 GB)
+exceeds the 129 MB L2, so no L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1|c2|c3]
   python bench.py --impl reference ...   # the CPU arm (oracle, all cores)
@@ -31,9 +31,14 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-ALG_BYTES_STEP = 96   # per cell-step: H half 9 x 4 B, E half 15 x 4 B
-ALG_BYTES_E = 60      # E half-step: read 3 E + 3 H + 6 coefficients, write 3 E
-ALG_BYTES_H = 36      # H half-step: read 3 H + 3 E, write 3 H
+# Algorithmic bytes per cell.  The reference's layout (per-cell coefficient
+# arrays): H half-step read 3 H + 3 E, write 3 H = 36 B; E half-step read
+# 3 E + 3 H + 6 coefficients, write 3 E = 60 B; 96 B per step.
+REF_BYTES_H, REF_BYTES_E = 36, 60
+# Compulsory bytes of this design: the E coefficients are a 2-byte material
+# id per cell (a table of the distinct tuples in shared memory) when the grid
+# has at most 32768 distinct tuples, else the six arrays; H as above.
+ID_BYTES_E = 38
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -135,16 +140,16 @@ def measured_hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic(workload: str):
-    """DRAM bytes per launch of the E half-step kernel from the committed
-    ncu summary (profiles/ncu_traffic.json), scaled to this workload."""
+def ncu_traffic(workload: str) -> dict:
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    of this workload's kernels from the committed ncu summary
+    (profiles/ncu_traffic.json)."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
-            d = json.load(f)
-        return d.get(workload, {}).get("k_half_e_bytes_per_launch")
+            return json.load(f).get(workload, {})
     except (OSError, ValueError):
-        return None
+        return {}
 
 
 # ----------------------------------------------------------------- CPU arm
@@ -203,7 +208,7 @@ def run_reference(args, ranks):
         "unit": "Mcell-steps/s", "n_gpus": args.gpus, "steps": done, "warmup": warmup,
         "ms_per_step": round(secs / done * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(w),
+        "config": {**workload_config(w), "parallelism": f"replicas x{args.gpus}"},
         "cpu_baseline": {"value": round(rate, 3), "unit": "Mcell-steps/s", "cores": cores,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(rate, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
@@ -227,18 +232,41 @@ def workload_config(w):
 # ----------------------------------------------------------------- GPU arm
 
 def run_ours(args, ranks):
-    from maxwell_solver_gb300 import _native, launch_count, simFDTD
+    import ctypes
+    import tempfile
+
+    from maxwell_solver_gb300 import _native, info, launch_count, simFDTD
     from maxwell_solver_gb300.simfdtd import _check
     from maxwell_solver_gb300.workloads import WORKLOADS, materials, probe_locations, setup, sources
 
+    # a fresh autotune cache: the end-to-end leg, which runs first, pays the
+    # autotuner's trial steps as a first drop-in call on this machine would
+    tune_dir = tempfile.mkdtemp(prefix="fdtd_tune_")
+    os.environ["FDTD_TUNE_CACHE"] = os.path.join(tune_dir, "autotune.txt")
     lib = _native.load()
     _check(lib.fdtd_set_device(ranks.local))
     w = WORKLOADS[args.workload]
     W, K = args.warmup, args.steps
+    cells = w.cells
+
+    # end to end through the public per-op interface (host buffers, H2D of
+    # materials and sources, D2H of probes and a field, all inside the timing)
+    # (every rank runs its replica's; the whole job's rate is the cell-steps
+    # of all ranks over the slowest rank's time)
+    e2e = None
+    if not args.no_e2e:
+        e2e_steps = args.e2e_steps or w.steps
+        ranks.barrier()
+        e2e = run_e2e(w, e2e_steps, simFDTD, materials, probe_locations, sources)
+        slowest = ranks.max(e2e["seconds"])
+        e2e["value"] = round(cells * e2e_steps * ranks.world / slowest / 1e6, 2)
+        e2e["seconds"] = round(slowest, 3)
+
     KP = max(8, min(64, K // 4))  # per-kernel profiled steps
     T = W + K + KP
     P = setup(simFDTD, w, steps=T)
     h = int(P[0])
+    inf = info(P)
     simFDTD("Synchronize", P)
 
     simFDTD("StepN", P, np.int32([0, W, w.mode]))
@@ -260,45 +288,64 @@ def run_ours(args, ranks):
     ranks.barrier()
     ms_max = ranks.max(ms.value)
 
-    # per-kernel device time, measured live with CUDA events around every launch
-    import ctypes
-
-    acc = (ctypes.c_float * 3)()
+    # per-kernel device time, measured live with CUDA events around every
+    # launch (on the handle's stream, where the kernels run)
+    acc = (ctypes.c_float * 6)()
     _check(lib.fdtd_profile_steps(h, W + K, KP, w.mode, None, ctypes.byref(acc)))
-    t_h, t_e, t_o = acc[0] / KP, acc[1] / KP, acc[2] / KP
+    t_h, t_e, t_o, t_hc, t_ec = (acc[i] / KP for i in range(5))
     simFDTD("DeleteSimulation", P)
 
     peak, peak_kind = measured_hbm_peak()
-    cells = w.cells
     value = cells * K * ranks.world / (ms_max / 1e3) / 1e6
-    ach_e = ALG_BYTES_E * cells / (t_e / 1e3) / 1e9
-    ach_h = ALG_BYTES_H * cells / (t_h / 1e3) / 1e9
-    ach_step = ALG_BYTES_STEP * cells * K / (ms.value / 1e3) / 1e9
-    traffic = ncu_traffic(w.name)
-
-    # end to end through the public per-op interface (host buffers, H2D of
-    # materials and sources, D2H of probes and a field, all inside the timing)
-    # (every rank runs its replica's; the whole job's rate is the cell-steps
-    # of all ranks over the slowest rank's time)
-    e2e = None
-    if not args.no_e2e:
-        ranks.barrier()
-        e2e = run_e2e(w, K, simFDTD, materials, probe_locations, sources)
-        slowest = ranks.max(e2e["seconds"])
-        e2e["value"] = round(cells * K * ranks.world / slowest / 1e6, 2)
-        e2e["seconds"] = round(slowest, 3)
+    step_ms = ms.value / K
+    e_bytes = ID_BYTES_E if inf["coef_mode"] == 1 else REF_BYTES_E
+    gbs = lambda b, t_ms: b * cells / (t_ms / 1e3) / 1e9  # noqa: E731
+    tr = ncu_traffic(w.name)
+    tr_e, tr_h = tr.get("k_half_e_bytes_per_launch"), tr.get("k_half_h_bytes_per_launch")
+    kern = {
+        "E": {"kernel": "k_half_e_tma (E curl + CPML Y, Z)", "alg_bytes_per_cell": e_bytes,
+              "avg_launch_ms": round(t_ec, 5), "achieved": round(gbs(e_bytes, t_ec), 1),
+              "frac": round(gbs(e_bytes, t_ec) / peak, 4), "traffic": tr_e,
+              "half_step_ms": round(t_e, 5)},
+        "H": {"kernel": "k_half_h_tma (H curl + CPML X, Y, Z)", "alg_bytes_per_cell": REF_BYTES_H,
+              "avg_launch_ms": round(t_hc, 5), "achieved": round(gbs(REF_BYTES_H, t_hc), 1),
+              "frac": round(gbs(REF_BYTES_H, t_hc) / peak, 4), "traffic": tr_h,
+              "half_step_ms": round(t_h, 5)},
+    }
+    dom = "E" if t_ec >= t_hc else "H"
+    d = kern[dom]
+    step_bytes = tr.get("step_dram_bytes")
+    roofline = {
+        "bound": "hbm", "kernel": d["kernel"], "achieved": d["achieved"], "peak": peak,
+        "unit": "GB/s", "frac": d["frac"], "traffic": d["traffic"],
+        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, copy bandwidth)",
+        "alg_bytes_per_cell": d["alg_bytes_per_cell"], "units_per_launch": cells,
+        "avg_launch_ms": d["avg_launch_ms"],
+        "convention": "compulsory bytes of this design (E: read 3 E + 3 H + a 2-byte "
+                      "material id, write 3 E; H: read 3 H + 3 E, write 3 H) / the kernel's "
+                      "average launch time, CUDA events on the handle's stream",
+        "kernels": kern,
+        "step": {"ms": round(step_ms, 5),
+                 "compulsory_bytes_per_cell": e_bytes + REF_BYTES_H,
+                 "achieved": round(gbs(e_bytes + REF_BYTES_H, step_ms), 1),
+                 "frac": round(gbs(e_bytes + REF_BYTES_H, step_ms) / peak, 4),
+                 "dram_bytes_per_step": step_bytes,
+                 "dram_frac": (round(step_bytes / (step_ms / 1e3) / 1e9 / peak, 4)
+                               if step_bytes else None),
+                 "probe_gather_ms": round(t_o, 5)},
+        "reference_layout": {
+            "bytes_per_cell_step": REF_BYTES_H + REF_BYTES_E,
+            "note": "the reference's per-cell coefficient layout (H 36 B, E 60 B); the "
+                    "material ids read 2 B for its 24 B of coefficients, so this can "
+                    "exceed 1",
+            "step_frac": round(gbs(REF_BYTES_H + REF_BYTES_E, step_ms) / peak, 4),
+            "E_frac": round(gbs(REF_BYTES_E, t_ec) / peak, 4),
+            "H_frac": round(gbs(REF_BYTES_H, t_hc) / peak, 4)},
+        "traffic_source": tr.get("source"),
+    }
 
     # the batched, served and CPU legs: one GPU only (N = 1)
     solo = ranks.world == 1
-    batched = None
-    if solo and not args.no_batch:
-        batched = run_batched(args.batch_grids)
-
-    served = None
-    if solo and not args.no_serve:
-        served = run_served(args.serve_requests,
-                            [float(x) for x in args.serve_loads.split(",") if x])
-
     cpu = None
     if solo and not args.no_cpu:
         rate, done, secs, cores = cpu_oracle_rate(w, target_s=args.cpu_seconds, max_steps=2000)
@@ -306,6 +353,15 @@ def run_ours(args, ranks):
                "kind": "port",
                "sample": f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} grid, {done} steps "
                          f"({secs:.1f} s) of the FP32 oracle, OpenMP {cores} threads"}
+
+    served = None
+    if solo and not args.no_serve:
+        served = run_served(args.serve_requests,
+                            [float(x) for x in args.serve_loads.split(",") if x])
+
+    batched = None
+    if solo and not args.no_batch:
+        batched = run_batched(args.batch_grids)
     ranks.close()
     if ranks.rank != 0:
         return None
@@ -314,27 +370,18 @@ def run_ours(args, ranks):
         "n_gpus": ranks.world, "steps": K, "warmup": W, "ms_per_step": round(ms_max / K, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded spheres/layers, Gaussian-modulated plane wave)",
-        "config": {**workload_config(w), "parallelism": f"replicas x{ranks.world}",
-                   "timed": "fdtd_step_n: H and E curl kernels, their face passes, the E "
-                            "x-slab pass and the probe gather (6 launches per step), "
-                            "CUDA graph"},
-        "roofline": {"bound": "hbm", "kernel": "k_half_e (E half-step)",
-                     "achieved": round(ach_e, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(ach_e / peak, 4), "traffic": traffic,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "alg_bytes_per_cell": ALG_BYTES_E, "units_per_launch": cells,
-                     "avg_launch_ms": round(t_e, 5),
-                     "h_kernel": {"achieved": round(ach_h, 1), "frac": round(ach_h / peak, 4),
-                                  "alg_bytes_per_cell": ALG_BYTES_H, "avg_launch_ms": round(t_h, 5)},
-                     "probe_gather_ms": round(t_o, 5),
-                     "step": {"achieved": round(ach_step, 1), "frac": round(ach_step / peak, 4),
-                              "alg_bytes_per_cell_step": ALG_BYTES_STEP}},
+        "config": {**workload_config(w), "parallelism": f"replicas x{ranks.world}"},
+        "timed": "fdtd_step_n: H and E curl kernels, their face passes, the E x-slab pass "
+                 "and the probe gather, replayed as CUDA graphs",
+        "tuned": {"zchunk_h": inf["zchunk_h"], "zchunk_e": inf["zchunk_e"],
+                  "coef_mode": inf["coef_mode"], "num_materials": inf["num_materials"]},
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "batched": batched,
-        "served": served,
         "clocks": clk,
         "gpu_launches": int(launches),
+        "served": served,
+        "batched": batched,
     }
 
 
@@ -345,6 +392,9 @@ def ctypes_float():
 
 
 def run_e2e(w, K, simFDTD, materials, probe_locations, sources):
+    """A whole solve through the per-op simFDTD calls: create, set-up (with
+    the autotuner's trial steps when the shape is not in its cache), upload
+    of the media and sources, K steps, readout of the probes and Ez."""
     I, J, K3 = w.dims
     T = K
     mats = materials(w)
@@ -386,9 +436,10 @@ def run_e2e(w, K, simFDTD, materials, probe_locations, sources):
     d2h = ijk * 4 + probes.size * 4
     return {"value": round(ijk * K / dt / 1e6, 2), "unit": "Mcell-steps/s",
             "h2d_bytes_per_step": int(round(h2d / K)), "d2h_bytes_per_step": int(round(d2h / K)),
-            "seconds": round(dt, 6),
-            "path": "simFDTD per-op calls (6 per step, as highfrequency.m) incl. setup, "
-                    "material/source upload, probe + Ez readout"}
+            "seconds": round(dt, 6), "steps": K,
+            "path": "simFDTD per-op calls (6 per step, as highfrequency.m) for the "
+                    "configuration's step count, incl. set-up with the autotuner's trial "
+                    "steps (empty tune cache), material/source upload, probe + Ez readout"}
 
 
 def run_batched(n_grids: int, batched_only: bool = False):
@@ -552,7 +603,9 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--workload", default="c2", choices=("c1", "c2", "c3"))
+    ap.add_argument("--workload", default="c3", choices=("c1", "c2", "c3"))
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="steps of the end-to-end solve (0: the configuration's)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")

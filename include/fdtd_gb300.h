@@ -40,7 +40,8 @@ typedef enum {
   FDTD_ERR_ALREADY_INITIALIZED = 4, /* SetConst twice (simFDTD:AlreadyInitialized) */
   FDTD_ERR_CUDA = 5,             /* CUDA runtime / launch error */
   FDTD_ERR_OOM = 6,              /* device or pinned allocation failed */
-  FDTD_ERR_UNSUPPORTED = 7       /* outside the supported envelope */
+  FDTD_ERR_UNSUPPORTED = 7,      /* outside the supported envelope */
+  FDTD_ERR_CANCELLED = 8         /* a served request cancelled before it finished */
 } fdtd_status;
 
 /* Extension (no reference counterpart): runtime CPML and TF/SF settings.
@@ -252,12 +253,15 @@ int fdtd_checkpoint_load(fdtd_handle h, const void *buf, size_t n);
 int fdtd_event_record(fdtd_handle h, int32_t slot);
 int fdtd_event_elapsed_ms(fdtd_handle h, int32_t slot_a, int32_t slot_b, float *ms);
 
-/* Runs steps like fdtd_step_n but with direct launches and a CUDA event
- * pair around every kernel; adds the summed device time of the H half-step
- * kernels, the E half-step kernels and the remaining kernels (probe gather)
- * to ms_out[0..2].  For measurement only. */
+/* Runs steps like fdtd_step_n but with direct launches and CUDA events
+ * around every kernel; adds summed device times (ms) to ms_out:
+ * [0] H half-steps (curl kernel and its face pass), [1] E half-steps (curl
+ * kernel, x-slab and face passes), [2] the remaining kernels (probe
+ * gather), [3] the H curl kernel alone, [4] the E curl kernel alone,
+ * [5] steps whose H and E half-steps ran as one fused kernel (that kernel
+ * alone; its passes are in [0] and [1]).  For measurement only. */
 int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t tfsf_mode,
-                       const fdtd_current *cur, float ms_out[3]);
+                       const fdtd_current *cur, float ms_out[6]);
 
 /* Selects the CUDA device used by handles created afterwards on the calling
  * thread (one process per GPU: pass the local rank). */
@@ -376,6 +380,7 @@ typedef struct {
   double latency_p50_s, latency_p90_s, latency_p99_s, latency_mean_s;
   double solves_per_s;          /* completed / elapsed_s */
   uint64_t hbm_budget;          /* the budget in use */
+  uint64_t cancelled;           /* finished by fdtd_server_cancel (not in failed) */
 } fdtd_server_stats;
 
 int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg);
@@ -393,6 +398,33 @@ int fdtd_server_result(fdtd_server srv, uint64_t ticket, float *probes, size_t n
 /* Blocks until nothing is queued or running. */
 int fdtd_server_drain(fdtd_server srv);
 int fdtd_server_get_stats(fdtd_server srv, fdtd_server_stats *out);
+/* Cancels a request.  A queued request finishes at once with status
+ * FDTD_ERR_CANCELLED; a request on the device leaves at the end of the
+ * current round (its handle deleted, its memory returned to the budget) and
+ * finishes with FDTD_ERR_CANCELLED -- the others keep stepping and their
+ * results do not change.  In one_at_a_time mode a running request runs to
+ * its end.  Returns FDTD_ERR_STATE when the request had already finished,
+ * FDTD_ERR_INVALID_ARG for an unknown or released ticket.  The ticket is
+ * released by fdtd_server_result as usual. */
+int fdtd_server_cancel(fdtd_server srv, uint64_t ticket);
+
+/* ---------------------------------------------------------------------
+ * Host-side fault injection, for tests of the error paths (no reference
+ * counterpart: the reference checks no CUDA call).  Nothing here faults,
+ * traps or stalls the GPU: the failures are made on the host.
+ * --------------------------------------------------------------------- */
+#define FDTD_FAULT_NONE 0
+#define FDTD_FAULT_DEVICE_ALLOC 1
+/* FDTD_FAULT_DEVICE_ALLOC: the countdown-th device allocation a handle makes
+ * from now on (any handle, any thread; countdown >= 1) fails as if the
+ * device were out of memory (FDTD_ERR_OOM), once.  FDTD_FAULT_NONE disarms
+ * a pending one. */
+int fdtd_inject_fault(int32_t kind, int32_t countdown);
+/* Writes value into the handle's device error word, as a kernel whose
+ * bounded pipeline wait gave up would: the handle's next synchronising call
+ * (fdtd_synchronize, a readout) reports FDTD_ERR_CUDA and clears the word.
+ * Other handles are unaffected. */
+int fdtd_inject_device_error(fdtd_handle h, int32_t value);
 
 /* Allocation-free coefficient indexing.  No counterpart in the reference:
  * it serves callers that cannot allocate device memory -- hosts whose
@@ -411,8 +443,13 @@ int fdtd_server_get_stats(fdtd_server srv, fdtd_server_stats *out);
  * 1.25 MiB that every GPU loading the library holds until the process
  * exits.  Limit: max_ids <= 32768; larger values are rejected with
  * FDTD_ERR_INVALID_ARG, and inputs with more distinct tuples than max_ids
- * fail with FDTD_ERR_UNSUPPORTED.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
+ * fail with FDTD_ERR_UNSUPPORTED.  FDTD_ERR_UNSUPPORTED is also returned when
+ * two distinct tuples share a 64-bit hash (fdtd_last_error says which of the
+ * two happened); ReadySimulation keeps the six arrays in either case.  The
+ * first call on a device looks up the array's device address and keeps it
+ * for the process; make that first call before any stream capture, and do
+ * not call it again on a device after cudaDeviceReset (the kept address
+ * would be stale).
  * All calls share the one array, so calls that overlap on the GPU (on
  * different streams or host threads) race; serialise them.  stream is a
  * cudaStream_t (NULL: the legacy default stream); the call waits for it. */

@@ -76,7 +76,8 @@ class FdtdServerStats(ctypes.Structure):
                 ("queued", I32), ("active", I32), ("elapsed_s", ctypes.c_double),
                 ("latency_p50_s", ctypes.c_double), ("latency_p90_s", ctypes.c_double),
                 ("latency_p99_s", ctypes.c_double), ("latency_mean_s", ctypes.c_double),
-                ("solves_per_s", ctypes.c_double), ("hbm_budget", ctypes.c_uint64)]
+                ("solves_per_s", ctypes.c_double), ("hbm_budget", ctypes.c_uint64),
+                ("cancelled", ctypes.c_uint64)]
 
 
 class FdtdInfo(ctypes.Structure):
@@ -129,7 +130,7 @@ SIGNATURES = {
     "fdtd_event_record": (ctypes.c_int, [U64, I32]),
     "fdtd_event_elapsed_ms": (ctypes.c_int, [U64, I32, I32, ctypes.POINTER(ctypes.c_float)]),
     "fdtd_profile_steps": (ctypes.c_int, [U64, I32, I32, I32, ctypes.POINTER(FdtdCurrent),
-                                          ctypes.POINTER(ctypes.c_float * 3)]),
+                                          ctypes.POINTER(ctypes.c_float * 6)]),
     "fdtd_set_device": (ctypes.c_int, [I32]),
     "fdtd_index_coefficients_static": (ctypes.c_int, [ctypes.POINTER(P), I32, I32, I32, I32, P,
                                                       P, I32, ctypes.POINTER(I32), P]),
@@ -151,6 +152,9 @@ SIGNATURES = {
                                           ctypes.POINTER(FdtdRequestInfo)]),
     "fdtd_server_drain": (ctypes.c_int, [U64]),
     "fdtd_server_get_stats": (ctypes.c_int, [U64, ctypes.POINTER(FdtdServerStats)]),
+    "fdtd_server_cancel": (ctypes.c_int, [U64, ctypes.c_uint64]),
+    "fdtd_inject_fault": (ctypes.c_int, [I32, I32]),
+    "fdtd_inject_device_error": (ctypes.c_int, [U64, I32]),
     "fdtd_estimate_device_bytes": (ctypes.c_int, [I32, I32, I32, I32, I32, I32,
                                                   ctypes.POINTER(ctypes.c_uint64)]),
     "fdtd_division_plan": (ctypes.c_int, [ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
@@ -192,5 +196,5 @@ def load():
 STATUS_NAMES = {
     0: "FDTD_OK", 1: "FDTD_ERR_INVALID_HANDLE", 2: "FDTD_ERR_INVALID_ARG",
     3: "FDTD_ERR_STATE", 4: "FDTD_ERR_ALREADY_INITIALIZED", 5: "FDTD_ERR_CUDA",
-    6: "FDTD_ERR_OOM", 7: "FDTD_ERR_UNSUPPORTED",
+    6: "FDTD_ERR_OOM", 7: "FDTD_ERR_UNSUPPORTED", 8: "FDTD_ERR_CANCELLED",
 }

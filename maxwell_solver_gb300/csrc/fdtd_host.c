@@ -16,6 +16,7 @@
  * same order.  Ops arriving out of that order flush the queue first.
  */
 #define _GNU_SOURCE
+#include <assert.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdarg.h>
@@ -423,7 +424,35 @@ int fdtd_destroy(fdtd_handle h) {
   return FDTD_OK;
 }
 
+/* Host-side fault injection (fdtd_inject_fault): the countdown of device
+ * allocations until an injected failure; 0 = none armed. */
+static int32_t g_fault_alloc = 0;
+
+static int injected_alloc_failure(void) {
+  int32_t v = __atomic_load_n(&g_fault_alloc, __ATOMIC_SEQ_CST);
+  while (v > 0)
+    if (__atomic_compare_exchange_n(&g_fault_alloc, &v, v - 1, 0, __ATOMIC_SEQ_CST,
+                                    __ATOMIC_SEQ_CST))
+      return v == 1;
+  return 0;
+}
+
+int fdtd_inject_fault(int32_t kind, int32_t countdown) {
+  if (kind == FDTD_FAULT_NONE) {
+    __atomic_store_n(&g_fault_alloc, 0, __ATOMIC_SEQ_CST);
+    return FDTD_OK;
+  }
+  if (kind != FDTD_FAULT_DEVICE_ALLOC || countdown < 1)
+    return fail(FDTD_ERR_INVALID_ARG, "fault kind %d / countdown %d", kind, countdown);
+  __atomic_store_n(&g_fault_alloc, countdown, __ATOMIC_SEQ_CST);
+  return FDTD_OK;
+}
+
 static int dalloc(sim *s, void **p, size_t bytes) {
+  if (injected_alloc_failure()) {
+    *p = NULL;
+    return fail(FDTD_ERR_OOM, "device allocation of %zu bytes: injected failure", bytes);
+  }
   cudaMemPool_t pool;
   cudaError_t e = device_pool(&pool);
   if (e == cudaSuccess) e = cudaMallocFromPoolAsync(p, bytes ? bytes : 4, pool, s->stream);
@@ -1541,6 +1570,16 @@ static int check_device_error(sim *s) {
   return FDTD_OK;
 }
 
+int fdtd_inject_device_error(fdtd_handle h, int32_t value) {
+  GET(h);
+  if (!s->d_err) return fail(FDTD_ERR_STATE, "the handle has no device error word yet");
+  int rc = flush(s);
+  if (rc) return rc;
+  CU(cudaMemcpyAsync(s->d_err, &value, sizeof(value), cudaMemcpyHostToDevice, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
 static int run_steps(sim *s, int32_t first, int32_t count, int32_t mode,
                      const fdtd_current *cur);
 
@@ -1870,7 +1909,7 @@ static int run_steps(sim *s, int32_t first, int32_t count, int32_t mode,
 }
 
 int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t mode,
-                       const fdtd_current *cur, float ms_out[3]) {
+                       const fdtd_current *cur, float ms_out[6]) {
   GET(h);
   int rc = need_ready(s);
   if (rc) return rc;
@@ -1893,21 +1932,35 @@ int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t mode
       oe.cur_mode = cur->mode;
       memcpy(oe.cur_box, cur->box, sizeof(oe.cur_box));
     }
+    /* ev[12] / ev[13]: recorded right after the H / E curl kernel (the
+     * mark stays at the half-step's start when no curl kernel runs) */
     CU(cudaEventRecord(ev[8], s->stream));
     if (s->dev.num_ant > 0) KL(fdtdk_probe_gather(&s->dev, s->stream));
     CU(cudaEventRecord(ev[9], s->stream));
-    if ((rc = issue(s, 1, &oh))) return rc;
+    CU(cudaEventRecord(ev[12], s->stream));
+    fdtdk_set_profile_mark(ev[12]);
+    rc = issue(s, 1, &oh);
+    fdtdk_set_profile_mark(NULL);
+    if (rc) return rc;
     CU(cudaEventRecord(ev[10], s->stream));
-    if ((rc = issue(s, 0, &oe))) return rc;
+    CU(cudaEventRecord(ev[13], s->stream));
+    fdtdk_set_profile_mark(ev[13]);
+    rc = issue(s, 0, &oe);
+    fdtdk_set_profile_mark(NULL);
+    if (rc) return rc;
     CU(cudaEventRecord(ev[11], s->stream));
     CU(cudaEventSynchronize(ev[11]));
-    float a = 0, b = 0, d = 0;
+    float a = 0, b = 0, d = 0, hc = 0, ec = 0;
     CU(cudaEventElapsedTime(&d, ev[8], ev[9]));
     CU(cudaEventElapsedTime(&a, ev[9], ev[10]));
     CU(cudaEventElapsedTime(&b, ev[10], ev[11]));
+    CU(cudaEventElapsedTime(&hc, ev[9], ev[12]));
+    CU(cudaEventElapsedTime(&ec, ev[10], ev[13]));
     ms_out[0] += a;
     ms_out[1] += b;
     ms_out[2] += d;
+    ms_out[3] += hc;
+    ms_out[4] += ec;
   }
   return FDTD_OK;
 }
@@ -2358,6 +2411,9 @@ int fdtd_batch_add(fdtd_batch bh, fdtd_handle h, int32_t first, int32_t count, i
   if (!s->maps_b.valid) return fail(FDTD_ERR_UNSUPPORTED, "batch members need the TMA kernels");
   if (s->hcoef_mode)
     return fail(FDTD_ERR_UNSUPPORTED, "batch members need uniform H coefficients (no SetMagnetic)");
+  /* a work item packs its first z-plane into 16 bits (add_items) */
+  if (s->K > 65535)
+    return fail(FDTD_ERR_UNSUPPORTED, "batch members need K <= 65535 (K = %d)", s->K);
   if (first < 0 || count < 0) return fail(FDTD_ERR_INVALID_ARG, "negative step range");
   if (mode < 1 || mode > FDTD_MODE_OBLIQUE) mode = 0;
   const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
@@ -2423,6 +2479,7 @@ static int ensure_cap(void **d, void **hbuf, int *cap, int need, size_t elem, cu
 
 static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk) {
   const int zr = batch_zrun();
+  assert(nk <= 65536 && zr < 32768); /* kb and np share one int32 (fdtd_batch_add) */
   for (int kb = 0; kb < nk; kb += zr) {
     const int np = nk - kb < zr ? nk - kb : zr;
     for (int y0 = 0; y0 < nj; y0 += FDTD_BTILE_Y)

@@ -248,6 +248,11 @@ int fdtdk_compute_mu(float *out, const float *mu, const float *den_hx,
                      int64_t IJK, int32_t I, float delT, float sigma_m,
                      cudaStream_t s);
 unsigned long long fdtdk_launch_count(void);
+/* Measurement: while ev is set (not NULL), the half-step launchers of the
+ * calling thread record it on the stream right after the curl kernel, so
+ * that the curl kernel's time can be told from its passes' time. */
+void fdtdk_set_profile_mark(cudaEvent_t ev);
+void fdtdk_profile_mark(cudaStream_t s);
 /* Records an error message for the calling thread (fdtd_last_error) and
  * returns code. */
 int fdtd_internal_fail(int code, const char *msg);

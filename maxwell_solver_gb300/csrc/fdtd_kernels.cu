@@ -1144,6 +1144,12 @@ int fdtdk_batch_advance(int32_t *steps, int32_t n, cudaStream_t s) {
 
 void fdtdk_count_launches(unsigned long long n) { g_launches += n; }
 
+static thread_local cudaEvent_t g_profile_mark = nullptr;
+void fdtdk_set_profile_mark(cudaEvent_t ev) { g_profile_mark = ev; }
+void fdtdk_profile_mark(cudaStream_t s) {
+  if (g_profile_mark) cudaEventRecord(g_profile_mark, s);
+}
+
 unsigned long long fdtdk_launch_count(void) { return g_launches; }
 
 }  // extern "C"

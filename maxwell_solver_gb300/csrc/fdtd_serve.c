@@ -68,6 +68,7 @@ typedef struct req {
   /* batched mode: stepping this round, steps completed before its current
    * stretch in the batch, and steps completed now */
   int in_batch, want;
+  int cancel; /* fdtd_server_cancel while on the device (read with __atomic) */
   double key; /* this round's order (ascending) */
   int32_t done_base, done;
   struct req *next;
@@ -97,7 +98,7 @@ typedef struct server {
   cudaEvent_t ev[2];
   int ev_used[2], ev_i;
   /* statistics, under mu */
-  uint64_t submitted, completed, failed, cell_steps, peak_reserved;
+  uint64_t submitted, completed, failed, cancelled, cell_steps, peak_reserved;
   int peak_active;
   double first_submit, last_finish;
   double *lat;
@@ -162,6 +163,8 @@ static void finish(server *S, req *r, int32_t status, const char *msg) {
       }
     }
     if (S->n_lat < S->cap_lat) S->lat[S->n_lat++] = r->t_finish - r->t_submit;
+  } else if (status == FDTD_ERR_CANCELLED) {
+    S->cancelled += 1;
   } else {
     S->failed += 1;
   }
@@ -446,6 +449,12 @@ static void *serve_loop(void *arg) {
     }
     for (int a = 0; a < S->n_act;) {
       req *r = S->act[a];
+      if (__atomic_load_n(&r->cancel, __ATOMIC_ACQUIRE)) { /* fdtd_server_cancel */
+        drop_handle(S, r);
+        finish(S, r, FDTD_ERR_CANCELLED, "cancelled");
+        S->act[a] = S->act[--S->n_act];
+        continue;
+      }
       if (r->done < r->r.steps) {
         ++a;
         continue;
@@ -658,6 +667,40 @@ int fdtd_server_result(fdtd_server h, uint64_t ticket, float *probes, size_t n_p
   return st;
 }
 
+int fdtd_server_cancel(fdtd_server h, uint64_t ticket) {
+  server *S = slookup(h);
+  if (!S) return SFAIL(FDTD_ERR_INVALID_HANDLE, "invalid server handle");
+  pthread_mutex_lock(&S->mu);
+  req *r = ticket_req(S, ticket);
+  int rc = FDTD_OK;
+  if (!r) {
+    rc = SFAIL(FDTD_ERR_INVALID_ARG, "unknown or released ticket");
+  } else if (r->state == R_DONE) {
+    rc = SFAIL(FDTD_ERR_STATE, "the request has already finished");
+  } else if (r->state == R_QUEUED) { /* out of the queue, finished now */
+    req *prev = NULL;
+    for (req *q = S->q_head; q; prev = q, q = q->next)
+      if (q == r) {
+        if (prev) prev->next = r->next;
+        else S->q_head = r->next;
+        if (S->q_tail == r) S->q_tail = prev;
+        break;
+      }
+    r->next = NULL;
+    S->queued -= 1;
+    snprintf(r->message, sizeof(r->message), "cancelled");
+    r->status = FDTD_ERR_CANCELLED;
+    r->t_finish = now_s(S);
+    r->state = R_DONE;
+    S->cancelled += 1;
+    pthread_cond_broadcast(&S->cv_done);
+  } else { /* on the device: the loop drops it at the end of the round */
+    __atomic_store_n(&r->cancel, 1, __ATOMIC_RELEASE);
+  }
+  pthread_mutex_unlock(&S->mu);
+  return rc;
+}
+
 int fdtd_server_drain(fdtd_server h) {
   server *S = slookup(h);
   if (!S) return SFAIL(FDTD_ERR_INVALID_HANDLE, "invalid server handle");
@@ -690,6 +733,7 @@ int fdtd_server_get_stats(fdtd_server h, fdtd_server_stats *out) {
   out->submitted = S->submitted;
   out->completed = S->completed;
   out->failed = S->failed;
+  out->cancelled = S->cancelled;
   out->cell_steps = S->cell_steps;
   out->peak_reserved_bytes = S->peak_reserved;
   out->peak_active = S->peak_active;

@@ -887,6 +887,7 @@ int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
                        d->zc_e)
               : launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, &o, s, I, J, K,
                        d->zc_e);
+  if (!e) fdtdk_profile_mark(s);
   if (!e && o.xsplit) e = fdtdk_e_xslab(d, s);
   if (e || !o.tfsf_split) return e;
   return fdtdk_faces(0, d, &o, s);
@@ -912,6 +913,7 @@ int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
                        nk, d->zc_h)
               : launch(k_half_h_tma<false, false>, H_SMEM, &g_blocks_h[0], d, m, &o, s, ni, nj,
                        nk, d->zc_h);
+  if (!e) fdtdk_profile_mark(s);
   if (e || !o.tfsf_split) return e;
   return fdtdk_faces(1, d, &o, s);
 }

@@ -40,6 +40,7 @@ static void raise_status(int rc) {
     case FDTD_ERR_CUDA: id = "simFDTD:CudaError"; break;
     case FDTD_ERR_OOM: id = "simFDTD:OutOfMemory"; break;
     case FDTD_ERR_UNSUPPORTED: id = "simFDTD:Unsupported"; break;
+    case FDTD_ERR_CANCELLED: id = "simFDTD:Cancelled"; break;
   }
   mexErrMsgIdAndTxt(id, "%s", fdtd_last_error());
 }

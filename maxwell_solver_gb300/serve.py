@@ -98,6 +98,12 @@ class Server:
             raise SimFDTDError("simFDTD:ServeFailed", f"{name}: {out['info']['message']}")
         return out
 
+    def cancel(self, ticket: int) -> int:
+        """fdtd_server_cancel: 0 when the request was cancelled (its result
+        then raises with FDTD_ERR_CANCELLED), else the status (e.g. 3 when it
+        had finished already)."""
+        return int(self._lib.fdtd_server_cancel(self.handle, int(ticket)))
+
     def drain(self) -> None:
         _check(self._lib.fdtd_server_drain(self.handle))
 

@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libfdtd_oracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_fdtd.so")
+REF_FUNLIB_PATH = os.path.join(HERE, "_ref", "libref_funlib.so")
 _SRC = os.path.join(HERE, "fdtd_oracle.c")
 
 # field ids shared with fdtd_oracle.c's OR(field)
@@ -54,15 +55,36 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+def reference_root(ref_root: str | None = None) -> str | None:
+    """The reference checkout: the argument, else $MAXWELL_REF; None when
+    neither names a directory holding the reference's sources."""
+    root = ref_root or os.environ.get("MAXWELL_REF")
+    if not root or not os.path.exists(os.path.join(root, "src", "simulation.h")):
+        return None
+    return root
+
+
 def build_reference(ref_root: str | None = None) -> str | None:
     """Builds oracle/_ref/libref_fdtd.so from the reference sources when
-    they are present (this container only); returns its path or None."""
-    root = ref_root or os.environ.get("MAXWELL_REF", "/root/reference")
-    if not os.path.exists(os.path.join(root, "src", "simulation.h")):
+    they are present (see reference_root); returns its path or None."""
+    root = reference_root(ref_root)
+    if root is None:
         return None
     subprocess.run([os.path.join(HERE, "ref_build.sh"), root], check=True,
                    stdout=subprocess.DEVNULL)
     return REF_LIB_PATH
+
+
+def build_reference_funlib(ref_root: str | None = None) -> str | None:
+    """Builds oracle/_ref/libref_funlib.so, the reference's source-waveform
+    MEX file (src/cpucode/FunLib.cpp) against the test MEX stand-in, when
+    the reference sources are present; returns its path or None."""
+    root = reference_root(ref_root)
+    if root is None or not os.path.exists(os.path.join(root, "src", "cpucode", "FunLib.cpp")):
+        return None
+    subprocess.run([os.path.join(HERE, "funlib_build.sh"), root], check=True,
+                   stdout=subprocess.DEVNULL)
+    return REF_FUNLIB_PATH
 
 
 def _load():

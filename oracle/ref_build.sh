@@ -14,9 +14,13 @@
 #     the oracle; the reference's nvcc build may contract into FMA, which
 #     moves results by rounding only.
 #
-# Usage: oracle/ref_build.sh [reference_root]   (default /root/reference)
+# Usage: oracle/ref_build.sh <reference_root>   (or $MAXWELL_REF)
 set -euo pipefail
-REF="${1:-${MAXWELL_REF:-/root/reference}}"
+REF="${1:-${MAXWELL_REF:-}}"
+if [ -z "$REF" ]; then
+  echo "usage: ref_build.sh <reference_root> (or set MAXWELL_REF)" >&2
+  exit 2
+fi
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 STUB="$HERE/../tests/mexstub"

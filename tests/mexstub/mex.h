@@ -41,6 +41,7 @@ mxArray *mxCreateNumericArray(mwSize ndim, const mwSize *dims, mxClassID cls,
 mxArray *mxCreateNumericMatrix(mwSize m, mwSize n, mxClassID cls,
                                mxComplexity cplx);
 mxArray *mxCreateDoubleScalar(double v);
+mxArray *mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity cplx);
 mxArray *mxCreateString(const char *s);
 void mxDestroyArray(mxArray *a);
 void *mxGetData(const mxArray *a);
@@ -56,6 +57,8 @@ int mxGetString(const mxArray *a, char *buf, mwSize buflen);
 void mxFree(void *p);
 
 void mexErrMsgIdAndTxt(const char *id, const char *fmt, ...);
+/* The MEX file's entry point (C linkage, as MATLAB's own header gives it). */
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]);
 int mexPrintf(const char *fmt, ...);
 
 /* ---- harness side (not part of MATLAB's API) ---- */

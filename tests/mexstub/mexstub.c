@@ -57,6 +57,10 @@ mxArray *mxCreateDoubleScalar(double v) {
   return a;
 }
 
+mxArray *mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity cplx) {
+  return mxCreateNumericMatrix(m, n, mxDOUBLE_CLASS, cplx);
+}
+
 mxArray *mxCreateString(const char *s) {
   size_t len = strlen(s);
   mxArray *a = mxCreateNumericMatrix(1, len, mxCHAR_CLASS, mxREAL);

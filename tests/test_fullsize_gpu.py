@@ -1,9 +1,14 @@
 """Parity and size-independent properties at the benchmark configurations'
-full sizes (c2: 256^3 with a 12-cell CPML and 40 spheres; c3: 512x512x448
-with a 16-cell CPML and a 6-layer earth).
+full sizes (c1: 64^3 with a 10-cell CPML, vacuum, 8 probes; c2: 256^3 with
+a 12-cell CPML and 40 spheres; c3: 512x512x448 with a 16-cell CPML and a
+6-layer earth).
 
-- a few steps against the FP32 oracle, bit for bit (the oracle finishes
-  these in seconds on the host cores);
+- long runs against the FP32 oracle, bit for bit, fields and every probe
+  series: c1 for its full 500 steps with the reference's CPML constants
+  (src/simulation.h:86-90) and with the configuration's (kappa_max 5,
+  alpha_max 0.05, R0 1e-6), c2 for 200 steps, c3 for 20 (the oracle
+  finishes these in seconds on the host cores); the FP64 oracle gives the
+  error floor of the FP32 arithmetic itself;
 - linearity: doubling the plane-wave amplitude (Init1D rate 2) doubles every
   field over hundreds of steps, up to the subnormal rounding ahead of the
   wave front (the oracle departs by the same 6e-7);
@@ -18,12 +23,15 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
 
 
-def oracle_for(w, T):
+def oracle_for(w, T, params=None, precision="f32"):
     import oracle
     from maxwell_solver_gb300.workloads import materials, probe_locations, sources
 
-    o = oracle.OracleSim("f32")
-    o.set_params(pml=w.pml, tfsf_width=w.pml + 5)
+    o = oracle.OracleSim(precision)
+    if params is None:
+        o.set_params(pml=w.pml, tfsf_width=w.pml + 5)
+    else:
+        o.set_params(*params)
     I, J, K = w.dims
     o.set_const(np.float32([w.fctr, w.delX, w.delT]), np.int32([T, I, J, K, w.n_probes]))
     pw, cur = sources(w, T)
@@ -39,26 +47,76 @@ def oracle_for(w, T):
     return o
 
 
-@pytest.mark.parametrize("name,steps", [("c2", 6), ("c3", 3)])
-def test_full_size_steps_match_oracle(name, steps):
+REF_CPML = [3, 1, 0.08, 1, 0.8, 0]        # poly_m, alpha_m, alpha_max, kappa_max, sig_factor, r0
+CONFIG_CPML = [3, 1, 0.05, 5, 0.8, 1e-6]   # configuration 1: kappa_max 5, alpha_max 0.05, R0 1e-6
+
+
+def rel_l2(a, b):
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(np.asarray(a, dtype=np.float64) - b) /
+                 max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.parametrize("name,steps,cpml", [("c1", 500, "reference"), ("c1", 500, "config"),
+                                             ("c2", 200, "reference"), ("c3", 20, "reference")])
+def test_long_run_matches_oracle(name, steps, cpml):
+    """The fields after `steps` steps and every probe series of the run
+    equal the FP32 oracle's bit for bit (relative L2 0 <= 1e-5)."""
     from maxwell_solver_gb300 import simFDTD
     from maxwell_solver_gb300.workloads import WORKLOADS, setup
 
     w = WORKLOADS[name]
-    T = 40
-    P = setup(simFDTD, w, steps=T)
-    # advance into the run so that the incident wave is inside the grid
-    # (the oracle replays the same steps)
+    T = steps
+    tail = REF_CPML if cpml == "reference" else CONFIG_CPML
+    params = [w.pml, w.pml + 5] + tail
+    P = setup(simFDTD, w, steps=T, params=params)
     simFDTD("StepN", P, np.int32([0, steps, w.mode]))
-    o = oracle_for(w, T)
+    o = oracle_for(w, T, params)
     for n in range(steps):
         o.step(n, w.mode)
     ijk = w.cells
     for f, n in zip(range(1, 7), FIELDS):
         got = simFDTD("OutputVis", P, np.uint32(ijk), np.int32(f))
-        np.testing.assert_array_equal(got, o.field(n), err_msg=n)
+        want = o.field(n)
+        assert rel_l2(got, want) <= 1e-5, n
+        np.testing.assert_array_equal(got, want, err_msg=n)
     rec = simFDTD("OutputProbes", P, np.uint32(T * w.n_probes * 6))
-    np.testing.assert_array_equal(rec, o.array("probes"))
+    want = o.array("probes")
+    if name != "c3":  # (c3's pulse reaches its surface line after about 200 steps)
+        assert np.abs(want).max() > 0  # the wave reached the probes
+    assert rel_l2(rec, want) <= 1e-5
+    np.testing.assert_array_equal(rec, want)
+    simFDTD("DeleteSimulation", P)
+    o.close()
+
+
+@pytest.mark.parametrize("cpml", ["reference", "config"])
+def test_c1_error_floor_fp64(cpml):
+    """c1's 500 steps against the FP64 oracle: the GPU result is the FP32
+    arithmetic's own result (bit-identical to the FP32 oracle above), so its
+    distance from FP64 is the error floor of FP32 itself.  Measured: about
+    2.7e-5 (reference constants) and 2.0e-5 (configuration constants) of
+    the E and H family norms after 500 steps, 7e-7 on the probe series;
+    the bounds leave a factor of about two."""
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.workloads import WORKLOADS, setup
+
+    w = WORKLOADS["c1"]
+    T = w.steps
+    params = [w.pml, w.pml + 5] + (REF_CPML if cpml == "reference" else CONFIG_CPML)
+    P = setup(simFDTD, w, steps=T, params=params)
+    simFDTD("StepN", P, np.int32([0, T, w.mode]))
+    o = oracle_for(w, T, params, precision="f64")
+    for n in range(T):
+        o.step(n, w.mode)
+    for group in (range(0, 3), range(3, 6)):
+        got = [simFDTD("OutputVis", P, np.uint32(w.cells), np.int32(f + 1)) for f in group]
+        want = [o.field(FIELDS[f]) for f in group]
+        num = np.sqrt(sum(np.linalg.norm(a.astype(np.float64) - b) ** 2 for a, b in zip(got, want)))
+        den = np.sqrt(sum(np.linalg.norm(b) ** 2 for b in want))
+        assert num / den <= 6e-5, (group, num / den)
+    rec = simFDTD("OutputProbes", P, np.uint32(T * w.n_probes * 6))
+    assert rel_l2(rec, o.array("probes")) <= 2e-6
     simFDTD("DeleteSimulation", P)
     o.close()
 

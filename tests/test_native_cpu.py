@@ -54,6 +54,24 @@ def test_create_signal_matches_funlib_formula(native_lib):
         np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
 
 
+def test_create_signal_matches_reference_funlib(native_lib):
+    """fdtd_create_signal against the reference's own FunLib.cpp
+    ('CreateSignal', src/cpucode/FunLib.cpp:6-45), whose outputs for five
+    argument sets are in tests/golden/funlib_signal.npz (generated by
+    tests/golden/make_funlib_golden.py from the reference built by
+    oracle/funlib_build.sh): fmaxx equal, every sample within 1 ulp."""
+    from maxwell_solver_gb300 import create_signal
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "funlib_signal.npz"))
+    for c, args in enumerate(g["args"]):
+        fctr, dt, bw, lobes, steps = (float(v) for v in args)
+        fmaxx, got = create_signal(fctr, dt, bw, lobes, int(steps))
+        assert fmaxx == float(g[f"fmaxx_{c}"])
+        want = g[f"source_{c}"]
+        assert got.shape == want.shape
+        np.testing.assert_array_max_ulp(got, want, maxulp=1)
+
+
 def test_invalid_handle_is_rejected(native_lib):
     for fn in ("fdtd_update_h_all", "fdtd_update_e_all", "fdtd_ready_simulation",
                "fdtd_destroy", "fdtd_synchronize"):
