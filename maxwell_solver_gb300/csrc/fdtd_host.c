@@ -2624,7 +2624,7 @@ static int batch_rebuild(batch *b) {
 }
 
 /* One step of every active member: the probe rows, H (+ faces), E (+ x-slab
- * pass, faces) and the step counters. */
+ * pass unless the E kernel applies CPML X, faces) and the step counters. */
 static int batch_step_ops(batch *b) {
   if (b->any_probes) KL(fdtdk_batch_probes(b->d_devs, b->n_act, b->stream));
   KL(fdtdk_batch_half(1, b->all_lean_h, b->d_devs, b->d_maps, b->d_ops, b->d_steps, b->d_tab_h,
@@ -2637,7 +2637,8 @@ static int batch_step_ops(batch *b) {
                                  b->stream));
   KL(fdtdk_batch_half(0, b->all_lean, b->d_devs, b->d_maps, b->d_ops, b->d_steps,
                       b->d_tab_e, b->n_e, b->d_work + 2, b->d_err, b->stream));
-  if (b->any_xsplit)
+  /* the lean E kernel may apply CPML X itself (compacted per warp) */
+  if (b->any_xsplit && !(b->all_lean && fdtdk_batch_e_applies_x(1)))
     KL(fdtdk_batch_e_xslab(b->d_devs, b->d_ops, b->n_act, b->xs_max, b->stream));
   if (b->any_split)
     KL(fdtdk_batch_faces(0, b->d_devs, b->d_ops, b->d_steps, b->n_act, b->face_max,

@@ -236,6 +236,9 @@ int fdtdk_batch_half(int hfam, int lean, const fdtd_dev *devs, const void *maps,
 /* Probe rows of every grid of a batch, then +1 on each grid's probe row
  * and step (fdtd_kernels.cu). */
 int fdtdk_batch_probes(const fdtd_dev *devs, int32_t n, cudaStream_t s);
+/* 1 when the batched E kernel (lean variant when lean) applies the CPML X
+ * corrections itself, so the batch needs no x-slab pass. */
+int fdtdk_batch_e_applies_x(int lean);
 int fdtdk_batch_advance(int32_t *steps, int32_t n, cudaStream_t s);
 /* Batched-tile geometry of the TMA kernels. */
 #define FDTD_TILE_X 64

@@ -213,15 +213,19 @@ static int collect(server *S, req *r) {
     rc = fdtd_output_vis(r->h, r->out_field, r->n_out_field, q->out_field);
   }
   if (!rc) rc = fdtd_synchronize(r->h);
-  if (!S->cfg.one_at_a_time && S->batch) fdtd_batch_remove(S->batch, r->h);
+  if (S->batch && r->in_batch) fdtd_batch_remove(S->batch, r->h);
+  r->in_batch = 0;
   fdtd_destroy(r->h);
   r->h = 0;
   return rc;
 }
 
+/* (a handle that never joined the batch is not removed from it: that call
+ * would fail and replace the message of the error being reported) */
 static void drop_handle(server *S, req *r) {
   if (!r->h) return;
-  if (S->batch) fdtd_batch_remove(S->batch, r->h);
+  if (S->batch && r->in_batch) fdtd_batch_remove(S->batch, r->h);
+  r->in_batch = 0;
   fdtd_destroy(r->h);
   r->h = 0;
 }

@@ -341,16 +341,49 @@ __device__ __forceinline__ void cell_map(int tid, int &xo, int &r0) {
   r0 = w / WPR;
 }
 
+// The CPML X columns of a warp's 32-cell run as at most two runs of lanes
+// (the low and the high x slab): lanes a1 .. a1+len1-1 and a2 .. a2+len2-1.
+struct XRuns {
+  int a1, len1, a2, n;  // n = len1 + len2
+};
+__device__ __forceinline__ XRuns x_runs(unsigned mask) {
+  XRuns r{0, 0, 0, __popc(mask)};
+  if (!mask) return r;
+  r.a1 = __ffs(mask) - 1;
+  const unsigned up = mask >> r.a1;
+  r.len1 = (~up == 0u) ? 32 - r.a1 : __ffs(~up) - 1;
+  const unsigned rest = r.len1 >= 32 ? 0u : mask & ~(((1u << r.len1) - 1u) << r.a1);
+  r.a2 = rest ? __ffs(rest) - 1 : 0;
+  return r;
+}
+// Lane of the t-th X column (t < n).
+__device__ __forceinline__ int x_run_lane(const XRuns &r, int t) {
+  return t < r.len1 ? r.a1 + t : r.a2 + (t - r.len1);
+}
+// Generic-proxy writes into a ring stage before the stage goes back to the
+// producer, whose TMA copies (async proxy) overwrite it next.
+__device__ __forceinline__ void stage_writes_fence() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // ----------------------------------------------------------------- E half
 
 // LEAN: every grid the launch serves has its TF/SF corrections in the face
-// pass (or none), CPML X in the x-slab pass (or no CPML) and no current
-// source, so the consumer drops those per-cell paths (fewer registers and
-// branches; the cells it updates and their arithmetic are the same).
-template <bool PML, bool BATCH, bool LEAN = false>
+// pass (or none), CPML X split from the per-cell path (or no CPML) and no
+// current source, so the consumer drops those per-cell paths (fewer
+// registers and branches; the cells it updates and their arithmetic are the
+// same).
+// XC (with LEAN and PML): the CPML X corrections, the last operation of an
+// x-slab cell, run inside this kernel after each plane's curl and Y / Z
+// corrections, compacted per warp: the warp's x-slab cells (a few lanes of
+// each of its two rows) leave their Ey, Ez in the stage's E tile, and
+// then the warp's lanes take them one per lane.  Without XC the x-slab pass
+// (k_e_xslab) applies them after the kernel.
+template <bool PML, bool BATCH, bool LEAN = false, bool XC = false>
 __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_E)
     k_half_e_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
+  static_assert(!XC || (LEAN && PML), "compacted CPML X needs the lean kernel with CPML");
   extern __shared__ __align__(128) unsigned char smem[];
   using G = GeoOf<BATCH>;
   constexpr int ST = EG<BATCH>::STAGE;
@@ -362,6 +395,13 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // single grid: the coefficient table (if small) lives in shared memory
   const bool tab_in_smem = !BATCH && d0.coef_mode == 1 && d0.n_mat <= kSmemTabMax;
+  // XC, single grid: the E grading tables for the per-lane X corrections
+  __shared__ float s_xbcE[2][XC && !BATCH ? 2 * FDTD_MAX_PML : 1];
+  if (XC && !BATCH)
+    for (int t = tid; t < 2 * FDTD_MAX_PML; t += NT) {
+      s_xbcE[0][t] = d0.bE[t];
+      s_xbcE[1][t] = d0.cE[t];
+    }
 
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
@@ -425,6 +465,9 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
   bool valid[2] = {false, false}, col_special[2] = {false, false}, cur_col[2] = {false, false};
   float hx_km[2] = {0.f, 0.f}, hy_km[2] = {0.f, 0.f};
   int64_t n0[2] = {0, 0};
+  // XC: this warp's x-slab lanes and which of its rows hold x-slab cells
+  XRuns xr{0, 0, 0, 0};
+  bool x_lane = false, x_row[2] = {false, false};
 
   for (int q = 0;; ++q) {
     const int s = q % NS;
@@ -472,6 +515,12 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
           hx_km[c] = d.f[3][n0[c] - d.plane];
           hy_km[c] = d.f[4][n0[c] - d.plane];
         }
+        // E x-slab cells: 1 <= j <= J-2 and 1 <= k <= K-2 (gpu.h:776-777)
+        if (XC) x_row[c] = j >= 1 && j <= J - 2;
+      }
+      if (XC) {
+        x_lane = i < I && slab_e(i, I, d.p) >= 0;
+        xr = x_runs(__ballot_sync(0xffffffffu, x_lane));
       }
     }
     const int k = kb + m.y;
@@ -521,13 +570,55 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
         ey = C.eye * ey + C.eyh * (+(hx - hx_km[c]) - (hz - hz_im));
         ez = C.eze * ez + C.ezh * (+(hy - hy_im) - (hx - hx_jm));
       }
+      const bool xcell = XC && x_lane && x_row[c] && k >= 1 && k <= K - 2;
       if (act) {
         d.f[0][n0[c] + off] = ex;
-        d.f[1][n0[c] + off] = ey;
-        d.f[2][n0[c] + off] = ez;
+        if (xcell) {  // CPML X below: Ey, Ez wait in the stage's E tile
+          const_cast<float *>(sEy)[eb] = ey;
+          const_cast<float *>(sEz)[eb] = ez;
+        } else {
+          d.f[1][n0[c] + off] = ey;
+          d.f[2][n0[c] + off] = ez;
+        }
       }
       hx_km[c] = hx;
       hy_km[c] = hy;
+    }
+    if (XC && xr.n && k >= 1 && k <= K - 2 && (x_row[0] || x_row[1])) {
+      // CPML X of the warp's x-slab cells (gpu.h:765-788), one per lane
+      __syncwarp();
+      const int nrow = (int)x_row[0] + (int)x_row[1];
+      for (int t = lane; t < xr.n * nrow; t += 32) {
+        const int c = x_row[0] ? t / xr.n : 1;
+        const int xl = x_run_lane(xr, t % xr.n);
+        const int ty = r0 + (G::BY / 2) * c;
+        const int tcol = xo - lane + xl;  // the lane's column in the tile
+        const int ix = i - xo + tcol, j = y0 + ty;
+        const int eb = ty * G::BX + tcol, hb = (ty + 1) * G::HW + tcol + 4;
+        const int px = slab_e(ix, I, d.p);
+        const int64_t n = ix + (int64_t)j * d.Ip + (int64_t)k * d.plane;
+        Coef6 C;
+        if (use_mat) {
+          const int mi = sM[eb];
+          if (tab_local) {
+            const float *r = ttab + mi * 6;
+            C.eyh = r[4];
+            C.ezh = r[5];
+          } else {
+            C = coef_from_table(d, mi);
+          }
+        } else {
+          C = coef_from_arrays(d, n);
+        }
+        float ey = sEy[eb], ez = sEz[eb];
+        float2 *X = psi_at_x(d, PSI_EX, px, j, k);
+        const float xb = BATCH ? d.bE[px] : s_xbcE[0][px];
+        const float xc = BATCH ? d.cE[px] : s_xbcE[1][px];
+        e_corr_x_bc(d, xb, xc, *X, X, C, sHz[hb], sHz[hb - 1], sHy[hb], sHy[hb - 1], ey, ez);
+        d.f[1][n] = ey;
+        d.f[2][n] = ez;
+      }
+      stage_writes_fence();
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
@@ -540,10 +631,16 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
 // material ids and table (or the arrays); compiled for 3 blocks per SM.
 // LEAN: every grid the launch serves has its TF/SF corrections in the face
 // pass (or none), so the consumer drops the inline TF/SF path.
-template <bool PML, bool BATCH, bool MU = false, bool LEAN = false>
+// XC (with LEAN and PML, not MU): on planes outside the z slabs, the CPML X
+// corrections (after curl and Y, gpu.h:604-642) run compacted per warp: the
+// x-slab cells leave their Hy, Hz in the stage's H tile and the warp's
+// lanes then take them one per lane, instead of every row of a warp that
+// holds a few x-slab lanes taking the correction path.
+template <bool PML, bool BATCH, bool MU = false, bool LEAN = false, bool XC = false>
 __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_MIN_BLOCKS_H))
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
+  static_assert(!XC || (LEAN && PML && !MU), "compacted CPML X needs the lean kernel with CPML");
   extern __shared__ __align__(128) unsigned char smem[];
   using G = GeoOf<BATCH>;
   constexpr int ST = HG<BATCH>::STAGE;
@@ -632,6 +729,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
     const int px = PML ? slab_h(i, I, p) : -1;
     const bool x_face = mode && (i == d.i0 - 1 || i == d.i1);
     bool valid[2], col_face[2];  // col_face: a TF/SF face cell (not split off)
+    bool valid_row[2];           // the row holds H cells (j <= J-2)
     bool ax[2];                  // a cell of the warp row is in an x slab
     int py[2];
     int64_t n0[2];
@@ -639,11 +737,15 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
     for (int c = 0; c < 2; ++c) {
       const int j = y0 + r0 + (G::BY / 2) * c;
       valid[c] = i < I - 1 && j < J - 1;
+      valid_row[c] = j < J - 1;
       py[c] = PML ? slab_h(j, J, p) : -1;
       col_face[c] = x_face || (mode && (j == d.j0 - 1 || j == d.j1));
       n0[c] = valid[c] ? i + (int64_t)j * d.Ip + (int64_t)kb * d.plane : 0;
       ax[c] = PML && __any_sync(0xffffffffu, valid[c] && px >= 0);
     }
+    // XC: the warp's x-slab lanes (i <= I-2: H cells) as runs
+    const bool x_lane = XC && i < I - 1 && px >= 0;
+    const XRuns xr = XC ? x_runs(__ballot_sync(0xffffffffu, x_lane)) : XRuns{0, 0, 0, 0};
     // the item's first load is plane kb + np: Ex, Ey of the own cells, the
     // upper ends of plane kb + np - 1's z differences; then the planes from
     // the top down, each carrying its own Ex, Ey to the plane below
@@ -681,6 +783,8 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
       const int pz = PML ? slab_h(k, K, p) : -1;
       const bool plane_face = mode && (k == dp.k0 - 1 || k == dp.k1);
       const int64_t off = (int64_t)t * dp.plane;
+      // XC on this plane: outside the z slabs, X is compacted below
+      const bool xc_plane = XC && pz < 0 && xr.n > 0;
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         const int ty = r0 + (G::BY / 2) * c;
@@ -700,6 +804,26 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
         const bool ay = PML && py[c] >= 0, az = PML && pz >= 0;
         const int j = y0 + ty;
         const HCoef C = MU ? hcoef_at(dp, act ? n0[c] + off : 0) : HCoef{Chh, Chh, Chh, Che, Che, Che};
+        if (xc_plane) {  // curl, Y (warp-uniform); X below for the x-slab lanes
+          hx = C.hhx * hx + C.hex * (-dEz_y + dEy_z);
+          hy = C.hhy * hy + C.hey * (-dEx_z + dEz_x);
+          hz = C.hhz * hz + C.hez * (-dEy_x + dEx_y);
+          if (ay && act) {
+            float2 *Y = psi_at_y(dp, PSI_HY, i, py[c], k);
+            h_corr_y(dp, py[c], *Y, Y, dEz_y, dEx_y, hx, hz, C.hex, C.hez);
+          }
+          if (act) {
+            dp.f[3][n0[c] + off] = hx;
+            if (x_lane) {  // Hy, Hz wait in the stage's H tile
+              const_cast<float *>(sHy)[hb] = hy;
+              const_cast<float *>(sHz)[hb] = hz;
+            } else {
+              dp.f[4][n0[c] + off] = hy;
+              dp.f[5][n0[c] + off] = hz;
+            }
+          }
+          continue;
+        }
         if (oth || (int)ax[c] + (int)ay + (int)az > 1) {
           if (act) {
             update_h_cell<true, PML>(dp, C, mode, inc, i, j, k, px, py[c], pz,
@@ -732,6 +856,30 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
           dp.f[4][n0[c] + off] = hy;
           dp.f[5][n0[c] + off] = hz;
         }
+      }
+      if (xc_plane) {
+        // CPML X of the warp's x-slab cells, one per lane (H cells: j <= J-2)
+        __syncwarp();
+        const int nrow = (int)valid_row[0] + (int)valid_row[1];
+        for (int u = lane; u < xr.n * nrow; u += 32) {
+          const int c = valid_row[0] ? u / xr.n : 1;
+          const int xl = x_run_lane(xr, u % xr.n);
+          const int ty = r0 + (G::BY / 2) * c;
+          const int tcol = xo - lane + xl;
+          const int ix = x0 + tcol, j = y0 + ty;
+          const int eb = ty * G::HW + tcol, hb = ty * G::BX + tcol;
+          const int pxx = slab_h(ix, I, p);
+          const int64_t n = ix + (int64_t)j * dp.Ip + (int64_t)k * dp.plane;
+          float hy = sHy[hb], hz = sHz[hb];
+          float2 *X = psi_at_x(dp, PSI_HX, pxx, j, k);
+          const float xb = BATCH ? dp.bH[pxx] : s_xbc[0][pxx];
+          const float xc = BATCH ? dp.cH[pxx] : s_xbc[1][pxx];
+          h_corr_x_bc(dp, xb, xc, *X, X, sEz[eb + 1] - sEz[eb], sEy[eb + 1] - sEy[eb], hy, hz,
+                      Che, Che);
+          dp.f[4][n] = hy;
+          dp.f[5][n] = hz;
+        }
+        stage_writes_fence();
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
@@ -817,8 +965,20 @@ int encode(CUtensorMap *out, void *base, CUtensorMapDataType dt, int esize, cons
   return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
 }
 
-int g_blocks_e[4] = {0, 0, 0, 0}, g_blocks_h[6] = {0, 0, 0, 0, 0, 0};
-int g_blocks_b[4] = {0, 0, 0, 0};
+int g_blocks_e[5] = {0, 0, 0, 0, 0}, g_blocks_h[7] = {0, 0, 0, 0, 0, 0, 0};
+int g_blocks_b[6] = {0, 0, 0, 0, 0, 0};
+
+// The compacted CPML X kernels (XC) unless FDTD_XC=0 selects the lean
+// kernels without it, with E's CPML X as the x-slab pass (for comparison;
+// both give the same results).
+bool use_xc() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("FDTD_XC");
+    v = !(e && strcmp(e, "0") == 0);
+  }
+  return v != 0;
+}
 
 // Resident blocks of a kernel on the current device (cached per kernel).
 template <class KH>
@@ -877,7 +1037,12 @@ int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
   o.xsplit = fdtd_xsplit(d, op);
   const int I = d->I, J = d->J, K = d->K;
   int e;
-  if (fdtd_e_lean(&o))
+  bool xslab_pass = o.xsplit;
+  if (fdtd_e_lean(&o) && o.pml && use_xc()) {
+    e = launch(k_half_e_tma<true, false, true, true>, E_SMEM, &g_blocks_e[4], d, m, &o, s, I, J,
+               K, d->zc_e);
+    xslab_pass = false;  // the kernel applied CPML X
+  } else if (fdtd_e_lean(&o))
     e = o.pml ? launch(k_half_e_tma<true, false, true>, E_SMEM, &g_blocks_e[3], d, m, &o, s, I,
                        J, K, d->zc_e)
               : launch(k_half_e_tma<false, false, true>, E_SMEM, &g_blocks_e[2], d, m, &o, s, I,
@@ -888,7 +1053,7 @@ int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
               : launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, &o, s, I, J, K,
                        d->zc_e);
   if (!e) fdtdk_profile_mark(s);
-  if (!e && o.xsplit) e = fdtdk_e_xslab(d, s);
+  if (!e && xslab_pass) e = fdtdk_e_xslab(d, s);
   if (e || !o.tfsf_split) return e;
   return fdtdk_faces(0, d, &o, s);
 }
@@ -903,6 +1068,9 @@ int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
                        nj, nk, d->zc_h)
               : launch(k_half_h_tma<false, false, true>, H_SMEM, &g_blocks_h[2], d, m, &o, s,
                        ni, nj, nk, d->zc_h);
+  else if (fdtd_h_lean(&o) && o.pml && use_xc())
+    e = launch(k_half_h_tma<true, false, false, true, true>, H_SMEM, &g_blocks_h[6], d, m, &o, s,
+               ni, nj, nk, d->zc_h);
   else if (fdtd_h_lean(&o))
     e = o.pml ? launch(k_half_h_tma<true, false, false, true>, H_SMEM, &g_blocks_h[5], d, m, &o,
                        s, ni, nj, nk, d->zc_h)
@@ -937,7 +1105,14 @@ int fdtdk_batch_half(int hfam, int lean, const fdtd_dev *devs, const void *maps,
   static fdtd_op op0;
   static Maps mp0;
   int e;
-  if (hfam && lean) {
+  if (hfam && lean && use_xc()) {
+    e = resident_blocks(k_half_h_tma<true, true, false, true, true>, HG<true>::SMEM,
+                        &g_blocks_b[4]);
+    if (e) return e;
+    const int blocks = n_items < g_blocks_b[4] ? n_items : g_blocks_b[4];
+    k_half_h_tma<true, true, false, true, true><<<blocks, NT, HG<true>::SMEM, s>>>(d0, op0, mp0,
+                                                                                  it);
+  } else if (hfam && lean) {
     e = resident_blocks(k_half_h_tma<true, true, false, true>, HG<true>::SMEM, &g_blocks_b[3]);
     if (e) return e;
     const int blocks = n_items < g_blocks_b[3] ? n_items : g_blocks_b[3];
@@ -947,6 +1122,11 @@ int fdtdk_batch_half(int hfam, int lean, const fdtd_dev *devs, const void *maps,
     if (e) return e;
     const int blocks = n_items < g_blocks_b[0] ? n_items : g_blocks_b[0];
     k_half_h_tma<true, true><<<blocks, NT, HG<true>::SMEM, s>>>(d0, op0, mp0, it);
+  } else if (lean && use_xc()) {
+    e = resident_blocks(k_half_e_tma<true, true, true, true>, EG<true>::SMEM, &g_blocks_b[5]);
+    if (e) return e;
+    const int blocks = n_items < g_blocks_b[5] ? n_items : g_blocks_b[5];
+    k_half_e_tma<true, true, true, true><<<blocks, NT, EG<true>::SMEM, s>>>(d0, op0, mp0, it);
   } else if (lean) {
     e = resident_blocks(k_half_e_tma<true, true, true>, EG<true>::SMEM, &g_blocks_b[2]);
     if (e) return e;
@@ -980,4 +1160,5 @@ extern "C" int fdtdk_check_wait(int arrive, long long out[2]) {
 }
 
 extern "C" unsigned fdtdk_wait_polls(void) { return kSpinLimit; }
+extern "C" int fdtdk_batch_e_applies_x(int lean) { return lean && use_xc(); }
 extern "C" unsigned fdtdk_check_polls(void) { return kCheckPolls; }
