@@ -37,8 +37,11 @@ sys.path.insert(0, ROOT)
 REF_BYTES_H, REF_BYTES_E = 36, 60
 # Compulsory bytes of this design: the E coefficients are a 2-byte material
 # id per cell (a table of the distinct tuples in shared memory) when the grid
-# has at most 32768 distinct tuples, else the six arrays; H as above.
+# has at most 32768 distinct tuples, else the six arrays; H as above.  The
+# fused step (H and E in one pass, fields read from one buffer and written
+# to a second): read 3 E + 3 H + the id, write 3 E + 3 H.
 ID_BYTES_E = 38
+FUSED_BYTES = 50
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -262,7 +265,7 @@ def run_ours(args, ranks):
         e2e["value"] = round(cells * e2e_steps * ranks.world / slowest / 1e6, 2)
         e2e["seconds"] = round(slowest, 3)
 
-    KP = max(8, min(64, K // 4))  # per-kernel profiled steps
+    KP = max(8, min(64, K // 4)) // 2 * 2  # per-kernel profiled steps (even: fused pairs)
     T = W + K + KP
     P = setup(simFDTD, w, steps=T)
     h = int(P[0])
@@ -292,7 +295,7 @@ def run_ours(args, ranks):
     # launch (on the handle's stream, where the kernels run)
     acc = (ctypes.c_float * 6)()
     _check(lib.fdtd_profile_steps(h, W + K, KP, w.mode, None, ctypes.byref(acc)))
-    t_h, t_e, t_o, t_hc, t_ec = (acc[i] / KP for i in range(5))
+    t_h, t_e, t_o, t_hc, t_ec, t_f = (acc[i] / KP for i in range(6))
     simFDTD("DeleteSimulation", P)
 
     peak, peak_kind = measured_hbm_peak()
@@ -312,23 +315,36 @@ def run_ours(args, ranks):
               "frac": round(gbs(REF_BYTES_H, t_hc) / peak, 4), "traffic": tr_h,
               "half_step_ms": round(t_h, 5)},
     }
-    dom = "E" if t_ec >= t_hc else "H"
+    fused = t_f > 0
+    if fused:  # the steps ran as the fused pass (the half-step kernels did not run)
+        f_bytes = FUSED_BYTES if inf["coef_mode"] == 1 else FUSED_BYTES + 22
+        kern = {"F": {"kernel": "k_step_fused (H and E curl + CPML Y, Z and H X, one pass)",
+                      "alg_bytes_per_cell": f_bytes, "avg_launch_ms": round(t_f, 5),
+                      "achieved": round(gbs(f_bytes, t_f), 1),
+                      "frac": round(gbs(f_bytes, t_f) / peak, 4),
+                      "traffic": tr.get("k_step_fused_bytes_per_launch"),
+                      "passes_ms": round(t_e, 5)}}
+        dom = "F"
+    else:
+        dom = "E" if t_ec >= t_hc else "H"
     d = kern[dom]
-    step_bytes = tr.get("step_dram_bytes")
+    step_comp = (kern["F"]["alg_bytes_per_cell"] if fused else e_bytes + REF_BYTES_H)
+    step_bytes = tr.get("step_dram_bytes_fused" if fused else "step_dram_bytes")
     roofline = {
         "bound": "hbm", "kernel": d["kernel"], "achieved": d["achieved"], "peak": peak,
         "unit": "GB/s", "frac": d["frac"], "traffic": d["traffic"],
         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, copy bandwidth)",
         "alg_bytes_per_cell": d["alg_bytes_per_cell"], "units_per_launch": cells,
         "avg_launch_ms": d["avg_launch_ms"],
-        "convention": "compulsory bytes of this design (E: read 3 E + 3 H + a 2-byte "
-                      "material id, write 3 E; H: read 3 H + 3 E, write 3 H) / the kernel's "
+        "convention": "compulsory bytes of this design (fused step: read 3 E + 3 H + a "
+                      "2-byte material id, write 3 E + 3 H; half-step kernels: E read 3 E + "
+                      "3 H + the id, write 3 E, H read 3 H + 3 E, write 3 H) / the kernel's "
                       "average launch time, CUDA events on the handle's stream",
         "kernels": kern,
         "step": {"ms": round(step_ms, 5),
-                 "compulsory_bytes_per_cell": e_bytes + REF_BYTES_H,
-                 "achieved": round(gbs(e_bytes + REF_BYTES_H, step_ms), 1),
-                 "frac": round(gbs(e_bytes + REF_BYTES_H, step_ms) / peak, 4),
+                 "compulsory_bytes_per_cell": step_comp,
+                 "achieved": round(gbs(step_comp, step_ms), 1),
+                 "frac": round(gbs(step_comp, step_ms) / peak, 4),
                  "dram_bytes_per_step": step_bytes,
                  "dram_frac": (round(step_bytes / (step_ms / 1e3) / 1e9 / peak, 4)
                                if step_bytes else None),
@@ -339,8 +355,9 @@ def run_ours(args, ranks):
                     "material ids read 2 B for its 24 B of coefficients, so this can "
                     "exceed 1",
             "step_frac": round(gbs(REF_BYTES_H + REF_BYTES_E, step_ms) / peak, 4),
-            "E_frac": round(gbs(REF_BYTES_E, t_ec) / peak, 4),
-            "H_frac": round(gbs(REF_BYTES_H, t_hc) / peak, 4)},
+            **({"E_frac": round(gbs(REF_BYTES_E, t_ec) / peak, 4),
+                "H_frac": round(gbs(REF_BYTES_H, t_hc) / peak, 4)} if not fused else
+               {"fused_frac": round(gbs(REF_BYTES_H + REF_BYTES_E, t_f) / peak, 4)})},
         "traffic_source": tr.get("source"),
     }
 
@@ -371,9 +388,12 @@ def run_ours(args, ranks):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded spheres/layers, Gaussian-modulated plane wave)",
         "config": {**workload_config(w), "parallelism": f"replicas x{ranks.world}"},
-        "timed": "fdtd_step_n: H and E curl kernels, their face passes, the E x-slab pass "
-                 "and the probe gather, replayed as CUDA graphs",
-        "tuned": {"zchunk_h": inf["zchunk_h"], "zchunk_e": inf["zchunk_e"],
+        "timed": ("fdtd_step_n: pairs of steps as the fused H+E pass with its x-slab, face "
+                  "and fix-up passes and the probe gather" if inf["fused"] else
+                  "fdtd_step_n: H and E curl kernels, their face passes, the E x-slab pass "
+                  "and the probe gather") + ", replayed as CUDA graphs",
+        "tuned": {"fused": inf["fused"], "zchunk_f": inf["zchunk_f"],
+                  "zchunk_h": inf["zchunk_h"], "zchunk_e": inf["zchunk_e"],
                   "coef_mode": inf["coef_mode"], "num_materials": inf["num_materials"]},
         "roofline": roofline,
         "cpu_baseline": cpu,

@@ -229,6 +229,11 @@ typedef struct {
                                  (autotuned; 0 = built-in heuristic) */
   int32_t hcoef_mode;      /* H coefficients: 0 uniform, per cell
                               (fdtd_set_magnetic): 1 arrays, 2 indexed */
+  int32_t fused;           /* 1: fdtd_step_n runs pairs of steps as the fused
+                              H+E pass (a second field buffer is held; chosen
+                              by the autotuner) */
+  int32_t zchunk_f;        /* z-planes per work item of the fused pass (0:
+                              default) */
 } fdtd_info;
 int fdtd_get_info(fdtd_handle h, fdtd_info *out);
 

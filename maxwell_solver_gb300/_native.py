@@ -86,7 +86,8 @@ class FdtdInfo(ctypes.Structure):
                 ("j1", I32), ("k0", I32), ("k1", I32), ("coef_mode", I32),
                 ("num_materials", I32), ("device_bytes", ctypes.c_uint64),
                 ("Chh", ctypes.c_float), ("Che", ctypes.c_float),
-                ("zchunk_h", I32), ("zchunk_e", I32), ("hcoef_mode", I32)]
+                ("zchunk_h", I32), ("zchunk_e", I32), ("hcoef_mode", I32), ("fused", I32),
+                ("zchunk_f", I32)]
 
 
 # name -> (restype, argtypes)

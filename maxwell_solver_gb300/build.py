@@ -37,7 +37,8 @@ def cuda_home() -> str:
 def _sources():
     cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     c = sorted(glob.glob(os.path.join(CSRC, "*.c")))
-    hdr = sorted(glob.glob(os.path.join(CSRC, "*.h"))) + [os.path.join(INCLUDE, "fdtd_gb300.h")]
+    hdr = (sorted(glob.glob(os.path.join(CSRC, "*.h"))) + sorted(glob.glob(os.path.join(CSRC, "*.cuh")))
+           + [os.path.join(INCLUDE, "fdtd_gb300.h")])
     return cu, c, hdr
 
 

@@ -149,6 +149,17 @@ typedef struct sim {
   cudaGraphExec_t gexec;
   int g_mode, g_cur_mode, g_cur_box[6], g_probes;
   unsigned long long g_kernels;
+  /* the fused step (fdtd_fused.cu): a second field buffer and second H psi
+   * pairs, the descriptor with them (dev_b), the tensor maps of each buffer
+   * as the step's source (fmaps[0]: the handle's, fmaps[1]: the second),
+   * the z-run and whether the step uses it (fused: autotuned), its graph */
+  float *d_fb[6], *d_psib_pool;
+  fdtd_dev dev_b;
+  fdtd_maps_fused fmaps[2];
+  int32_t zc_f, fused;
+  cudaGraphExec_t gexec_f;
+  int gf_mode, gf_probes;
+  unsigned long long gf_kernels;
 } sim;
 
 /* ------------------------------------------------------------ registry */
@@ -381,7 +392,10 @@ int fdtd_destroy(fdtd_handle h) {
   pthread_mutex_unlock(&g_reg_lock);
   cudaStreamSynchronize(s->stream);
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->gexec_f) cudaGraphExecDestroy(s->gexec_f);
+  dfree(s->d_psib_pool);
   for (int a = 0; a < 6; ++a) {
+    dfree(s->d_fb[a]);
     dfree(s->d_f[a]);
     dfree(s->d_ce[a]);
     dfree(s->d_raw[a]);
@@ -696,6 +710,24 @@ static void build_tables(sim *s, float *kaE, float *kaH) {
   }
 }
 
+/* The second buffer's descriptor and both buffers' tensor maps for the
+ * fused step, after every change of the handle's descriptor. */
+static void fused_refresh(sim *s) {
+  if (s->gexec_f) {
+    cudaGraphExecDestroy(s->gexec_f);
+    s->gexec_f = NULL;
+  }
+  s->fmaps[0].valid = s->fmaps[1].valid = 0;
+  if (!s->d_fb[0] || !s->d_psib_pool) return;
+  s->dev_b = s->dev;
+  for (int a = 0; a < 6; ++a) s->dev_b.f[a] = s->d_fb[a];
+  s->dev_b.psi[PSI_HY] = s->d_psib_pool;
+  s->dev_b.psi[PSI_HX] = s->d_psib_pool + 4 * s->size_y;
+  s->dev_b.psi[PSI_HZ] = s->d_psib_pool + 4 * (s->size_y + s->size_x);
+  if (fdtdk_make_maps_fused(&s->dev, &s->fmaps[0])) s->fmaps[0].valid = 0;
+  if (fdtdk_make_maps_fused(&s->dev_b, &s->fmaps[1])) s->fmaps[1].valid = 0;
+}
+
 static void fill_dev_struct(sim *s) {
   fdtd_dev *d = &s->dev;
   if (s->gexec) { /* a captured step graph holds the old descriptor */
@@ -768,6 +800,7 @@ static void fill_dev_struct(sim *s) {
   d->probes = s->d_probes;
   d->probe_idx = s->d_probe_idx;
   d->num_ant = (s->init_ant && s->d_probes) ? s->num_ant : 0;
+  fused_refresh(s);
 }
 
 /* Material of cell (i,j,k) from the shapes (see k_rasterize; the same
@@ -882,28 +915,51 @@ static int zero_state(sim *s) {
   const size_t psi_total = (size_t)(4 * 2 * (s->size_x + s->size_y + s->size_z)) * sizeof(float);
   CU(cudaMemsetAsync(s->d_psi_pool, 0, psi_total, s->stream));
   CU(cudaMemsetAsync(s->d_ctr, 0, 4 * sizeof(int32_t), s->stream));
+  for (int a = 0; a < 6; ++a)
+    if (s->d_fb[a]) CU(cudaMemsetAsync(s->d_fb[a], 0, bytes, s->stream));
+  if (s->d_psib_pool)
+    CU(cudaMemsetAsync(s->d_psib_pool, 0, psi_total / 2, s->stream));
   return FDTD_OK;
 }
 
 /* ------------------------------------------------------------ autotune
  *
- * The TMA half-steps split the grid into work items of one tile and a run of
- * z-planes; the best run length depends on the grid (how many items keep
- * the GPU busy, how wide a band of planes the blocks sweep together).  It is
- * measured once per grid shape, at the end of ReadySimulation, while every
- * field and psi value is still exactly zero: a source-free step maps zero to
- * zero exactly, so the trial steps leave the state bit-identical and need no
- * snapshot.  Results are kept per process and in a text file
- * (FDTD_TUNE_CACHE, default $HOME/.cache/fdtd_gb300/autotune.txt);
- * FDTD_AUTOTUNE=0 disables it. */
+ * Measured once per grid shape at the end of ReadySimulation, while every
+ * field and psi value is still exactly zero (a source-free step maps zero
+ * to zero exactly, so the trial steps leave the state bit-identical and
+ * need no snapshot):
+ *   - the work-item height (z-planes per item, 2..32) of each half-step
+ *     kernel: how many items keep the GPU busy, how wide a band of planes
+ *     the blocks sweep together;
+ *   - the fused H+E pass against the two half-step kernels (E/H fusion
+ *     depth 2 or 1), and the fused pass's item height (8..64);
+ * Results are kept per process and in a text file (FDTD_TUNE_CACHE, default
+ * $HOME/.cache/fdtd_gb300/autotune.txt), keyed by the grid shape, the
+ * coefficient layouts, the device (name and SM count) and the library
+ * build (kernels change between builds), so an entry measured elsewhere is
+ * not reused; FDTD_AUTOTUNE=0 disables it. */
 
 #define TUNE_MAX 128
 typedef struct {
-  int32_t I, J, K, p, coef_mode, zh, ze;
+  char key[96]; /* device and build */
+  int32_t I, J, K, p, coef_mode, hcoef_mode, zh, ze, zf, fused;
 } tune_entry;
 static tune_entry g_tune[TUNE_MAX];
 static int g_tune_n = 0, g_tune_loaded = 0;
 static pthread_mutex_t g_tune_lock = PTHREAD_MUTEX_INITIALIZER;
+
+/* "<device name>|sm<count>|<build>" with blanks replaced. */
+static void tune_key(char *buf, size_t n) {
+  int dev = 0, sms = 0;
+  struct cudaDeviceProp pr;
+  memset(&pr, 0, sizeof(pr));
+  cudaGetDevice(&dev);
+  if (cudaGetDeviceProperties(&pr, dev) != cudaSuccess) snprintf(pr.name, sizeof(pr.name), "?");
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  snprintf(buf, n, "%s|sm%d|%s_%s", pr.name, sms, __DATE__, __TIME__);
+  for (char *c = buf; *c; ++c)
+    if (*c == ' ' || *c == '\t') *c = '_';
+}
 
 static void tune_cache_path(char *buf, size_t n) {
   const char *e = getenv("FDTD_TUNE_CACHE");
@@ -916,15 +972,17 @@ static void tune_cache_path(char *buf, size_t n) {
 static void tune_load(void) {
   if (g_tune_loaded) return;
   g_tune_loaded = 1;
-  char path[512];
+  char path[512], line[512];
   tune_cache_path(path, sizeof(path));
   if (!path[0]) return;
   FILE *f = fopen(path, "r");
   if (!f) return;
-  tune_entry t;
-  while (g_tune_n < TUNE_MAX && fscanf(f, "%d %d %d %d %d %d %d", &t.I, &t.J, &t.K, &t.p,
-                                       &t.coef_mode, &t.zh, &t.ze) == 7)
-    g_tune[g_tune_n++] = t;
+  while (g_tune_n < TUNE_MAX && fgets(line, sizeof(line), f)) {
+    tune_entry t;
+    if (sscanf(line, "v2 %95s %d %d %d %d %d %d %d %d %d %d", t.key, &t.I, &t.J, &t.K, &t.p,
+               &t.coef_mode, &t.hcoef_mode, &t.zh, &t.ze, &t.zf, &t.fused) == 11)
+      g_tune[g_tune_n++] = t; /* older formats are skipped */
+  }
   fclose(f);
 }
 
@@ -948,7 +1006,8 @@ static void tune_store(const tune_entry *t) {
   }
   FILE *f = fopen(path, "a");
   if (!f) return;
-  fprintf(f, "%d %d %d %d %d %d %d\n", t->I, t->J, t->K, t->p, t->coef_mode, t->zh, t->ze);
+  fprintf(f, "v2 %s %d %d %d %d %d %d %d %d %d %d\n", t->key, t->I, t->J, t->K, t->p,
+          t->coef_mode, t->hcoef_mode, t->zh, t->ze, t->zf, t->fused);
   fclose(f);
 }
 
@@ -982,19 +1041,64 @@ static int tune_measure(sim *s, int z, int steps, float *th, float *te) {
   return FDTD_OK;
 }
 
+/* Mean device time per step of source-free fused pairs with item height z
+ * (after one untimed pair). */
+static int tune_measure_fused(sim *s, int z, int pairs, float *t) {
+  fdtd_op op;
+  memset(&op, 0, sizeof(op));
+  op.curl = 1;
+  op.pml = 1;
+  float sum = 0;
+  for (int c = -1; c < pairs; ++c) {
+    CU(cudaEventRecord(s->ev[12], s->stream));
+    KL(fdtdk_step_fused(&s->dev_b, &s->dev, &s->fmaps[0], &op, z, s->stream));
+    KL(fdtdk_step_fused(&s->dev, &s->dev_b, &s->fmaps[1], &op, z, s->stream));
+    CU(cudaEventRecord(s->ev[13], s->stream));
+    CU(cudaEventSynchronize(s->ev[13]));
+    float a = 0;
+    CU(cudaEventElapsedTime(&a, s->ev[12], s->ev[13]));
+    if (c >= 0) sum += a;
+  }
+  *t = sum / (2 * pairs);
+  return FDTD_OK;
+}
+
+static int fused_usable(sim *s, int32_t mode, const fdtd_current *cur);
+
+/* The fused step's second buffer goes back to the pool when the autotuner
+ * chose the half-step kernels. */
+static void release_second_buffer(sim *s) {
+  if (!s->d_fb[0]) return;
+  for (int a = 0; a < 6; ++a) {
+    dfree(s->d_fb[a]);
+    s->d_fb[a] = NULL;
+  }
+  dfree(s->d_psib_pool);
+  s->d_psib_pool = NULL;
+  s->device_bytes -= (uint64_t)6 * s->cells * sizeof(float) +
+                     (uint64_t)4 * (s->size_x + s->size_y + s->size_z) * sizeof(float);
+  s->fused = 0;
+}
+
 static int autotune_zero_state(sim *s) {
   const char *e = getenv("FDTD_AUTOTUNE");
   if ((e && strcmp(e, "0") == 0) || !s->use_tma || !s->maps.valid) return FDTD_OK;
   if (s->cells < (int64_t)1 << 21) return FDTD_OK; /* small grids: heuristic */
+  char key[96];
+  tune_key(key, sizeof(key));
   pthread_mutex_lock(&g_tune_lock);
   tune_load();
   for (int i = 0; i < g_tune_n; ++i) {
     const tune_entry *t = &g_tune[i];
     if (t->I == s->I && t->J == s->J && t->K == s->K && t->p == s->p &&
-        t->coef_mode == s->coef_mode) {
+        t->coef_mode == s->coef_mode && t->hcoef_mode == s->hcoef_mode &&
+        strcmp(t->key, key) == 0) {
       s->zc_h = t->zh;
       s->zc_e = t->ze;
+      s->zc_f = t->zf;
+      s->fused = s->fused && t->fused;
       pthread_mutex_unlock(&g_tune_lock);
+      if (!s->fused) release_second_buffer(s);
       fill_dev_struct(s);
       return FDTD_OK;
     }
@@ -1013,12 +1117,50 @@ static int autotune_zero_state(sim *s) {
   }
   s->zc_h = zh;
   s->zc_e = ze;
+  int zf = 0, fused = 0;
+  if (fused_usable(s, 0, NULL)) {
+    static const int fcand[] = {8, 16, 32, 64};
+    float best_f = 1e30f;
+    for (size_t c = 0; c < sizeof(fcand) / sizeof(fcand[0]); ++c) {
+      if (fcand[c] > s->K && c > 0) break;
+      float tf = 0;
+      int rc = tune_measure_fused(s, fcand[c], 2, &tf);
+      if (rc) return rc;
+      if (tf < best_f) { best_f = tf; zf = fcand[c]; }
+    }
+    fused = best_f < best_h + best_e;
+  }
+  s->zc_f = zf;
+  s->fused = s->fused && fused;
+  if (!s->fused) release_second_buffer(s);
   fill_dev_struct(s);
-  tune_entry t = {s->I, s->J, s->K, s->p, s->coef_mode, zh, ze};
+  tune_entry t;
+  memset(&t, 0, sizeof(t));
+  snprintf(t.key, sizeof(t.key), "%s", key);
+  t.I = s->I;
+  t.J = s->J;
+  t.K = s->K;
+  t.p = s->p;
+  t.coef_mode = s->coef_mode;
+  t.hcoef_mode = s->hcoef_mode;
+  t.zh = zh;
+  t.ze = ze;
+  t.zf = zf;
+  t.fused = fused;
   pthread_mutex_lock(&g_tune_lock);
   tune_store(&t);
   pthread_mutex_unlock(&g_tune_lock);
   return FDTD_OK;
+}
+
+/* The fused step is used unless FDTD_FUSED=0 (read once). */
+static int fused_enabled(void) {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("FDTD_FUSED");
+    v = !(e && strcmp(e, "0") == 0);
+  }
+  return v;
 }
 
 /* src/simulation.h:640-979 */
@@ -1094,6 +1236,13 @@ int fdtd_ready_simulation(fdtd_handle h) {
       s->d_psi[a] = s->d_psi_pool + off;
       off += psi_n[a];
     }
+  }
+  if (s->use_tma && fused_enabled()) { /* the fused step's second buffer */
+    for (int a = 0; a < 6; ++a)
+      if ((rc = dalloc(s, (void **)&s->d_fb[a], bytes))) return rc;
+    const int64_t hpsi = psi_n[PSI_HY] + psi_n[PSI_HX] + psi_n[PSI_HZ];
+    if ((rc = dalloc(s, (void **)&s->d_psib_pool, (size_t)hpsi * sizeof(float)))) return rc;
+    s->fused = 1;
   }
   if ((rc = dalloc(s, (void **)&s->d_den_ex, (size_t)s->I * sizeof(float)))) return rc;
   if ((rc = dalloc(s, (void **)&s->d_den_hx, (size_t)s->I * sizeof(float)))) return rc;
@@ -1857,6 +2006,83 @@ int fdtd_step_n(fdtd_handle h, int32_t first, int32_t count, int32_t mode,
   return run_steps(s, first, count, mode, cur);
 }
 
+/* Can steps of this mode (and current) run as fused pairs? */
+static int fused_usable(sim *s, int32_t mode, const fdtd_current *cur) {
+  if (!s->fused || !s->fmaps[0].valid || !s->fmaps[1].valid) return 0;
+  if (cur && cur->mode >= 1 && cur->mode <= 3) return 0;
+  if (mode == FDTD_MODE_OBLIQUE && !s->d_ob[0]) return 0;
+  fdtd_op o;
+  memset(&o, 0, sizeof(o));
+  o.curl = 1;
+  o.pml = 1;
+  o.tfsf_mode = mode;
+  return fdtd_fused_ok(&s->dev, &o);
+}
+
+/* One fused step out of buffer `from` (0: the handle's fields, 1: the
+ * second buffer) into the other: the probe row of the state it starts
+ * from, then the pass and its face / x-slab passes. */
+static int fused_step(sim *s, int from, int32_t step, int from_dev, int32_t mode) {
+  fdtd_op o;
+  memset(&o, 0, sizeof(o));
+  o.curl = 1;
+  o.pml = 1;
+  o.tfsf_mode = mode;
+  o.step = step;
+  o.step_from_dev = from_dev;
+  const fdtd_dev *dold = from ? &s->dev_b : &s->dev, *dnew = from ? &s->dev : &s->dev_b;
+  if (s->dev.num_ant > 0) KL(fdtdk_probe_gather(dold, s->stream));
+  KL(fdtdk_step_fused(dnew, dold, &s->fmaps[from], &o, s->zc_f, s->stream));
+  return FDTD_OK;
+}
+
+/* Steps first..first+count-1 as fused pairs: GRAPH_CHUNK-step graph
+ * replays, then single pairs; an odd last step goes the plain way. */
+static int run_fused(sim *s, int32_t first, int32_t count, int32_t mode) {
+  int rc;
+  const int probes = s->dev.num_ant > 0;
+  int32_t done = 0;
+  if (count >= GRAPH_CHUNK) {
+    if (!(s->gexec_f && s->gf_mode == mode && s->gf_probes == probes)) {
+      if (s->gexec_f) {
+        cudaGraphExecDestroy(s->gexec_f);
+        s->gexec_f = NULL;
+      }
+      cudaGraph_t g;
+      const unsigned long long before = fdtdk_launch_count();
+      CU(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+      int crc = FDTD_OK;
+      for (int c = 0; c < GRAPH_CHUNK && !crc; ++c) crc = fused_step(s, c & 1, c, 1, mode);
+      if (!crc) crc = fdtdk_add_i32(s->d_ctr, GRAPH_CHUNK, s->stream) ? FDTD_ERR_CUDA : FDTD_OK;
+      cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+      if (crc) return crc;
+      if (ce != cudaSuccess) return fail(FDTD_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&s->gexec_f, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) {
+        s->gexec_f = NULL;
+        return fail(FDTD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+      }
+      s->gf_kernels = fdtdk_launch_count() - before;
+      g_captured_kernels += s->gf_kernels;
+      s->gf_mode = mode;
+      s->gf_probes = probes;
+    }
+    KL(fdtdk_set_i32(s->d_ctr, first, s->stream));
+    while (count - done >= GRAPH_CHUNK) {
+      CU(cudaGraphLaunch(s->gexec_f, s->stream));
+      g_graph_kernels += s->gf_kernels;
+      done += GRAPH_CHUNK;
+    }
+  }
+  for (; count - done >= 2; done += 2) {
+    if ((rc = fused_step(s, 0, first + done, 0, mode))) return rc;
+    if ((rc = fused_step(s, 1, first + done + 1, 0, mode))) return rc;
+  }
+  if (done < count) return step_ops(s, first + done, 0, mode, NULL);
+  return FDTD_OK;
+}
+
 /* Steps first..first+count-1 as GRAPH_CHUNK-step graph replays and single
  * steps (the arguments already checked). */
 static int run_steps(sim *s, int32_t first, int32_t count, int32_t mode,
@@ -1865,6 +2091,7 @@ static int run_steps(sim *s, int32_t first, int32_t count, int32_t mode,
   const int use_cur = cur && cur->mode >= 1 && cur->mode <= 3;
   const int probes = s->dev.num_ant > 0;
   int32_t done = 0;
+  if (count >= 2 && fused_usable(s, mode, cur)) return run_fused(s, first, count, mode);
   if (count >= GRAPH_CHUNK) {
     const int cm = use_cur ? cur->mode : 0;
     int same = s->gexec && s->g_mode == mode && s->g_cur_mode == cm && s->g_probes == probes;
@@ -1920,7 +2147,40 @@ int fdtd_profile_steps(fdtd_handle h, int32_t first, int32_t count, int32_t mode
     return fail(FDTD_ERR_INVALID_ARG, "steps [%d, %d) exceed T=%d", first, first + count, s->T);
   if ((rc = flush(s))) return rc;
   cudaEvent_t *ev = s->ev;
-  for (int32_t c = 0; c < count; ++c) {
+  int32_t c0 = 0;
+  if (count >= 2 && fused_usable(s, mode, cur)) {
+    /* fused pairs: [2] the probe gathers, [5] the fused pass, [1] its
+     * x-slab, face and fix-up passes */
+    const int32_t nf = count & ~1;
+    for (; c0 < nf; ++c0) {
+      const int from = c0 & 1;
+      const fdtd_dev *dold = from ? &s->dev_b : &s->dev, *dnew = from ? &s->dev : &s->dev_b;
+      fdtd_op o;
+      memset(&o, 0, sizeof(o));
+      o.curl = 1;
+      o.pml = 1;
+      o.tfsf_mode = mode;
+      o.step = first + c0;
+      CU(cudaEventRecord(ev[8], s->stream));
+      if (s->dev.num_ant > 0) KL(fdtdk_probe_gather(dold, s->stream));
+      CU(cudaEventRecord(ev[9], s->stream));
+      CU(cudaEventRecord(ev[12], s->stream));
+      fdtdk_set_profile_mark(ev[12]);
+      const int e = fdtdk_step_fused(dnew, dold, &s->fmaps[from], &o, s->zc_f, s->stream);
+      fdtdk_set_profile_mark(NULL);
+      KL(e);
+      CU(cudaEventRecord(ev[10], s->stream));
+      CU(cudaEventSynchronize(ev[10]));
+      float d = 0, f = 0, r = 0;
+      CU(cudaEventElapsedTime(&d, ev[8], ev[9]));
+      CU(cudaEventElapsedTime(&f, ev[9], ev[12]));
+      CU(cudaEventElapsedTime(&r, ev[12], ev[10]));
+      ms_out[1] += r;
+      ms_out[2] += d;
+      ms_out[5] += f;
+    }
+  }
+  for (int32_t c = c0; c < count; ++c) {
     fdtd_op oh, oe;
     memset(&oh, 0, sizeof(oh));
     oh.curl = 1;
@@ -1986,6 +2246,7 @@ int fdtd_estimate_device_bytes(int32_t I, int32_t J, int32_t K, int32_t pml, int
   b += cells * 2 + (uint64_t)MAX_MATERIALS * 6 * 4; /* material ids + table */
   b += (uint64_t)HASH_CAP * (8 + 8 + 4) + 16 + 4;  /* indexing scratch, error word */
   b += 8 * (sx + sy + sz) * 4;                     /* psi pairs */
+  b += 6 * cells * 4 + 4 * (sx + sy + sz) * 4;     /* the fused step's second buffer */
   b += 2 * (uint64_t)I * 4 + 16;                   /* stretch denominators, counters */
   b += (uint64_t)T * num_ant * 6 * 4 + (uint64_t)num_ant * 8; /* probes */
   b += 4 * (uint64_t)T * S * 4 + (uint64_t)T * 4 + 16 * S + (uint64_t)T * 4; /* 1D tables */
@@ -2164,6 +2425,8 @@ int fdtd_get_info(fdtd_handle h, fdtd_info *o) {
   o->zchunk_h = s->zc_h;
   o->zchunk_e = s->zc_e;
   o->hcoef_mode = s->hcoef_mode;
+  o->fused = s->fused && s->fmaps[0].valid && s->fmaps[1].valid;
+  o->zchunk_f = s->zc_f;
   return FDTD_OK;
 }
 

@@ -183,6 +183,32 @@ static inline int fdtd_h_lean(const fdtd_op *op) { return !op->tfsf_mode || op->
  * the CPML and the current source (fdtd_tfsf_faces_clear). */
 #define FDTD_MODE_OBLIQUE 5
 
+/* The fused step (fdtd_fused.cu): H and E of a step in one pass that reads
+ * the fields from one buffer and writes them to a second one (steps go in
+ * pairs).  Tensor maps of the old buffer: Ex Ey Ez and Hx Hy Hz as boxes
+ * with the tile's halo, the material ids. */
+#define FDTD_FUSED_MAPS 7
+typedef struct {
+  FDTD_ALIGN64 unsigned char bytes[FDTD_FUSED_MAPS][128];
+  int32_t valid;
+} fdtd_maps_fused;
+
+/* Can a step of this op run as the fused pass?  Curl and CPML, no current
+ * source, uniform H coefficients, CPML X of E split off (fdtd_xsplit), and
+ * TF/SF faces at least three cells inside every CPML slab (the E cells on
+ * both sides of an H face plane, +-2 cells along it, are recomputed after
+ * the H face pass and must hold no CPML work). */
+static inline int fdtd_fused_ok(const fdtd_dev *d, const fdtd_op *op) {
+  if (!op->curl || !op->pml || op->cur_mode || d->hcoef_mode || d->p < 1) return 0;
+  if (d->I < 2 || d->J < 2 || d->K < 2) return 0;
+  if (2 * (int64_t)d->p * d->J * d->K > 0x7fffffff) return 0; /* the x-slab pass */
+  if (!op->tfsf_mode) return 1;
+  const int p = d->p;
+  if (d->i0 < p + 3 || d->j0 < p + 3 || d->k0 < p + 3) return 0;
+  if (d->i1 > d->I - p - 3 || d->j1 > d->J - p - 3 || d->k1 > d->K - p - 3) return 0;
+  return d->i0 <= d->i1 && d->j0 <= d->j1 && d->k0 <= d->k1;
+}
+
 /* Launchers (fdtd_kernels.cu).  Return cudaError_t as int.  With valid
  * maps and op->curl set, the TMA-pipelined kernels run (fdtd_tma.cu);
  * otherwise the direct kernels.  use_tma = 0 forces the direct kernels. */
@@ -240,6 +266,16 @@ int fdtdk_batch_probes(const fdtd_dev *devs, int32_t n, cudaStream_t s);
  * corrections itself, so the batch needs no x-slab pass. */
 int fdtdk_batch_e_applies_x(int lean);
 int fdtdk_batch_advance(int32_t *steps, int32_t n, cudaStream_t s);
+/* The fused pass's maps, its default z-run, the pass alone, and one whole
+ * fused step: the pass from d_old (fields through m_old, H psi pairs) into
+ * d_new (fields, H psi pairs; E psi in place), the E x-slab pass, the H
+ * face pass, the E fix-up and the E face pass of op (zchunk 0: default). */
+int fdtdk_make_maps_fused(const fdtd_dev *old, fdtd_maps_fused *m);
+int fdtdk_fused_zchunk_default(int I, int J, int K);
+int fdtdk_fused_pass(const fdtd_dev *d_new, const fdtd_dev *d_old, const fdtd_maps_fused *m_old,
+                     int zchunk, cudaStream_t s);
+int fdtdk_step_fused(const fdtd_dev *d_new, const fdtd_dev *d_old, const fdtd_maps_fused *m_old,
+                     const fdtd_op *op, int zchunk, cudaStream_t s);
 /* Batched-tile geometry of the TMA kernels. */
 #define FDTD_TILE_X 64
 #define FDTD_TILE_Y 8
