@@ -302,7 +302,7 @@ def run_ours(args, ranks):
     value = cells * K * ranks.world / (ms_max / 1e3) / 1e6
     step_ms = ms.value / K
     e_bytes = ID_BYTES_E if inf["coef_mode"] == 1 else REF_BYTES_E
-    gbs = lambda b, t_ms: b * cells / (t_ms / 1e3) / 1e9  # noqa: E731
+    gbs = lambda b, t_ms: b * cells / (t_ms / 1e3) / 1e9 if t_ms > 0 else 0.0  # noqa: E731
     tr = ncu_traffic(w.name)
     tr_e, tr_h = tr.get("k_half_e_bytes_per_launch"), tr.get("k_half_h_bytes_per_launch")
     kern = {

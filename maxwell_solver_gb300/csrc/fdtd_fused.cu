@@ -77,12 +77,15 @@ constexpr int XW = BX + 1, XH = BY + 1;
 constexpr int XPLANE = XW * XH;                    // floats per component
 constexpr int XB_B = (3 * XPLANE * 4 + 127) / 128 * 128;
 constexpr int CTRL_B = 512;
-constexpr int kTabMax = 512;                       // coefficient ids staged in shared memory
+#ifndef FDTD_FUSED_TAB
+#define FDTD_FUSED_TAB 256
+#endif
+constexpr int kTabMax = FDTD_FUSED_TAB;  // coefficient ids staged in shared memory
 #ifndef FDTD_FUSED_NS
-#define FDTD_FUSED_NS 4
+#define FDTD_FUSED_NS 3
 #endif
 #ifndef FDTD_FUSED_MIN_BLOCKS
-#define FDTD_FUSED_MIN_BLOCKS 2
+#define FDTD_FUSED_MIN_BLOCKS 3
 #endif
 constexpr int NS = FDTD_FUSED_NS;
 constexpr int SMEM = NS * STAGE + 2 * XB_B + CTRL_B + kTabMax * 6 * 4;
@@ -435,7 +438,9 @@ __global__ void k_fix_e(const __grid_constant__ fdtd_dev d, const float *eox, co
   --axis;
   const int which = r & 3;
   const int lo[3] = {d.i0, d.j0, d.k0}, hi[3] = {d.i1, d.j1, d.k1};
-  const int u = (axis + 1) % 3, v = (axis + 2) % 3;
+  // u: the faster-varying of the other two axes (x before y before z), so
+  // that consecutive threads touch consecutive cells on y and z planes
+  const int u = axis == 0 ? 1 : 0, v = axis == 2 ? 1 : 2;
   const int plane = which < 2 ? lo[axis] - 1 + which : hi[axis] + (which - 2);
   const int u0 = lo[u] - 2, nu = hi[u] - lo[u] + 5, v0 = lo[v] - 2, nv = hi[v] - lo[v] + 5;
   const int64_t cnt = (int64_t)nu * nv;
@@ -523,6 +528,12 @@ int fdtdk_fused_pass(const fdtd_dev *d_new, const fdtd_dev *d_old, const fdtd_ma
   fp.psi_h_old[2] = d_old->psi[PSI_HZ];
   fp.tiles_x = (d_new->I + BX - 1) / BX;
   fp.tiles_y = (d_new->J + BY - 1) / BY;
+  static int forced = -1;  // FDTD_FUSED_ZCHUNK: a fixed item height (measurement sweeps)
+  if (forced < 0) {
+    const char *ev = getenv("FDTD_FUSED_ZCHUNK");
+    forced = ev ? atoi(ev) : 0;
+  }
+  if (forced > 0) zchunk = forced;
   fp.zchunk = zchunk > 0 ? (zchunk < d_new->K ? zchunk : d_new->K)
                          : fdtdk_fused_zchunk_default(d_new->I, d_new->J, d_new->K);
   fp.n_items = fp.tiles_x * fp.tiles_y * ((d_new->K + fp.zchunk - 1) / fp.zchunk);

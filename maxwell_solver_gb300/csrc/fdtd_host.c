@@ -940,6 +940,12 @@ static int zero_state(sim *s) {
  * not reused; FDTD_AUTOTUNE=0 disables it. */
 
 #define TUNE_MAX 128
+#define TUNE_MIN_CELLS ((int64_t)1 << 21) /* smaller grids: built-in heuristics */
+
+static int tune_enabled(void) {
+  const char *e = getenv("FDTD_AUTOTUNE");
+  return !(e && strcmp(e, "0") == 0);
+}
 typedef struct {
   char key[96]; /* device and build */
   int32_t I, J, K, p, coef_mode, hcoef_mode, zh, ze, zf, fused;
@@ -1064,6 +1070,7 @@ static int tune_measure_fused(sim *s, int z, int pairs, float *t) {
 }
 
 static int fused_usable(sim *s, int32_t mode, const fdtd_current *cur);
+static int fused_mode(void);
 
 /* The fused step's second buffer goes back to the pool when the autotuner
  * chose the half-step kernels. */
@@ -1081,9 +1088,8 @@ static void release_second_buffer(sim *s) {
 }
 
 static int autotune_zero_state(sim *s) {
-  const char *e = getenv("FDTD_AUTOTUNE");
-  if ((e && strcmp(e, "0") == 0) || !s->use_tma || !s->maps.valid) return FDTD_OK;
-  if (s->cells < (int64_t)1 << 21) return FDTD_OK; /* small grids: heuristic */
+  if (!tune_enabled() || !s->use_tma || !s->maps.valid) return FDTD_OK;
+  if (s->cells < TUNE_MIN_CELLS) return FDTD_OK; /* small grids: heuristic */
   char key[96];
   tune_key(key, sizeof(key));
   pthread_mutex_lock(&g_tune_lock);
@@ -1096,7 +1102,7 @@ static int autotune_zero_state(sim *s) {
       s->zc_h = t->zh;
       s->zc_e = t->ze;
       s->zc_f = t->zf;
-      s->fused = s->fused && t->fused;
+      s->fused = s->fused && (t->fused || fused_mode() == 1);
       pthread_mutex_unlock(&g_tune_lock);
       if (!s->fused) release_second_buffer(s);
       fill_dev_struct(s);
@@ -1128,7 +1134,7 @@ static int autotune_zero_state(sim *s) {
       if (rc) return rc;
       if (tf < best_f) { best_f = tf; zf = fcand[c]; }
     }
-    fused = best_f < best_h + best_e;
+    fused = best_f < best_h + best_e || fused_mode() == 1;
   }
   s->zc_f = zf;
   s->fused = s->fused && fused;
@@ -1153,14 +1159,14 @@ static int autotune_zero_state(sim *s) {
   return FDTD_OK;
 }
 
-/* The fused step is used unless FDTD_FUSED=0 (read once). */
-static int fused_enabled(void) {
-  static int v = -1;
-  if (v < 0) {
-    const char *e = getenv("FDTD_FUSED");
-    v = !(e && strcmp(e, "0") == 0);
-  }
-  return v;
+/* The fused step: FDTD_FUSED=0 never, =1 always (no autotuning of the
+ * choice), otherwise where the autotuner measures it faster (grids it
+ * tunes).  Read at every ReadySimulation. */
+static int fused_mode(void) {
+  const char *e = getenv("FDTD_FUSED");
+  if (e && strcmp(e, "0") == 0) return 0;
+  if (e && strcmp(e, "1") == 0) return 1;
+  return -1;
 }
 
 /* src/simulation.h:640-979 */
@@ -1237,7 +1243,9 @@ int fdtd_ready_simulation(fdtd_handle h) {
       off += psi_n[a];
     }
   }
-  if (s->use_tma && fused_enabled()) { /* the fused step's second buffer */
+  const int fmode = fused_mode();
+  if (s->use_tma && (fmode == 1 || (fmode < 0 && tune_enabled() &&
+                                    s->cells >= TUNE_MIN_CELLS))) { /* the fused step's second buffer */
     for (int a = 0; a < 6; ++a)
       if ((rc = dalloc(s, (void **)&s->d_fb[a], bytes))) return rc;
     const int64_t hpsi = psi_n[PSI_HY] + psi_n[PSI_HX] + psi_n[PSI_HZ];

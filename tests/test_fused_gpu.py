@@ -3,8 +3,8 @@ the FP32 oracle, bit for bit: every TF/SF mode (1-4 and oblique 5, whose
 face passes and E fix-up run after the pass), spheres in the CPML's
 reach, probes, runs through graph replays, single pairs and an odd last
 step, through the per-op calls, and with per-cell coefficient arrays
-instead of material ids.  Grids this small skip the autotuner, so the
-fused pass is the one that runs (checked with fdtd_get_info)."""
+instead of material ids.  FDTD_FUSED=1 makes the handles run the fused
+pass whatever the autotuner would choose (checked with fdtd_get_info)."""
 import math
 
 import numpy as np
@@ -15,6 +15,11 @@ pytestmark = pytest.mark.gpu
 DIMS, PML, W = (64, 56, 60), 8, 13
 FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
 ANG = (math.radians(55), math.radians(-35), math.radians(70))
+
+
+@pytest.fixture(autouse=True)
+def _force_fused(monkeypatch):
+    monkeypatch.setenv("FDTD_FUSED", "1")
 
 
 def _inputs(steps, seed=5):
