@@ -393,6 +393,8 @@ def run_ours(args, ranks):
                   "fdtd_step_n: H and E curl kernels, their face passes, the E x-slab pass "
                   "and the probe gather") + ", replayed as CUDA graphs",
         "tuned": {"fused": inf["fused"], "zchunk_f": inf["zchunk_f"],
+                  "tile_h": ("64x8", "32x16", "128x4")[inf["tile_h"]],
+                  "tile_e": ("64x8", "32x16", "128x4")[inf["tile_e"]],
                   "zchunk_h": inf["zchunk_h"], "zchunk_e": inf["zchunk_e"],
                   "coef_mode": inf["coef_mode"], "num_materials": inf["num_materials"]},
         "roofline": roofline,

@@ -234,6 +234,8 @@ typedef struct {
                               by the autotuner) */
   int32_t zchunk_f;        /* z-planes per work item of the fused pass (0:
                               default) */
+  int32_t tile_h, tile_e;  /* tile geometry of the H / E curl kernels
+                              (autotuned): 0 64x8, 1 32x16, 2 128x4 */
 } fdtd_info;
 int fdtd_get_info(fdtd_handle h, fdtd_info *out);
 

@@ -87,7 +87,7 @@ class FdtdInfo(ctypes.Structure):
                 ("num_materials", I32), ("device_bytes", ctypes.c_uint64),
                 ("Chh", ctypes.c_float), ("Che", ctypes.c_float),
                 ("zchunk_h", I32), ("zchunk_e", I32), ("hcoef_mode", I32), ("fused", I32),
-                ("zchunk_f", I32)]
+                ("zchunk_f", I32), ("tile_h", I32), ("tile_e", I32)]
 
 
 # name -> (restype, argtypes)

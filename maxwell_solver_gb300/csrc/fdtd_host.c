@@ -133,7 +133,8 @@ typedef struct sim {
   int32_t *d_hid, *d_hcnt;
   int32_t coef_mode, num_mat;
   int use_tma, allow_compress;
-  fdtd_maps maps, maps_b; /* single-grid and batched kernels' tiles */
+  fdtd_maps maps[FDTD_NUM_TILES]; /* per tile geometry (1: also the batch's) */
+  int32_t tile_h, tile_e;          /* the autotuner's geometries */
   int32_t zc_h, zc_e; /* tuned z-planes per TMA work item (0: heuristic) */
   uint64_t device_bytes;
   fdtd_dev dev;
@@ -780,6 +781,8 @@ static void fill_dev_struct(sim *s) {
   d->err = s->d_err;
   d->zc_h = s->zc_h;
   d->zc_e = s->zc_e;
+  d->tile_h = s->tile_h;
+  d->tile_e = s->tile_e;
   for (int a = 0; a < FDTD_NUM_PSI; ++a) d->psi[a] = s->d_psi[a];
   for (int a = 0; a < 4; ++a) d->inc[a] = s->d_inc[a];
   d->src = s->d_src;
@@ -939,7 +942,7 @@ static int zero_state(sim *s) {
  * build (kernels change between builds), so an entry measured elsewhere is
  * not reused; FDTD_AUTOTUNE=0 disables it. */
 
-#define TUNE_MAX 128
+#define TUNE_MAX 256
 #define TUNE_MIN_CELLS ((int64_t)1 << 21) /* smaller grids: built-in heuristics */
 
 static int tune_enabled(void) {
@@ -948,7 +951,7 @@ static int tune_enabled(void) {
 }
 typedef struct {
   char key[96]; /* device and build */
-  int32_t I, J, K, p, coef_mode, hcoef_mode, zh, ze, zf, fused;
+  int32_t I, J, K, p, coef_mode, hcoef_mode, zh, ze, zf, fused, th, te;
 } tune_entry;
 static tune_entry g_tune[TUNE_MAX];
 static int g_tune_n = 0, g_tune_loaded = 0;
@@ -985,8 +988,9 @@ static void tune_load(void) {
   if (!f) return;
   while (g_tune_n < TUNE_MAX && fgets(line, sizeof(line), f)) {
     tune_entry t;
-    if (sscanf(line, "v2 %95s %d %d %d %d %d %d %d %d %d %d", t.key, &t.I, &t.J, &t.K, &t.p,
-               &t.coef_mode, &t.hcoef_mode, &t.zh, &t.ze, &t.zf, &t.fused) == 11)
+    if (sscanf(line, "v3 %95s %d %d %d %d %d %d %d %d %d %d %d %d", t.key, &t.I, &t.J, &t.K,
+               &t.p, &t.coef_mode, &t.hcoef_mode, &t.zh, &t.ze, &t.zf, &t.fused, &t.th,
+               &t.te) == 13)
       g_tune[g_tune_n++] = t; /* older formats are skipped */
   }
   fclose(f);
@@ -1012,19 +1016,20 @@ static void tune_store(const tune_entry *t) {
   }
   FILE *f = fopen(path, "a");
   if (!f) return;
-  fprintf(f, "v2 %s %d %d %d %d %d %d %d %d %d %d\n", t->key, t->I, t->J, t->K, t->p,
-          t->coef_mode, t->hcoef_mode, t->zh, t->ze, t->zf, t->fused);
+  fprintf(f, "v3 %s %d %d %d %d %d %d %d %d %d %d %d %d\n", t->key, t->I, t->J, t->K, t->p,
+          t->coef_mode, t->hcoef_mode, t->zh, t->ze, t->zf, t->fused, t->th, t->te);
   fclose(f);
 }
 
 /* Mean device time of the H and E half-steps over `steps` source-free steps
- * with z-run length z (after one untimed step). */
-static int tune_measure(sim *s, int z, int steps, float *th, float *te) {
+ * with z-run length z in tile geometry `tile` (after one untimed step). */
+static int tune_measure(sim *s, int tile, int z, int steps, float *th, float *te) {
   fdtd_op op;
   memset(&op, 0, sizeof(op));
   op.curl = 1;
   op.pml = 1;
   s->dev.zc_h = s->dev.zc_e = z;
+  s->dev.tile_h = s->dev.tile_e = tile;
   float sh = 0, se = 0;
   for (int c = -1; c < steps; ++c) {
     CU(cudaEventRecord(s->ev[12], s->stream));
@@ -1088,7 +1093,7 @@ static void release_second_buffer(sim *s) {
 }
 
 static int autotune_zero_state(sim *s) {
-  if (!tune_enabled() || !s->use_tma || !s->maps.valid) return FDTD_OK;
+  if (!tune_enabled() || !s->use_tma || !s->maps[0].valid) return FDTD_OK;
   if (s->cells < TUNE_MIN_CELLS) return FDTD_OK; /* small grids: heuristic */
   char key[96];
   tune_key(key, sizeof(key));
@@ -1101,6 +1106,8 @@ static int autotune_zero_state(sim *s) {
         strcmp(t->key, key) == 0) {
       s->zc_h = t->zh;
       s->zc_e = t->ze;
+      s->tile_h = t->th;
+      s->tile_e = t->te;
       s->zc_f = t->zf;
       s->fused = s->fused && (t->fused || fused_mode() == 1);
       pthread_mutex_unlock(&g_tune_lock);
@@ -1112,17 +1119,23 @@ static int autotune_zero_state(sim *s) {
   pthread_mutex_unlock(&g_tune_lock);
   static const int cand[] = {2, 4, 8, 16, 32};
   float best_h = 1e30f, best_e = 1e30f;
-  int zh = 0, ze = 0;
-  for (size_t c = 0; c < sizeof(cand) / sizeof(cand[0]); ++c) {
-    if (cand[c] > s->K) break;
-    float th = 0, te = 0;
-    int rc = tune_measure(s, cand[c], 3, &th, &te);
-    if (rc) return rc;
-    if (th < best_h) { best_h = th; zh = cand[c]; }
-    if (te < best_e) { best_e = te; ze = cand[c]; }
+  int zh = 0, ze = 0, tlh = 0, tle = 0;
+  for (int tile = 0; tile < FDTD_NUM_TILES; ++tile) {
+    if (!s->maps[tile].valid) continue;
+    for (size_t c = 0; c < sizeof(cand) / sizeof(cand[0]); ++c) {
+      if (cand[c] > s->K) break;
+      float th = 0, te = 0;
+      int rc = tune_measure(s, tile, cand[c], 3, &th, &te);
+      if (rc) return rc;
+      if (th < best_h) { best_h = th; zh = cand[c]; tlh = tile; }
+      if (te < best_e) { best_e = te; ze = cand[c]; tle = tile; }
+    }
   }
   s->zc_h = zh;
   s->zc_e = ze;
+  s->tile_h = tlh;
+  s->tile_e = tle;
+  fill_dev_struct(s); /* the tuned half-steps for the fused comparison */
   int zf = 0, fused = 0;
   if (fused_usable(s, 0, NULL)) {
     static const int fcand[] = {8, 16, 32, 64};
@@ -1153,6 +1166,8 @@ static int autotune_zero_state(sim *s) {
   t.ze = ze;
   t.zf = zf;
   t.fused = fused;
+  t.th = tlh;
+  t.te = tle;
   pthread_mutex_lock(&g_tune_lock);
   tune_store(&t);
   pthread_mutex_unlock(&g_tune_lock);
@@ -1271,11 +1286,19 @@ int fdtd_ready_simulation(fdtd_handle h) {
   if ((rc = upload_coefficients(s))) return rc;
   if ((rc = zero_state(s))) return rc;
   if (s->use_tma) {
-    int e = fdtdk_make_maps(&s->dev, &s->maps);
-    if (e) s->maps.valid = 0; /* the direct kernels take over */
-    if (e || fdtdk_make_maps_batch(&s->dev, &s->maps_b)) s->maps_b.valid = 0;
+    for (int t = 0; t < FDTD_NUM_TILES; ++t)
+      if (fdtdk_make_maps(&s->dev, t, &s->maps[t])) s->maps[t].valid = 0;
+    if (!s->maps[0].valid) /* the direct kernels take over */
+      for (int t = 1; t < FDTD_NUM_TILES; ++t) s->maps[t].valid = 0;
   }
   if ((rc = autotune_zero_state(s))) return rc;
+  { /* FDTD_TILE=0|1|2: one tile geometry for both half-steps (comparisons) */
+    const char *et = getenv("FDTD_TILE");
+    if (et && et[0] >= '0' && et[0] < '0' + FDTD_NUM_TILES && !et[1]) {
+      s->tile_h = s->tile_e = et[0] - '0';
+      fill_dev_struct(s);
+    }
+  }
   CU(cudaStreamSynchronize(s->stream));
   s->init_ready = 1;
   return FDTD_OK;
@@ -1708,8 +1731,8 @@ int fdtd_init_1d(fdtd_handle h, float rate, const float *pw_source, size_t n) {
 /* ------------------------------------------------------------ step ops */
 
 static int issue(sim *s, int hfam, const fdtd_op *op) {
-  if (hfam) KL(fdtdk_half_h(&s->dev, &s->maps, s->use_tma, op, s->stream));
-  else KL(fdtdk_half_e(&s->dev, &s->maps, s->use_tma, op, s->stream));
+  if (hfam) KL(fdtdk_half_h(&s->dev, s->maps, s->use_tma, op, s->stream));
+  else KL(fdtdk_half_e(&s->dev, s->maps, s->use_tma, op, s->stream));
   return FDTD_OK;
 }
 
@@ -2435,6 +2458,8 @@ int fdtd_get_info(fdtd_handle h, fdtd_info *o) {
   o->hcoef_mode = s->hcoef_mode;
   o->fused = s->fused && s->fmaps[0].valid && s->fmaps[1].valid;
   o->zchunk_f = s->zc_f;
+  o->tile_h = s->tile_h;
+  o->tile_e = s->tile_e;
   return FDTD_OK;
 }
 
@@ -2679,7 +2704,7 @@ int fdtd_batch_add(fdtd_batch bh, fdtd_handle h, int32_t first, int32_t count, i
   sim *s = lookup(h);
   if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "invalid simulation handle");
   if (!s->init_ready) return fail(FDTD_ERR_STATE, "batch members need ReadySimulation");
-  if (!s->maps_b.valid) return fail(FDTD_ERR_UNSUPPORTED, "batch members need the TMA kernels");
+  if (!s->maps[1].valid) return fail(FDTD_ERR_UNSUPPORTED, "batch members need the TMA kernels");
   if (s->hcoef_mode)
     return fail(FDTD_ERR_UNSUPPORTED, "batch members need uniform H coefficients (no SetMagnetic)");
   /* a work item packs its first z-plane into 16 bits (add_items) */
@@ -2836,7 +2861,7 @@ static int batch_rebuild(batch *b) {
     sim *s = lookup(m->h);
     b->act[g] = i;
     b->h_devs[g] = s->dev;
-    memcpy(b->h_maps + (size_t)g * mapsz, s->maps_b.bytes, mapsz);
+    memcpy(b->h_maps + (size_t)g * mapsz, s->maps[1].bytes, mapsz);
     fdtd_op *op = &b->h_ops[g];
     memset(op, 0, sizeof(*op));
     op->curl = 1;

@@ -88,13 +88,18 @@ typedef struct {
   const float *hc;
   const uint16_t *hmat;
   const float *hmat_tab;
-  int32_t pad_[2];          /* size: a multiple of 16 bytes (bulk copies) */
+  /* tile geometry of the single-grid H and E curl kernels (autotuned):
+   * 0 64 x 8, 1 32 x 16, 2 128 x 4 (size: a multiple of 16 bytes) */
+  int32_t tile_h, tile_e;
 } fdtd_dev;
 
-/* TMA descriptors (CUtensorMap, 128 B each) of one grid: 0..5 = Ex Ey Ez Hx
- * Hy Hz as E-half-step boxes, 6..11 the same arrays as H-half-step boxes,
- * 12 = material ids.  Opaque to C. */
+/* TMA descriptors (CUtensorMap, 128 B each) of one grid in one tile
+ * geometry: 0..5 = Ex Ey Ez Hx Hy Hz as E-half-step boxes, 6..11 the same
+ * arrays as H-half-step boxes, 12 = material ids.  Opaque to C.  A handle
+ * holds one set per geometry (FDTD_NUM_TILES: 64 x 8, 32 x 16 -- also the
+ * batched kernels' -- and 128 x 4). */
 #define FDTD_NUM_MAPS 13
+#define FDTD_NUM_TILES 3
 #ifdef __cplusplus
 #define FDTD_ALIGN64 alignas(64)
 #else
@@ -209,18 +214,18 @@ static inline int fdtd_fused_ok(const fdtd_dev *d, const fdtd_op *op) {
   return d->i0 <= d->i1 && d->j0 <= d->j1 && d->k0 <= d->k1;
 }
 
-/* Launchers (fdtd_kernels.cu).  Return cudaError_t as int.  With valid
- * maps and op->curl set, the TMA-pipelined kernels run (fdtd_tma.cu);
- * otherwise the direct kernels.  use_tma = 0 forces the direct kernels. */
+/* Launchers (fdtd_kernels.cu).  Return cudaError_t as int.  m: the maps
+ * of every tile geometry (FDTD_NUM_TILES).  With valid maps and op->curl
+ * set, the TMA-pipelined kernels run (fdtd_tma.cu) in the descriptor's
+ * tile geometries; otherwise the direct kernels.  use_tma = 0 forces the
+ * direct kernels. */
 int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s);
 int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s);
-/* Encodes the TMA descriptors for the current device pointers (fdtd_tma.cu):
- * the single-grid kernels' boxes (FDTD_TILE_X x FDTD_TILE_Y tiles) and the
- * batched kernels' (FDTD_BTILE_X x FDTD_BTILE_Y). */
-int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m);
-int fdtdk_make_maps_batch(const fdtd_dev *d, fdtd_maps *m);
+/* Encodes the TMA descriptors for the current device pointers in tile
+ * geometry `tile` (fdtd_tma.cu; tile 1 is the batched kernels'). */
+int fdtdk_make_maps(const fdtd_dev *d, int tile, fdtd_maps *m);
 int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s);
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s);
 /* The E CPML X corrections over the x-slab cells of a grid whose curl kernel

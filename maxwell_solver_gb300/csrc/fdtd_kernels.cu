@@ -902,7 +902,7 @@ static int half_oblique(int hfam, const fdtd_dev *d, const fdtd_maps *m, int use
 int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s) {
   if (op->tfsf_mode == FDTD_MODE_OBLIQUE) return half_oblique(1, d, m, use_tma, op, s);
-  if (use_tma && m && m->valid && op->curl) return fdtdk_half_h_tma(d, m, op, s);
+  if (use_tma && m && m[0].valid && op->curl) return fdtdk_half_h_tma(d, m, op, s);
   const int ni = d->I - 1, nj = d->J - 1, nk = d->K - 1;
   if (op->curl && op->pml) return launch_half(k_half_h<true, true>, d, op, s, ni, nj, nk);
   if (op->curl) return launch_half(k_half_h<true, false>, d, op, s, ni, nj, nk);
@@ -914,7 +914,7 @@ int fdtdk_half_h(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_
 int fdtdk_half_e(const fdtd_dev *d, const fdtd_maps *m, int use_tma, const fdtd_op *op,
                  cudaStream_t s) {
   if (op->tfsf_mode == FDTD_MODE_OBLIQUE) return half_oblique(0, d, m, use_tma, op, s);
-  if (use_tma && m && m->valid && op->curl) return fdtdk_half_e_tma(d, m, op, s);
+  if (use_tma && m && m[0].valid && op->curl) return fdtdk_half_e_tma(d, m, op, s);
   const int ni = d->I, nj = d->J, nk = d->K;
   if (op->curl && op->pml) return launch_half(k_half_e<true, true>, d, op, s, ni, nj, nk);
   if (op->curl) return launch_half(k_half_e<true, false>, d, op, s, ni, nj, nk);

@@ -115,10 +115,15 @@ struct Geo {
   static_assert((HW * 4) % 16 == 0 && (BX * 4) % 16 == 0 && (BX * 2) % 16 == 0,
                 "TMA inner box extents must be multiples of 16 bytes");
 };
-using GS = Geo<64, 8>;   // single-grid kernels
-using GB = Geo<32, 16>;  // batched kernels
+using GS = Geo<64, 8>;   // single-grid kernels (tile 0, the default)
+using GB = Geo<32, 16>;  // batched kernels; single-grid tile 1 (narrow grids)
+using GW = Geo<128, 4>;  // single-grid tile 2 (wide grids)
 template <bool BATCH>
 using GeoOf = typename std::conditional<BATCH, GB, GS>::type;
+// The single-grid tile geometry by index (fdtd_dev::tile_e / tile_h).
+template <int T>
+using TileGeo = typename std::conditional<T == 0, GS,
+                                          typename std::conditional<T == 1, GB, GW>::type>::type;
 constexpr int kSmemTabMax = 512;             // coefficient ids staged in shared memory
 constexpr int CTRL_B = 512;                  // barriers + stage metadata
 // Batch mode: every stage also carries its grid's descriptor and op (bulk
@@ -131,21 +136,23 @@ constexpr int kStageTabMax = 64;
 constexpr int TAB_B = kStageTabMax * 6 * 4;  // 1536 B
 static_assert(sizeof(fdtd_dev) <= DESC_B && sizeof(fdtd_dev) % 16 == 0, "descriptor slot");
 static_assert(sizeof(fdtd_op) <= OPSLOT_B && sizeof(fdtd_op) % 16 == 0, "op slot");
-template <bool BATCH>
+template <bool BATCH, class G = GeoOf<BATCH>>
 struct EG {
   static constexpr int NS = BATCH ? kBatchNS : NSE;
   static constexpr int STAGE =
-      BATCH ? GB::E_STAGE + DESC_B + OPSLOT_B + TAB_B : GS::E_STAGE;
+      BATCH ? G::E_STAGE + DESC_B + OPSLOT_B + TAB_B : G::E_STAGE;
   static constexpr int SMEM = NS * STAGE + CTRL_B + (BATCH ? 0 : kSmemTabMax * 6 * 4);
 };
-template <bool BATCH>
+template <bool BATCH, class G = GeoOf<BATCH>>
 struct HG {
   static constexpr int NS = BATCH ? kBatchNSH : NSH;
-  static constexpr int STAGE = BATCH ? GB::H_STAGE + DESC_B + OPSLOT_B : GS::H_STAGE;
+  static constexpr int STAGE = BATCH ? G::H_STAGE + DESC_B + OPSLOT_B : G::H_STAGE;
   static constexpr int SMEM = NS * STAGE + CTRL_B;
 };
 constexpr int E_SMEM = EG<false>::SMEM;
 constexpr int H_SMEM = HG<false>::SMEM;
+static_assert(EG<false, GW>::STAGE % 128 == 0 && HG<false, GW>::STAGE % 128 == 0,
+              "stage alignment");
 static_assert(EG<true>::STAGE % 128 == 0 && HG<true>::STAGE % 128 == 0, "batch stage alignment");
 static_assert(kBatchMinBlocks * (EG<true>::SMEM + 1024) <= 228 * 1024 &&
                   kBatchMinBlocksH * (HG<true>::SMEM + 1024) <= 228 * 1024,
@@ -193,7 +200,7 @@ __global__ void k_check_wait(long long *out, int arrive) {
     out[0] = ok ? 0 : 1;
   }
 }
-template <bool BATCH>
+template <bool BATCH, class G>
 __device__ __forceinline__ void decode_item(const Items &it, int w, int &g, int &x0, int &y0,
                                             int &kb, int &np) {
   if (BATCH) {
@@ -207,8 +214,8 @@ __device__ __forceinline__ void decode_item(const Items &it, int w, int &g, int 
     const int nt = it.tiles_x * it.tiles_y;
     const int chunk = w / nt, tile = w - chunk * nt;
     g = 0;
-    x0 = (tile % it.tiles_x) * GS::BX;
-    y0 = (tile / it.tiles_x) * GS::BY;
+    x0 = (tile % it.tiles_x) * G::BX;
+    y0 = (tile / it.tiles_x) * G::BY;
     kb = chunk * it.zchunk;
     np = min(it.zchunk, it.nk - kb);
   }
@@ -223,7 +230,7 @@ __device__ __forceinline__ void decode_item(const Items &it, int w, int &g, int 
 // top down; issue() is told which loads are such extra planes.
 // Ends with a sentinel stage, rewinds the work counter when it is the last
 // producer, and waits for its own copies before returning.
-template <int NS, bool BATCH, bool DOWN, class StepFn, class IssueFn>
+template <int NS, bool BATCH, bool DOWN, class G, class StepFn, class IssueFn>
 __device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *empty, int4 *meta,
                         StepFn step_of, IssueFn issue) {
   int q = 0;
@@ -232,7 +239,7 @@ __device__ void produce(const Items &it, int extra, uint64_t *full, uint64_t *em
     const int w = atomicAdd(&it.work[0], 1);
     if (w >= it.n_items) break;
     int g, x0, y0, kb, np;
-    decode_item<BATCH>(it, w, g, x0, y0, kb, np);
+    decode_item<BATCH, G>(it, w, g, x0, y0, kb, np);
     const int step = step_of(g);
     for (int t = 0; t < np + extra && ok; ++t, ++q) {
       const int s = q % NS;
@@ -315,15 +322,15 @@ __device__ __forceinline__ void stage_writes_fence() {
 // each of its two rows) leave their Ey, Ez in the stage's E tile, and
 // then the warp's lanes take them one per lane.  Without XC the x-slab pass
 // (k_e_xslab) applies them after the kernel.
-template <bool PML, bool BATCH, bool LEAN = false, bool XC = false>
+template <bool PML, bool BATCH, bool LEAN = false, bool XC = false, class GT = GeoOf<BATCH>>
 __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_E)
     k_half_e_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   static_assert(!XC || (LEAN && PML), "compacted CPML X needs the lean kernel with CPML");
   extern __shared__ __align__(128) unsigned char smem[];
-  using G = GeoOf<BATCH>;
-  constexpr int ST = EG<BATCH>::STAGE;
-  constexpr int NS = EG<BATCH>::NS;
+  using G = GT;
+  constexpr int ST = EG<BATCH, G>::STAGE;
+  constexpr int NS = EG<BATCH, G>::NS;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * ST);
   uint64_t *empty = full + NS;
   int4 *meta = reinterpret_cast<int4 *>(empty + NS);
@@ -359,7 +366,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
       const auto step_of = [&](int g) {
         return (BATCH ? it.steps[g] + it.ops[g].step : op_step(d0, op0));
       };
-      produce<NS, BATCH, false>(it, 0, full, empty, meta, step_of, [&](int s, int g, int x0,
+      produce<NS, BATCH, false, G>(it, 0, full, empty, meta, step_of, [&](int s, int g, int x0,
                                                                          int y0, int k, bool) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
         if (BATCH && g != g_um) {
@@ -572,15 +579,16 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocks : FDTD_MIN_BLOCKS_
 // x-slab cells leave their Hy, Hz in the stage's H tile and the warp's
 // lanes then take them one per lane, instead of every row of a warp that
 // holds a few x-slab lanes taking the correction path.
-template <bool PML, bool BATCH, bool MU = false, bool LEAN = false, bool XC = false>
+template <bool PML, bool BATCH, bool MU = false, bool LEAN = false, bool XC = false,
+          class GT = GeoOf<BATCH>>
 __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_MIN_BLOCKS_H))
     k_half_h_tma(const __grid_constant__ fdtd_dev d0, const __grid_constant__ fdtd_op op0,
                  const __grid_constant__ Maps mp, const Items it) {
   static_assert(!XC || (LEAN && PML && !MU), "compacted CPML X needs the lean kernel with CPML");
   extern __shared__ __align__(128) unsigned char smem[];
-  using G = GeoOf<BATCH>;
-  constexpr int ST = HG<BATCH>::STAGE;
-  constexpr int NS = HG<BATCH>::NS;
+  using G = GT;
+  constexpr int ST = HG<BATCH, G>::STAGE;
+  constexpr int NS = HG<BATCH, G>::NS;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * ST);
   uint64_t *empty = full + NS;
   int4 *meta = reinterpret_cast<int4 *>(empty + NS);
@@ -612,7 +620,7 @@ __global__ void __launch_bounds__(NT, BATCH ? kBatchMinBlocksH : (MU ? 3 : FDTD_
       };
       // planes from the top down; the item's first load is plane kb + np,
       // of which the consumers read Ex and Ey of their own cells
-      produce<NS, BATCH, true>(it, 1, full, empty, meta, step_of, [&](int s, int g, int x0,
+      produce<NS, BATCH, true, G>(it, 1, full, empty, meta, step_of, [&](int s, int g, int x0,
                                                                        int y0, int k,
                                                                        bool above) {
         const CUtensorMap *mm = BATCH ? it.maps + (int64_t)g * FDTD_NUM_MAPS : mp.m;
@@ -841,7 +849,7 @@ inline int pick_zchunk(int tiles, int nk, int blocks) {
   return z;
 }
 
-template <class KH>
+template <class G = GS, class KH>
 int launch(KH kern, int smem, int *cached_blocks, const fdtd_dev *d, const fdtd_maps *m,
            const fdtd_op *op, cudaStream_t s, int ni, int nj, int nk, int zc_tuned) {
   static_assert(sizeof(Maps) == sizeof(((fdtd_maps *)0)->bytes), "map layout");
@@ -862,8 +870,8 @@ int launch(KH kern, int smem, int *cached_blocks, const fdtd_dev *d, const fdtd_
   memset(&it, 0, sizeof(it));
   it.work = d->work;
   it.err = d->err;
-  it.tiles_x = (ni + GS::BX - 1) / GS::BX;
-  it.tiles_y = (nj + GS::BY - 1) / GS::BY;
+  it.tiles_x = (ni + G::BX - 1) / G::BX;
+  it.tiles_y = (nj + G::BY - 1) / G::BY;
   it.nk = nk;
   it.zchunk = pick_zchunk(it.tiles_x * it.tiles_y, nk, *cached_blocks);
   if (zc_tuned > 0 && !getenv("FDTD_TMA_ZCHUNK")) it.zchunk = zc_tuned < nk ? zc_tuned : nk;
@@ -935,15 +943,60 @@ int make_maps(const fdtd_dev *d, fdtd_maps *m) {
 }
 
 
+// The single-grid CPML curl kernels in the tile geometry T (maps: one set
+// per geometry; blocks per SM cached per instance).
+template <bool LEAN, int T>
+int launch_e_pml(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *o, cudaStream_t s) {
+  using G = TileGeo<T>;
+  static int blocks = 0;
+  return launch<G>(k_half_e_tma<true, false, LEAN, false, G>, EG<false, G>::SMEM, &blocks, d,
+                   &m[T], o, s, d->I, d->J, d->K, d->zc_e);
+}
+template <bool LEAN, int T>
+int launch_h_pml(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *o, cudaStream_t s) {
+  using G = TileGeo<T>;
+  static int blocks = 0;
+  return launch<G>(k_half_h_tma<true, false, false, LEAN, false, G>, HG<false, G>::SMEM, &blocks,
+                   d, &m[T], o, s, d->I - 1, d->J - 1, d->K - 1, d->zc_h);
+}
+// The tile the autotuner chose (when its maps encoded), else 64 x 8.
+inline int tile_of(int t, const fdtd_maps *m) {
+  return (t >= 0 && t < FDTD_NUM_TILES && m[t].valid) ? t : 0;
+}
+template <bool LEAN>
+int launch_e_tiled(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *o, cudaStream_t s) {
+  switch (tile_of(d->tile_e, m)) {
+    case 1: return launch_e_pml<LEAN, 1>(d, m, o, s);
+    case 2: return launch_e_pml<LEAN, 2>(d, m, o, s);
+    default: return launch_e_pml<LEAN, 0>(d, m, o, s);
+  }
+}
+template <bool LEAN>
+int launch_h_tiled(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *o, cudaStream_t s) {
+  switch (tile_of(d->tile_h, m)) {
+    case 1: return launch_h_pml<LEAN, 1>(d, m, o, s);
+    case 2: return launch_h_pml<LEAN, 2>(d, m, o, s);
+    default: return launch_h_pml<LEAN, 0>(d, m, o, s);
+  }
+}
+
 }  // namespace
 
 extern "C" {
 
-int fdtdk_make_maps(const fdtd_dev *d, fdtd_maps *m) { return make_maps<GS>(d, m); }
-int fdtdk_make_maps_batch(const fdtd_dev *d, fdtd_maps *m) { return make_maps<GB>(d, m); }
+int fdtdk_make_maps(const fdtd_dev *d, int tile, fdtd_maps *m) {
+  switch (tile) {
+    case 0: return make_maps<GS>(d, m);
+    case 1: return make_maps<GB>(d, m);
+    case 2: return make_maps<GW>(d, m);
+  }
+  m->valid = 0;
+  return (int)cudaErrorInvalidValue;
+}
 
 // The curl kernel, then the x-slab pass (CPML X, when it can be split off)
-// and the face pass (TF/SF, when it can): their cells are disjoint.
+// and the face pass (TF/SF, when it can): their cells are disjoint.  m: the
+// maps of every tile geometry (FDTD_NUM_TILES).
 int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, cudaStream_t s) {
   fdtd_op o = *op;
   o.tfsf_split = fdtd_tfsf_split(d, op);
@@ -956,13 +1009,11 @@ int fdtdk_half_e_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
                K, d->zc_e);
     xslab_pass = false;  // the kernel applied CPML X
   } else if (fdtd_e_lean(&o))
-    e = o.pml ? launch(k_half_e_tma<true, false, true>, E_SMEM, &g_blocks_e[3], d, m, &o, s, I,
-                       J, K, d->zc_e)
+    e = o.pml ? launch_e_tiled<true>(d, m, &o, s)
               : launch(k_half_e_tma<false, false, true>, E_SMEM, &g_blocks_e[2], d, m, &o, s, I,
                        J, K, d->zc_e);
   else
-    e = o.pml ? launch(k_half_e_tma<true, false>, E_SMEM, &g_blocks_e[1], d, m, &o, s, I, J, K,
-                       d->zc_e)
+    e = o.pml ? launch_e_tiled<false>(d, m, &o, s)
               : launch(k_half_e_tma<false, false>, E_SMEM, &g_blocks_e[0], d, m, &o, s, I, J, K,
                        d->zc_e);
   if (!e) fdtdk_profile_mark(s);
@@ -985,13 +1036,11 @@ int fdtdk_half_h_tma(const fdtd_dev *d, const fdtd_maps *m, const fdtd_op *op, c
     e = launch(k_half_h_tma<true, false, false, true, true>, H_SMEM, &g_blocks_h[6], d, m, &o, s,
                ni, nj, nk, d->zc_h);
   else if (fdtd_h_lean(&o))
-    e = o.pml ? launch(k_half_h_tma<true, false, false, true>, H_SMEM, &g_blocks_h[5], d, m, &o,
-                       s, ni, nj, nk, d->zc_h)
+    e = o.pml ? launch_h_tiled<true>(d, m, &o, s)
               : launch(k_half_h_tma<false, false, false, true>, H_SMEM, &g_blocks_h[4], d, m, &o,
                        s, ni, nj, nk, d->zc_h);
   else
-    e = o.pml ? launch(k_half_h_tma<true, false>, H_SMEM, &g_blocks_h[1], d, m, &o, s, ni, nj,
-                       nk, d->zc_h)
+    e = o.pml ? launch_h_tiled<false>(d, m, &o, s)
               : launch(k_half_h_tma<false, false>, H_SMEM, &g_blocks_h[0], d, m, &o, s, ni, nj,
                        nk, d->zc_h);
   if (!e) fdtdk_profile_mark(s);
