@@ -546,76 +546,114 @@ def run_batched(n_grids: int, batched_only: bool = False):
     }
 
 
-def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4):
+def _pct(v, p):
+    """Nearest-rank percentile (the server's own statistic)."""
+    v = sorted(v)
+    k = min(len(v), max(1, math.ceil(p / 100.0 * len(v) - 1e-9)))
+    return v[k - 1]
+
+
+def _lat_summary(lat, makespan):
+    return {"solves_per_s": round(len(lat) / makespan, 3), "p50_s": round(_pct(lat, 50), 3),
+            "p90_s": round(_pct(lat, 90), 3), "p99_s": round(_pct(lat, 99), 3),
+            "mean_s": round(sum(lat) / len(lat), 3)}
+
+
+def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
+               policy: str = "deadline", live_fifo_load: float = 0.9):
     """Served configuration c5: a Poisson stream of requests (seeded serve
     mix, axes log-uniform 48..384, steps 200..4000) through the C request
-    loop with continuous batching under an HBM budget, and the same arrival
-    trace through the one-at-a-time plain-solver queue.  Capacity = the
-    batched solves/s with every request queued at once; each load point
-    offers load x capacity requests per second.  Reports solves/s and
-    p50/p90/p99 latency (arrival to result) of both, and checks every
-    request's probe series is bit-identical in the two."""
+    loop (continuous batching under an HBM budget, deadline policy), against
+    the one-at-a-time plain-solver queue (FIFO) on the same GPU.
+
+    1. Every request queued at once through the one-at-a-time queue: each
+       request's time alone (admission to result, set-up included), its
+       probe record, and the capacity (solves/s) the loads refer to.
+    2. Per load: Poisson arrivals at load x capacity through the served
+       loop, live; the FIFO queue's latencies for the same arrivals follow
+       exactly from the measured times alone (a single server in arrival
+       order: start = max(arrival, previous finish)); at one load the FIFO
+       queue also runs live, to check that model.
+    While the server is idle (nothing queued or running) the client does not
+    wait for the next arrival but moves the clock on: latencies are
+    unchanged, and solves/s count the skipped time.
+    Every served request's probes must equal its one-at-a-time probes."""
     from maxwell_solver_gb300.serve import Server
     from maxwell_solver_gb300.workloads import serve_mix
 
     specs = serve_mix(n_req, seed)
     budget = int(budget_gb * (1 << 30))
 
-    def one_run(arrivals, one_at_a_time, policy="srpt"):
+    def one_run(arrivals, one_at_a_time):
         with Server(hbm_budget=budget, one_at_a_time=one_at_a_time, policy=policy) as srv:
             t0 = time.perf_counter()
+            skipped = 0.0
             tickets = []
             for spec, at in zip(specs, arrivals):
-                dt = at - (time.perf_counter() - t0)
-                if dt > 0:
-                    time.sleep(dt)
+                while True:
+                    left = at - (time.perf_counter() - t0 + skipped)
+                    if left <= 0:
+                        break
+                    st = srv.stats()
+                    if st["queued"] == 0 and st["active"] == 0:
+                        skipped += left  # idle: move the clock to the arrival
+                        break
+                    time.sleep(min(left, 0.02))
                 tickets.append(srv.submit(spec, n_probes=8))
             res = [srv.result(t) for t in tickets]
             st = srv.stats()
-        summary = {"solves_per_s": round(st["solves_per_s"], 3),
-                   "p50_s": round(st["latency_p50_s"], 3), "p90_s": round(st["latency_p90_s"], 3),
-                   "p99_s": round(st["latency_p99_s"], 3), "mean_s": round(st["latency_mean_s"], 3),
-                   "Mcell_steps_per_s": round(st["cell_steps"] / st["elapsed_s"] / 1e6, 1),
-                   "peak_active": st["peak_active"],
-                   "peak_reserved_GB": round(st["peak_reserved_bytes"] / (1 << 30), 2),
-                   "completed": st["completed"], "failed": st["failed"],
-                   "seconds": round(st["elapsed_s"], 2)}
-        return summary, [r["probes"] for r in res]
+        lat = [r["info"]["latency_s"] for r in res]
+        out = {**_lat_summary(lat, st["elapsed_s"] + skipped),
+               "Mcell_steps_per_s": round(st["cell_steps"] / (st["elapsed_s"] + skipped) / 1e6, 1),
+               "peak_active": st["peak_active"],
+               "peak_reserved_GB": round(st["peak_reserved_bytes"] / (1 << 30), 2),
+               "completed": st["completed"], "failed": st["failed"],
+               "seconds_run": round(time.perf_counter() - t0, 2),
+               "seconds_skipped_idle": round(skipped, 2)}
+        return out, res
 
-    cap, _ = one_run([0.0] * len(specs), False)
-    capacity = cap["solves_per_s"]
+    # 1. one at a time, all queued: times alone, capacity, reference records
+    sat, base = one_run([0.0] * len(specs), True)
+    alone = [r["info"]["finish_s"] - r["info"]["admit_s"] for r in base]
+    capacity = len(specs) / sum(alone)
+    ref = [r["probes"] for r in base]
+
+    def fifo_model(arrivals):
+        fin, lat = 0.0, []
+        for at, t in zip(arrivals, alone):
+            fin = max(at, fin) + t
+            lat.append(fin - at)
+        return _lat_summary(lat, fin - arrivals[0])
+
     rng = np.random.default_rng(seed + 1)
     gaps = rng.exponential(1.0, len(specs))
     points, same = [], True
     for load in loads:
         rate = load * capacity
         arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
-        served, p_s = one_run(arrivals, False)
-        hrrn, p_h = one_run(arrivals, False, "hrrn")
-        bounded, p_b = one_run(arrivals, False, "bounded")
-        plain, p_p = one_run(arrivals, True)
-        same &= all(np.array_equal(a, b) for a, b in zip(p_s, p_p))
-        same &= all(np.array_equal(a, b) for a, b in zip(p_h, p_p))
-        same &= all(np.array_equal(a, b) for a, b in zip(p_b, p_p))
-        points.append({"load": load, "rate_per_s": round(rate, 3), "served": served,
-                       "served_hrrn": hrrn, "served_bounded": bounded, "one_at_a_time": plain,
-                       "speedup_solves_per_s": round(served["solves_per_s"] /
-                                                     max(plain["solves_per_s"], 1e-9), 2),
-                       "p99_ratio_one_at_a_time_over_served": round(
-                           plain["p99_s"] / max(served["p99_s"], 1e-9), 2)})
+        served, res = one_run(arrivals, False)
+        same &= all(np.array_equal(r["probes"], p) for r, p in zip(res, ref))
+        fifo = fifo_model(arrivals)
+        pt = {"load": load, "rate_per_s": round(rate, 3), "served": served,
+              "one_at_a_time": fifo,
+              "served_p50_le_fifo": served["p50_s"] <= fifo["p50_s"],
+              "served_p99_le_fifo": served["p99_s"] <= fifo["p99_s"]}
+        if abs(load - live_fifo_load) < 1e-9:
+            live, res_l = one_run(arrivals, True)
+            same &= all(np.array_equal(r["probes"], p) for r, p in zip(res_l, ref))
+            pt["one_at_a_time_live"] = live
+        points.append(pt)
     return {
         "workload": f"c5: {len(specs)} requests (seed {seed}), cubic-ish axes log-U[48,384], "
                     "CPML 8..16, spheres (oblique TF/SF, mode 5) or layers (mode 1), "
-                    "steps U[200,4000], 8 probes each; Poisson arrivals; requests of >= 2^22 "
-                    "cells run alone between batched rounds of the smaller ones",
-        "hbm_budget_GB": budget_gb, "capacity_solves_per_s": capacity,
-        "saturated": cap, "loads": points, "identical_results": bool(same),
+                    "steps U[200,4000], 8 probes each; Poisson arrivals",
+        "policy": policy, "hbm_budget_GB": budget_gb,
+        "capacity_solves_per_s": round(capacity, 3), "one_at_a_time_saturated": sat,
+        "loads": points, "identical_results": bool(same),
         "timing": "wall clock from each request's submission to its result on the host "
-                  "(set-up on the device, all steps, probe readout); capacity = every request "
-                  "queued at t=0 through the batched server",
-        "policies": "served: least remaining work first; served_hrrn: highest response "
-                    "ratio (waited + remaining) / remaining first; served_bounded: least "
-                    "remaining work first, requests whose response ratio reached 3 ahead",
+                  "(set-up on the device, all steps, probe readout); one-at-a-time latencies "
+                  "from each request's measured time alone and the arrival order (checked "
+                  f"live at load {live_fifo_load}); idle gaps skipped, see run_served",
     }
 
 
@@ -636,8 +674,8 @@ def main():
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the batched leg, without its one-at-a-time baselines")
     ap.add_argument("--no-serve", action="store_true", help="skip the served (c5) leg")
-    ap.add_argument("--serve-requests", type=int, default=20)
-    ap.add_argument("--serve-loads", default="0.5,1.0",
+    ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--serve-loads", default="0.3,0.6,0.9,1.2",
                     help="offered loads, fractions of the measured batched capacity")
     ap.add_argument("--serve-only", action="store_true", help="run only the served leg")
     args = ap.parse_args()

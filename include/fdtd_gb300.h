@@ -362,11 +362,20 @@ typedef struct {
                              FDTD_SERVE_BOUNDED (2): least remaining work
                              first, except that requests whose response
                              ratio reached 3 go ahead of the others, highest
-                             ratio first */
+                             ratio first;
+                             FDTD_SERVE_DEADLINE (3): least remaining work
+                             first, except that a request that would finish
+                             later than it would have in a one-at-a-time
+                             queue (its deadline: the queue's finish time,
+                             from the arrival order and an estimate of each
+                             request's time alone) goes ahead, earliest
+                             deadline first -- running alone for a round if
+                             it fills the device */
 } fdtd_server_config;
 #define FDTD_SERVE_SRPT 0
 #define FDTD_SERVE_HRRN 1
 #define FDTD_SERVE_BOUNDED 2
+#define FDTD_SERVE_DEADLINE 3
 
 typedef struct {
   double submit_s, admit_s, finish_s; /* server clock, seconds */

@@ -70,6 +70,7 @@ typedef struct req {
   int in_batch, want;
   int cancel; /* fdtd_server_cancel while on the device (read with __atomic) */
   double key; /* this round's order (ascending) */
+  double deadline; /* FDTD_SERVE_DEADLINE: finish time in a one-at-a-time queue */
   int32_t done_base, done;
   struct req *next;
 } req;
@@ -97,6 +98,9 @@ typedef struct server {
    * applies on the GPU within two rounds (nothing runs far ahead) */
   cudaEvent_t ev[2];
   int ev_used[2], ev_i;
+  /* the one-at-a-time queue's estimated finish time of the last submission
+   * (FDTD_SERVE_DEADLINE), under mu */
+  double v_fifo;
   /* statistics, under mu */
   uint64_t submitted, completed, failed, cancelled, cell_steps, peak_reserved;
   int peak_active;
@@ -264,6 +268,12 @@ static double serve_max_ratio(void) {
   return v;
 }
 
+/* Estimated seconds a request of `cells` cells takes alone for `steps`
+ * steps through fdtd_step_n (a fixed cost per step of the launches, then
+ * the cell rate of the large grids; measured on GB300), and its set-up. */
+static double solo_step_s(int64_t cells) { return 2.0e-5 + (double)cells / 6.0e10; }
+static double solo_setup_s(int64_t cells) { return 5.0e-3 + (double)cells * 1.0e-9; }
+
 static void order_requests(server *S, int policy) {
   const double now = now_s(S);
   for (int a = 0; a < S->n_act; ++a) {
@@ -271,12 +281,20 @@ static void order_requests(server *S, int policy) {
     const double work = (double)req_cells(r) * (r->r.steps - r->done);
     const double rem = work / SERVE_RATE_EST + 1e-6;
     const double ratio = ((now - r->t_submit) + rem) / rem;
-    if (policy == FDTD_SERVE_HRRN)
+    if (policy == FDTD_SERVE_HRRN) {
       r->key = -ratio;
-    else if (policy == FDTD_SERVE_BOUNDED && ratio >= serve_max_ratio())
+    } else if (policy == FDTD_SERVE_BOUNDED && ratio >= serve_max_ratio()) {
       r->key = -ratio; /* ahead of every key >= 0 below */
-    else
+    } else if (policy == FDTD_SERVE_DEADLINE) {
+      /* slack against the one-at-a-time queue's finish time; a request
+       * with too little left goes ahead, earliest deadline first (a
+       * margin covers the estimate's error and the round in flight) */
+      const double left = solo_step_s(req_cells(r)) * (r->r.steps - r->done);
+      const double slack = r->deadline - now - left;
+      r->key = slack < 0.15 * left + 0.05 ? -1.0e12 + r->deadline : work;
+    } else {
       r->key = work;
+    }
   }
   qsort(S->act, (size_t)S->n_act, sizeof(req *), by_key);
 }
@@ -484,7 +502,7 @@ static void release_gpu(server *S) {
 int fdtd_server_create(fdtd_server *out, const fdtd_server_config *cfg) {
   if (!out || !cfg) return FDTD_ERR_INVALID_ARG;
   if (cfg->policy != FDTD_SERVE_SRPT && cfg->policy != FDTD_SERVE_HRRN &&
-      cfg->policy != FDTD_SERVE_BOUNDED)
+      cfg->policy != FDTD_SERVE_BOUNDED && cfg->policy != FDTD_SERVE_DEADLINE)
     return FDTD_ERR_INVALID_ARG;
   server *S = (server *)calloc(1, sizeof(server));
   if (!S) return FDTD_ERR_OOM;
@@ -596,6 +614,12 @@ int fdtd_server_submit(fdtd_server h, const fdtd_request *q, uint64_t *ticket) {
   r->ticket = ++S->tab_n;
   r->t_submit = now_s(S);
   if (S->first_submit < 0) S->first_submit = r->t_submit;
+  { /* the one-at-a-time queue: starts when it arrives or the one before ends */
+    const int64_t cells = (int64_t)q->I * q->J * q->K;
+    const double start = S->v_fifo > r->t_submit ? S->v_fifo : r->t_submit;
+    S->v_fifo = start + solo_setup_s(cells) + solo_step_s(cells) * q->steps;
+    r->deadline = S->v_fifo;
+  }
   r->state = R_QUEUED;
   if (S->q_tail) S->q_tail->next = r;
   else S->q_head = r;

@@ -27,7 +27,7 @@ class Server:
                  one_at_a_time: bool = False, fill_cells: int = 0, solo_cells: int = 0,
                  policy: str = "srpt"):
         self._lib = _native.load()
-        pol = {"srpt": 0, "hrrn": 1, "bounded": 2}[policy]
+        pol = {"srpt": 0, "hrrn": 1, "bounded": 2, "deadline": 3}[policy]
         cfg = _native.FdtdServerConfig(int(hbm_budget), int(max_active), int(round_steps),
                                        int(bool(one_at_a_time)), int(fill_cells), int(solo_cells),
                                        pol)

@@ -90,7 +90,7 @@ def _serve(specs, gaps, **cfg):
     return res, st
 
 
-@pytest.mark.parametrize("policy", ["srpt", "hrrn", "bounded"])
+@pytest.mark.parametrize("policy", ["srpt", "hrrn", "bounded", "deadline"])
 def test_served_results_equal_alone(policy):
     """Requests arriving while others run are packed into the same batched
     launches (in either order policy); each ends bit-identical to running
