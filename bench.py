@@ -361,8 +361,11 @@ def run_ours(args, ranks):
         "traffic_source": tr.get("source"),
     }
 
-    # the batched, served and CPU legs: one GPU only (N = 1)
+    # the batched, served, per-cell coefficient and CPU legs: one GPU only (N = 1)
     solo = ranks.world == 1
+    coef_arrays = None
+    if solo and not args.no_coef_arrays:
+        coef_arrays = run_coef_arrays("c2", 200, 5)
     cpu = None
     if solo and not args.no_cpu:
         rate, done, secs, cores = cpu_oracle_rate(w, target_s=args.cpu_seconds, max_steps=2000)
@@ -402,6 +405,7 @@ def run_ours(args, ranks):
         "e2e": e2e,
         "clocks": clk,
         "gpu_launches": int(launches),
+        "coef_arrays": coef_arrays,
         "served": served,
         "batched": batched,
     }
@@ -411,6 +415,49 @@ def ctypes_float():
     import ctypes
 
     return ctypes.c_float(0.0)
+
+
+def run_coef_arrays(name: str, steps: int, warmup: int):
+    """The reference's coefficient layout: six per-cell E coefficient arrays
+    (FDTD_COEF=arrays; 60 B per cell in the E half-step) instead of 2-byte
+    material ids, on the named workload: Mcell-steps/s and the E kernel's
+    roofline in those bytes."""
+    import ctypes
+
+    from maxwell_solver_gb300 import _native, info, simFDTD
+    from maxwell_solver_gb300.simfdtd import _check
+    from maxwell_solver_gb300.workloads import WORKLOADS, setup
+
+    lib = _native.load()
+    w = WORKLOADS[name]
+    KP = 16
+    os.environ["FDTD_COEF"] = "arrays"
+    try:
+        P = setup(simFDTD, w, steps=warmup + steps + KP)
+    finally:
+        del os.environ["FDTD_COEF"]
+    h = int(P[0])
+    inf = info(P)
+    simFDTD("StepN", P, np.int32([0, warmup, w.mode]))
+    _check(lib.fdtd_event_record(h, 0))
+    simFDTD("StepN", P, np.int32([warmup, steps, w.mode]))
+    _check(lib.fdtd_event_record(h, 1))
+    simFDTD("Synchronize", P)
+    ms = ctypes_float()
+    _check(lib.fdtd_event_elapsed_ms(h, 0, 1, ms))
+    acc = (ctypes.c_float * 6)()
+    _check(lib.fdtd_profile_steps(h, warmup + steps, KP, w.mode, None, ctypes.byref(acc)))
+    simFDTD("DeleteSimulation", P)
+    peak, _ = measured_hbm_peak()
+    t_ec = acc[4] / KP
+    ach = REF_BYTES_E * w.cells / (t_ec / 1e3) / 1e9 if t_ec > 0 else 0.0
+    return {"workload": f"{w.name}: {w.dims[0]}x{w.dims[1]}x{w.dims[2]}, per-cell coefficient "
+                        "arrays (FDTD_COEF=arrays)",
+            "coef_mode": inf["coef_mode"], "steps": steps,
+            "value": round(w.cells * steps / (ms.value / 1e3) / 1e6, 2), "unit": "Mcell-steps/s",
+            "ms_per_step": round(ms.value / steps, 5),
+            "E_kernel": {"alg_bytes_per_cell": REF_BYTES_E, "avg_launch_ms": round(t_ec, 5),
+                         "achieved": round(ach, 1), "frac": round(ach / peak, 4)}}
 
 
 def run_e2e(w, K, simFDTD, materials, probe_locations, sources):
@@ -560,7 +607,7 @@ def _lat_summary(lat, makespan):
 
 
 def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
-               policy: str = "deadline", live_fifo_load: float = 0.9):
+               policy: str = "deadline"):
     """Served configuration c5: a Poisson stream of requests (seeded serve
     mix, axes log-uniform 48..384, steps 200..4000) through the C request
     loop (continuous batching under an HBM budget, deadline policy), against
@@ -570,10 +617,10 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
        request's time alone (admission to result, set-up included), its
        probe record, and the capacity (solves/s) the loads refer to.
     2. Per load: Poisson arrivals at load x capacity through the served
-       loop, live; the FIFO queue's latencies for the same arrivals follow
-       exactly from the measured times alone (a single server in arrival
-       order: start = max(arrival, previous finish)); at one load the FIFO
-       queue also runs live, to check that model.
+       loop and through the one-at-a-time queue, both live; beside them the
+       queue's latencies as they follow from the measured times alone (a
+       single server in arrival order: start = max(arrival, previous
+       finish)), for reference.
     While the server is idle (nothing queued or running) the client does not
     wait for the next arrival but moves the clock on: latencies are
     unchanged, and solves/s count the skipped time.
@@ -630,18 +677,19 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
     points, same = [], True
     for load in loads:
         rate = load * capacity
-        arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
+        arrivals = [float(x) for x in np.cumsum(gaps / rate) - gaps[0] / rate]
         served, res = one_run(arrivals, False)
         same &= all(np.array_equal(r["probes"], p) for r, p in zip(res, ref))
         fifo = fifo_model(arrivals)
-        pt = {"load": load, "rate_per_s": round(rate, 3), "served": served,
-              "one_at_a_time": fifo,
-              "served_p50_le_fifo": served["p50_s"] <= fifo["p50_s"],
-              "served_p99_le_fifo": served["p99_s"] <= fifo["p99_s"]}
-        if abs(load - live_fifo_load) < 1e-9:
-            live, res_l = one_run(arrivals, True)
-            same &= all(np.array_equal(r["probes"], p) for r, p in zip(res_l, ref))
-            pt["one_at_a_time_live"] = live
+        pt = {"load": load, "rate_per_s": round(rate, 3), "served": served}
+        live, res_l = one_run(arrivals, True)
+        same &= all(np.array_equal(r["probes"], p) for r, p in zip(res_l, ref))
+        pt["one_at_a_time"] = live
+        pt["one_at_a_time_model"] = fifo
+        pt["served_p50_le_fifo"] = bool(served["p50_s"] <= live["p50_s"])
+        pt["served_p99_le_fifo"] = bool(served["p99_s"] <= live["p99_s"])
+        pt["speedup_solves_per_s"] = round(served["solves_per_s"] / live["solves_per_s"], 3)
+        log(f"served load {load}: {json.dumps(pt)}")
         points.append(pt)
     return {
         "workload": f"c5: {len(specs)} requests (seed {seed}), cubic-ish axes log-U[48,384], "
@@ -651,9 +699,8 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
         "capacity_solves_per_s": round(capacity, 3), "one_at_a_time_saturated": sat,
         "loads": points, "identical_results": bool(same),
         "timing": "wall clock from each request's submission to its result on the host "
-                  "(set-up on the device, all steps, probe readout); one-at-a-time latencies "
-                  "from each request's measured time alone and the arrival order (checked "
-                  f"live at load {live_fifo_load}); idle gaps skipped, see run_served",
+                  "(set-up on the device, all steps, probe readout), served and one at a "
+                  "time both live; idle gaps skipped, see run_served",
     }
 
 
@@ -670,6 +717,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (c4) leg")
+    ap.add_argument("--no-coef-arrays", action="store_true",
+                    help="skip the per-cell coefficient array leg")
     ap.add_argument("--batch-grids", type=int, default=256)
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the batched leg, without its one-at-a-time baselines")

@@ -269,10 +269,19 @@ static double serve_max_ratio(void) {
 }
 
 /* Estimated seconds a request of `cells` cells takes alone for `steps`
- * steps through fdtd_step_n (a fixed cost per step of the launches, then
- * the cell rate of the large grids; measured on GB300), and its set-up. */
-static double solo_step_s(int64_t cells) { return 2.0e-5 + (double)cells / 6.0e10; }
-static double solo_setup_s(int64_t cells) { return 5.0e-3 + (double)cells * 1.0e-9; }
+ * steps through fdtd_step_n (a fixed cost per step of the launches, then a
+ * cell rate rising from 60 G cell-steps/s at 16 M cells to 80 G at 100 M;
+ * measured on GB300), and its set-up (rasterising, indexing, autotuning). */
+static double solo_step_s(int64_t cells) {
+  const double c = (double)cells, rate = 6.0e10 + 2.0e10 * (c < 1.0e8 ? c / 1.0e8 : 1.0);
+  return 2.0e-5 + c / rate;
+}
+static double solo_setup_s(int64_t cells) { return 1.0e-2 + (double)cells * 1.5e-9; }
+
+static int by_deadline(const void *a, const void *b) {
+  const req *x = *(req *const *)a, *y = *(req *const *)b;
+  return x->deadline < y->deadline ? -1 : x->deadline > y->deadline;
+}
 
 static void order_requests(server *S, int policy) {
   const double now = now_s(S);
@@ -285,16 +294,26 @@ static void order_requests(server *S, int policy) {
       r->key = -ratio;
     } else if (policy == FDTD_SERVE_BOUNDED && ratio >= serve_max_ratio()) {
       r->key = -ratio; /* ahead of every key >= 0 below */
-    } else if (policy == FDTD_SERVE_DEADLINE) {
-      /* slack against the one-at-a-time queue's finish time; a request
-       * with too little left goes ahead, earliest deadline first (a
-       * margin covers the estimate's error and the round in flight) */
-      const double left = solo_step_s(req_cells(r)) * (r->r.steps - r->done);
-      const double slack = r->deadline - now - left;
-      r->key = slack < 0.15 * left + 0.05 ? -1.0e12 + r->deadline : work;
     } else {
       r->key = work;
     }
+  }
+  if (policy == FDTD_SERVE_DEADLINE && S->n_act > 1) {
+    /* Earliest deadline first over the resident requests: if running them
+     * in that order would bring a request within the margin of its
+     * deadline (the one-at-a-time queue's finish time), that request and
+     * every one due before it go ahead in deadline order; the others keep
+     * the least-remaining-work order behind them. */
+    qsort(S->act, (size_t)S->n_act, sizeof(req *), by_deadline);
+    double t = now;
+    int last = -1;
+    for (int a = 0; a < S->n_act; ++a) {
+      req *r = S->act[a];
+      const double left = solo_step_s(req_cells(r)) * (r->r.steps - r->done);
+      t += left;
+      if (t + 0.1 * left + 0.05 > r->deadline) last = a;
+    }
+    for (int a = 0; a <= last; ++a) S->act[a]->key = -1.0e12 + S->act[a]->deadline;
   }
   qsort(S->act, (size_t)S->n_act, sizeof(req *), by_key);
 }
