@@ -650,7 +650,10 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
             res = [srv.result(t) for t in tickets]
             st = srv.stats()
         lat = [r["info"]["latency_s"] for r in res]
+        slow = sorted(range(len(lat)), key=lambda i: -lat[i])[:3]
         out = {**_lat_summary(lat, st["elapsed_s"] + skipped),
+               "slowest": [{"latency_s": round(lat[i], 3), "cells": specs[i].cells,
+                            "steps": specs[i].steps} for i in slow],
                "Mcell_steps_per_s": round(st["cell_steps"] / (st["elapsed_s"] + skipped) / 1e6, 1),
                "peak_active": st["peak_active"],
                "peak_reserved_GB": round(st["peak_reserved_bytes"] / (1 << 30), 2),
