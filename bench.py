@@ -242,10 +242,14 @@ def run_ours(args, ranks):
     from maxwell_solver_gb300.simfdtd import _check
     from maxwell_solver_gb300.workloads import WORKLOADS, materials, probe_locations, setup, sources
 
-    # a fresh autotune cache: the end-to-end leg, which runs first, pays the
-    # autotuner's trial steps as a first drop-in call on this machine would
-    tune_dir = tempfile.mkdtemp(prefix="fdtd_tune_")
-    os.environ["FDTD_TUNE_CACHE"] = os.path.join(tune_dir, "autotune.txt")
+    # a fresh autotune cache (unless --tune-cache names one): the end-to-end
+    # leg, which runs first, pays the autotuner's trial steps as a first
+    # drop-in call on this machine would
+    if args.tune_cache:
+        os.environ["FDTD_TUNE_CACHE"] = args.tune_cache
+    else:
+        tune_dir = tempfile.mkdtemp(prefix="fdtd_tune_")
+        os.environ["FDTD_TUNE_CACHE"] = os.path.join(tune_dir, "autotune.txt")
     lib = _native.load()
     _check(lib.fdtd_set_device(ranks.local))
     w = WORKLOADS[args.workload]
@@ -714,6 +718,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--workload", default="c3", choices=("c1", "c2", "c3"))
+    ap.add_argument("--tune-cache", default="",
+                    help="autotuner cache file to use (default: a fresh one per run)")
     ap.add_argument("--e2e-steps", type=int, default=0,
                     help="steps of the end-to-end solve (0: the configuration's)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
