@@ -277,10 +277,12 @@ static double solo_step_s(int64_t cells) {
   return 2.0e-5 + c / rate;
 }
 static double solo_setup_s(int64_t cells) { return 1.0e-2 + (double)cells * 1.5e-9; }
-/* Deadlines use 3/4 of those estimates: they run about 12 % above the times
- * measured in the one-at-a-time queue, and a deadline that is too late lets
- * a large request fall behind the queue's finish time. */
-#define SERVE_DEADLINE_SCALE 0.75
+/* Deadlines use 0.85 of those estimates: they run about 12 % above the
+ * times measured in the one-at-a-time queue, and a deadline that is too late
+ * lets a large request fall behind the queue's finish time. */
+#define SERVE_DEADLINE_SCALE 0.85
+/* fdtd_step_n replays graphs of this many steps */
+#define GRAPH_STEPS 32
 
 static int by_deadline(const void *a, const void *b) {
   const req *x = *(req *const *)a, *y = *(req *const *)b;
@@ -451,7 +453,13 @@ static void *serve_loop(void *arg) {
     if (S->n_act > 0) {
       int rc = select_round(S, fill, solo_cells, &solo);
       if (!rc && solo) {
-        const int32_t n = solo->r.steps - solo->done < round ? solo->r.steps - solo->done : round;
+        /* a solo round lasts about 20 ms (at least `round` steps), so that
+         * the loop's turn between rounds costs little next to it while a
+         * request that must go ahead still waits at most one round */
+        int32_t want = (int32_t)(0.02 / solo_step_s(req_cells(solo)));
+        if (want < round) want = round;
+        want = (want + GRAPH_STEPS - 1) / GRAPH_STEPS * GRAPH_STEPS;
+        const int32_t n = solo->r.steps - solo->done < want ? solo->r.steps - solo->done : want;
         rc = fdtd_step_n(solo->h, solo->done, n, solo->r.tfsf_mode, NULL);
         if (!rc) solo->done_base = solo->done + n;
         else {
