@@ -381,7 +381,8 @@ def run_ours(args, ranks):
     served = None
     if solo and not args.no_serve:
         served = run_served(args.serve_requests,
-                            [float(x) for x in args.serve_loads.split(",") if x])
+                            [float(x) for x in args.serve_loads.split(",") if x],
+                            policy=args.serve_policy)
 
     batched = None
     if solo and not args.no_batch:
@@ -612,6 +613,13 @@ def _lat_summary(lat, makespan):
 
 def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
                policy: str = "deadline"):
+    """(see _run_served; policy may list several, comma-separated: the first
+    is the line's `served`, the others are reported beside it)"""
+    pols = [p for p in policy.split(",") if p]
+    return _run_served(n_req, loads, budget_gb, seed, pols)
+
+
+def _run_served(n_req: int, loads, budget_gb: float, seed: int, policies):
     """Served configuration c5: a Poisson stream of requests (seeded serve
     mix, axes log-uniform 48..384, steps 200..4000) through the C request
     loop (continuous batching under an HBM budget, deadline policy), against
@@ -635,7 +643,7 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
     specs = serve_mix(n_req, seed)
     budget = int(budget_gb * (1 << 30))
 
-    def one_run(arrivals, one_at_a_time):
+    def one_run(arrivals, one_at_a_time, policy=policies[0]):
         with Server(hbm_budget=budget, one_at_a_time=one_at_a_time, policy=policy) as srv:
             t0 = time.perf_counter()
             skipped = 0.0
@@ -689,6 +697,10 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
         same &= all(np.array_equal(r["probes"], p) for r, p in zip(res, ref))
         fifo = fifo_model(arrivals)
         pt = {"load": load, "rate_per_s": round(rate, 3), "served": served}
+        for pol in policies[1:]:
+            other, res_o = one_run(arrivals, False, pol)
+            same &= all(np.array_equal(r["probes"], p) for r, p in zip(res_o, ref))
+            pt[f"served_{pol}"] = other
         live, res_l = one_run(arrivals, True)
         same &= all(np.array_equal(r["probes"], p) for r, p in zip(res_l, ref))
         pt["one_at_a_time"] = live
@@ -702,7 +714,7 @@ def run_served(n_req: int, loads, budget_gb: float = 120.0, seed: int = 4,
         "workload": f"c5: {len(specs)} requests (seed {seed}), cubic-ish axes log-U[48,384], "
                     "CPML 8..16, spheres (oblique TF/SF, mode 5) or layers (mode 1), "
                     "steps U[200,4000], 8 probes each; Poisson arrivals",
-        "policy": policy, "hbm_budget_GB": budget_gb,
+        "policy": policies[0], "hbm_budget_GB": budget_gb,
         "capacity_solves_per_s": round(capacity, 3), "one_at_a_time_saturated": sat,
         "loads": points, "identical_results": bool(same),
         "timing": "wall clock from each request's submission to its result on the host "
@@ -736,6 +748,9 @@ def main():
     ap.add_argument("--serve-loads", default="0.3,0.6,0.9,1.2",
                     help="offered loads, fractions of the measured batched capacity")
     ap.add_argument("--serve-only", action="store_true", help="run only the served leg")
+    ap.add_argument("--serve-policy", default="deadline",
+                    help="served order(s): deadline, srpt, bounded, hrrn; a comma-separated "
+                         "list runs each (the first is the line's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -748,7 +763,8 @@ def main():
         return
     if args.serve_only:
         loads = [float(x) for x in args.serve_loads.split(",") if x]
-        print(json.dumps({"served": run_served(args.serve_requests, loads)}), flush=True)
+        print(json.dumps({"served": run_served(args.serve_requests, loads,
+                                               policy=args.serve_policy)}), flush=True)
         return
     if args.impl == "reference":
         out = run_reference(args, ranks)
