@@ -495,13 +495,13 @@ int fdtd_division_plan(float dx, float out[4]);
 int fdtd_check_division(float dx, uint64_t *mismatches);
 
 /* Bounded-wait self-check on the current GPU: every pipeline wait of the
- * kernels gives up after a fixed number of polls, raises the device error
- * word and returns (the host then reports FDTD_ERR_CUDA) instead of hanging.
- * This runs that wait with a short limit on a barrier nothing completes --
- * *timed_out must be 1 -- and then on one the waiting thread completes --
- * *completed must be 1, so the context is still usable; *poll_ns is the
- * measured time per poll, from which the production limit's duration
- * (*limit_ms, at most) follows.  No reference counterpart. */
+ * kernels gives up after a fixed time of the GPU's global timer (2 s),
+ * raises the device error word and returns (the host then reports
+ * FDTD_ERR_CUDA) instead of hanging.  This runs that wait with a 1 ms limit
+ * on a barrier nothing completes -- *timed_out must be 1, *poll_ns receives
+ * the ns it waited -- and then on one the waiting thread completes --
+ * *completed must be 1, so the context is still usable; *limit_ms is the
+ * production limit.  No reference counterpart. */
 int fdtd_check_bounded_wait(int32_t *timed_out, int32_t *completed, double *poll_ns,
                             double *limit_ms);
 

@@ -2318,14 +2318,10 @@ int fdtd_check_bounded_wait(int32_t *timed_out, int32_t *completed, double *poll
   int e = fdtdk_check_wait(0, a);
   if (!e) e = fdtdk_check_wait(1, b);
   if (e) return fail(FDTD_ERR_CUDA, "bounded-wait check: %s", cudaGetErrorString((cudaError_t)e));
-  int dev = 0, khz = 0;
-  cudaGetDevice(&dev);
-  if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev) != cudaSuccess || khz <= 0)
-    khz = 1000000;
   *timed_out = (int32_t)a[0];
   *completed = b[0] == 0;
-  *poll_ns = (double)a[1] / (double)fdtdk_check_polls() / ((double)khz * 1e-6);
-  *limit_ms = *poll_ns * (double)fdtdk_wait_polls() * 1e-6;
+  *poll_ns = (double)a[1]; /* the check's wait, limit fdtdk_check_ns() */
+  *limit_ms = (double)fdtdk_wait_ns() * 1e-6;
   return FDTD_OK;
 }
 

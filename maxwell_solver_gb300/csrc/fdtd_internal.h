@@ -335,10 +335,11 @@ fdtd_div_plan fdtd_make_div_plan(float dx);
  * [first, first + count) whose plan quotient differs bitwise from the IEEE
  * division on the GPU. */
 /* Bounded-wait self-check (fdtd_tma.cu): out[0] = 1 when the wait gave up,
- * out[1] = clock cycles it took; the production limit and the check's. */
+ * out[1] = global-timer ns it took; the production limit and the check's
+ * (ns). */
 int fdtdk_check_wait(int arrive, long long out[2]);
-unsigned fdtdk_wait_polls(void);
-unsigned fdtdk_check_polls(void);
+unsigned long long fdtdk_wait_ns(void);
+unsigned long long fdtdk_check_ns(void);
 int fdtdk_check_division(fdtd_div_plan p, uint64_t first, uint64_t count,
                          unsigned long long *out, cudaStream_t s);
 

@@ -13,9 +13,13 @@
 
 namespace fdtd_pipe {
 
-// Bounded mbarrier waits: about 1 s, since a poll of a phase that has not
-// completed suspends the thread for ~3.8 us (fdtd_check_bounded_wait).
-constexpr unsigned kSpinLimit = 1u << 18;
+// Bounded mbarrier waits give up after kWaitNs of the global timer (2 s),
+// whatever a poll costs on the GPU at hand; a poll of a phase that has not
+// completed suspends the thread for a few us, so the timer is read every
+// 32 polls, and a backstop of kSpinLimit polls (about 4 s at 3.8 us a
+// poll, measured on GB300) ends the wait even if the timer stood still.
+constexpr unsigned long long kWaitNs = 2000000000ull;
+constexpr unsigned kSpinLimit = 1u << 20;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -49,17 +53,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait for phase `parity` of an mbarrier; false on timeout.
-// Waits for the phase with the given parity, at most LIMIT polls; false
-// when it gave up (the caller reports the timeout and leaves).
-template <unsigned LIMIT>
-__device__ __forceinline__ bool mbar_wait_n(uint64_t *bar, uint32_t parity) {
-  for (unsigned it = 0; it < LIMIT; ++it)
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for the phase with the given parity at most limit_ns of the global
+// timer (and at most kSpinLimit polls); false when it gave up.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, uint32_t parity,
+                                              unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (unsigned it = 1; it < kSpinLimit; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 31u) == 0u && global_ns() - t0 > limit_ns) return false;
+  }
   return false;
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  return mbar_wait_n<kSpinLimit>(bar, parity);
+  return mbar_wait_for(bar, parity, kWaitNs);
 }
 
 // Plain bulk copy global -> shared (16-byte aligned, size a multiple of 16).

@@ -180,11 +180,12 @@ struct Items {
   const int32_t *steps;      // batch: step each grid is on
 };
 
-// Self-check of the bounded wait: one thread waits, at most kCheckPolls
-// polls, on a barrier that nothing completes (arrive = 0: it must give up
-// and report it) or that it completes itself first (arrive = 1: it must
-// succeed); out[0] = 1 when it gave up, out[1] = clock cycles spent.
-constexpr unsigned kCheckPolls = 1024;
+// Self-check of the bounded wait: one thread waits, with the production
+// wait but a limit of kCheckNs, on a barrier that nothing completes
+// (arrive = 0: it must give up and report it) or that it completes itself
+// first (arrive = 1: it must succeed); out[0] = 1 when it gave up, out[1] =
+// global-timer ns spent.
+constexpr unsigned long long kCheckNs = 1000000ull;
 __global__ void k_check_wait(long long *out, int arrive) {
   __shared__ uint64_t bar;
   if (threadIdx.x == 0) {
@@ -194,12 +195,13 @@ __global__ void k_check_wait(long long *out, int arrive) {
   __syncthreads();
   if (threadIdx.x == 0) {
     if (arrive) mbar_arrive(&bar);
-    const long long t0 = clock64();
-    const bool ok = mbar_wait_n<kCheckPolls>(&bar, 0);
-    out[1] = clock64() - t0;
+    const unsigned long long t0 = global_ns();
+    const bool ok = mbar_wait_for(&bar, 0, kCheckNs);
+    out[1] = (long long)(global_ns() - t0);
     out[0] = ok ? 0 : 1;
   }
 }
+
 template <bool BATCH, class G>
 __device__ __forceinline__ void decode_item(const Items &it, int w, int &g, int &x0, int &y0,
                                             int &kb, int &np) {
@@ -1121,6 +1123,6 @@ extern "C" int fdtdk_check_wait(int arrive, long long out[2]) {
   return (int)e;
 }
 
-extern "C" unsigned fdtdk_wait_polls(void) { return kSpinLimit; }
+extern "C" unsigned long long fdtdk_wait_ns(void) { return kWaitNs; }
 extern "C" int fdtdk_batch_e_applies_x(int lean) { return lean && use_xc(); }
-extern "C" unsigned fdtdk_check_polls(void) { return kCheckPolls; }
+extern "C" unsigned long long fdtdk_check_ns(void) { return kCheckNs; }

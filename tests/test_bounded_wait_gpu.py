@@ -1,9 +1,9 @@
 """Failure detection without a GPU fault: every pipeline wait of the TMA
-kernels is bounded.  The self-check runs that wait, with a short poll limit,
-on a barrier nothing completes (it must give up and report it) and on one
-the waiting thread completes (it must succeed); the context stays usable
-(a simulation steps afterwards and matches the oracle), and the measured
-time per poll bounds how long the production limit can take."""
+kernels is bounded by time (the GPU's global timer).  The self-check runs
+that wait, with a 1 ms limit, on a barrier nothing completes (it must give
+up, after about that long, and report it) and on one the waiting thread
+completes (it must succeed); the context stays usable (a simulation steps
+afterwards and matches the oracle), and the production limit is 2 s."""
 import ctypes
 
 import numpy as np
@@ -23,9 +23,9 @@ def test_wait_gives_up_and_context_survives():
                                        ctypes.byref(limit)) == 0
     assert t.value == 1  # nothing completed the barrier: the wait gave up
     assert c.value == 1  # completed barrier: the wait returned
-    assert 0 < poll.value < 1e6
-    assert limit.value < 3e3  # the production limit gives up within seconds
-    print(f"poll {poll.value:.1f} ns, production limit {limit.value:.1f} ms")
+    assert 1e6 <= poll.value < 5e7  # gave up after its 1 ms limit (timer read every 32 polls)
+    assert limit.value == 2000.0  # the production limit: 2 s
+    print(f"check waited {poll.value / 1e6:.3f} ms, production limit {limit.value:.1f} ms")
 
     from maxwell_solver_gb300 import simFDTD
 
