@@ -2277,7 +2277,10 @@ int fdtd_estimate_device_bytes(int32_t I, int32_t J, int32_t K, int32_t pml, int
   b += cells * 2 + (uint64_t)MAX_MATERIALS * 6 * 4; /* material ids + table */
   b += (uint64_t)HASH_CAP * (8 + 8 + 4) + 16 + 4;  /* indexing scratch, error word */
   b += 8 * (sx + sy + sz) * 4;                     /* psi pairs */
-  b += 6 * cells * 4 + 4 * (sx + sy + sz) * 4;     /* the fused step's second buffer */
+  if (fused_mode() == 1 || (fused_mode() < 0 && tune_enabled() &&
+                              (int64_t)cells >= TUNE_MIN_CELLS))
+    b += 6 * cells * 4 + 4 * (sx + sy + sz) * 4;   /* the fused step's second buffer
+                                                      (held until the autotuner decides) */
   b += 2 * (uint64_t)I * 4 + 16;                   /* stretch denominators, counters */
   b += (uint64_t)T * num_ant * 6 * 4 + (uint64_t)num_ant * 8; /* probes */
   b += 4 * (uint64_t)T * S * 4 + (uint64_t)T * 4 + 16 * S + (uint64_t)T * 4; /* 1D tables */

@@ -89,9 +89,12 @@ typedef struct server {
   req *q_head, *q_tail;
   int queued, active; /* counts, under mu */
   uint64_t reserved;  /* sum of the active requests' peak estimates */
-  /* server thread only */
+  /* server thread only: resident requests, and admitted ones (memory
+   * reserved) whose set-up waits (deadline order, see serve_loop) */
   req **act;
   int n_act, cap_act;
+  req **pend;
+  int n_pend, cap_pend;
   fdtd_batch batch;
   /* pacing: an event after each round; the loop queues a round only once
    * the round before the last has finished, so that the order it picks
@@ -299,6 +302,24 @@ static int by_deadline(const void *a, const void *b) {
   return x->deadline < y->deadline ? -1 : x->deadline > y->deadline;
 }
 
+/* Earliest deadline first over the resident requests: sorts S->act by
+ * deadline and returns the last index of the urgent prefix (-1: none) --
+ * if running them in that order would bring a request within the margin
+ * of its deadline (the one-at-a-time queue's finish time), that request and
+ * every one due before it are urgent. */
+static int urgent_prefix(server *S, double now) {
+  qsort(S->act, (size_t)S->n_act, sizeof(req *), by_deadline);
+  double t = now;
+  int last = -1;
+  for (int a = 0; a < S->n_act; ++a) {
+    req *r = S->act[a];
+    const double left = SERVE_DEADLINE_SCALE * solo_step_s(req_cells(r)) * (r->r.steps - r->done);
+    t += left;
+    if (t + 0.15 * left + 0.1 > r->deadline) last = a;
+  }
+  return last;
+}
+
 static void order_requests(server *S, int policy) {
   const double now = now_s(S);
   for (int a = 0; a < S->n_act; ++a) {
@@ -315,21 +336,9 @@ static void order_requests(server *S, int policy) {
     }
   }
   if (policy == FDTD_SERVE_DEADLINE && S->n_act > 1) {
-    /* Earliest deadline first over the resident requests: if running them
-     * in that order would bring a request within the margin of its
-     * deadline (the one-at-a-time queue's finish time), that request and
-     * every one due before it go ahead in deadline order; the others keep
-     * the least-remaining-work order behind them. */
-    qsort(S->act, (size_t)S->n_act, sizeof(req *), by_deadline);
-    double t = now;
-    int last = -1;
-    for (int a = 0; a < S->n_act; ++a) {
-      req *r = S->act[a];
-      const double left =
-          SERVE_DEADLINE_SCALE * solo_step_s(req_cells(r)) * (r->r.steps - r->done);
-      t += left;
-      if (t + 0.15 * left + 0.1 > r->deadline) last = a;
-    }
+    /* the urgent requests go ahead in deadline order; the others keep the
+     * least-remaining-work order behind them */
+    const int last = urgent_prefix(S, now);
     for (int a = 0; a <= last; ++a) S->act[a]->key = -1.0e12 + S->act[a]->deadline;
   }
   qsort(S->act, (size_t)S->n_act, sizeof(req *), by_key);
@@ -395,13 +404,14 @@ static void *serve_loop(void *arg) {
   req *adm[ADMIT_MAX];
   pthread_mutex_lock(&S->mu);
   for (;;) {
-    while (!S->stop && !S->q_head && S->n_act == 0) pthread_cond_wait(&S->cv_work, &S->mu);
-    if (S->stop && !S->q_head && S->n_act == 0) break;
+    while (!S->stop && !S->q_head && S->n_act == 0 && S->n_pend == 0)
+      pthread_cond_wait(&S->cv_work, &S->mu);
+    if (S->stop && !S->q_head && S->n_act == 0 && S->n_pend == 0) break;
     /* 1. admission, in arrival order */
     int na = 0;
     while (S->q_head && na < ADMIT_MAX) {
       req *r = S->q_head;
-      const int on_device = S->n_act + na;
+      const int on_device = S->n_act + S->n_pend + na;
       if (S->cfg.one_at_a_time && on_device > 0) break;
       if (S->cfg.max_active > 0 && on_device >= S->cfg.max_active) break;
       const int never = r->est > S->cfg.hbm_budget;
@@ -420,7 +430,10 @@ static void *serve_loop(void *arg) {
     if (S->active > S->peak_active) S->peak_active = S->active;
     pthread_mutex_unlock(&S->mu);
 
-    /* 2. set-up (one at a time: set-up, every step, outputs) */
+    /* 2. set-up (one at a time: set-up, every step, outputs).  In the
+     * deadline order a set-up waits while a resident request is urgent: it
+     * occupies the loop (and the GPU) for tens of ms, and a request that
+     * arrived later is due later, so the urgent one goes first. */
     for (int a = 0; a < na; ++a) {
       req *r = adm[a];
       if (r->status == FDTD_ERR_OOM) {
@@ -428,6 +441,31 @@ static void *serve_loop(void *arg) {
         snprintf(m, sizeof(m), "request needs %llu device bytes, budget %llu",
                  (unsigned long long)r->est, (unsigned long long)S->cfg.hbm_budget);
         finish(S, r, FDTD_ERR_OOM, m);
+        continue;
+      }
+      if (S->n_pend == S->cap_pend) {
+        const int nc = S->cap_pend ? 2 * S->cap_pend : 64;
+        req **p = (req **)realloc(S->pend, (size_t)nc * sizeof(req *));
+        if (!p) {
+          finish(S, r, FDTD_ERR_OOM, "out of host memory");
+          continue;
+        }
+        S->pend = p;
+        S->cap_pend = nc;
+      }
+      S->pend[S->n_pend++] = r;
+    }
+    const int hold = S->cfg.policy == FDTD_SERVE_DEADLINE && !S->cfg.one_at_a_time &&
+                     S->n_act > 0 && urgent_prefix(S, now_s(S)) >= 0;
+    int kept = 0;
+    for (int a = 0; a < S->n_pend; ++a) {
+      req *r = S->pend[a];
+      if (__atomic_load_n(&r->cancel, __ATOMIC_ACQUIRE)) { /* fdtd_server_cancel */
+        finish(S, r, FDTD_ERR_CANCELLED, "cancelled");
+        continue;
+      }
+      if (hold) {
+        S->pend[kept++] = r;
         continue;
       }
       int rc = setup(r);
@@ -456,6 +494,7 @@ static void *serve_loop(void *arg) {
       }
       S->act[S->n_act++] = r;
     }
+    S->n_pend = kept;
 
     /* 3. the round's members, then one round: the batch, or one request
      * alone through fdtd_step_n */
@@ -848,6 +887,7 @@ int fdtd_server_destroy(fdtd_server h) {
   for (size_t i = 0; i < S->tab_n; ++i) free_req(S->tab[i]);
   free(S->tab);
   free(S->act);
+  free(S->pend);
   free(S->lat);
   pthread_cond_destroy(&S->cv_work);
   pthread_cond_destroy(&S->cv_done);
