@@ -890,10 +890,11 @@ int g_blocks_b[6] = {0, 0, 0, 0, 0, 0};
 // The compacted CPML X kernels (XC) when FDTD_XC=1; by default the lean
 // kernels without it, with E's CPML X as the x-slab pass.  Both give the
 // same results.  Measured on GB300: XC is slower on the 256^3, 512x512x448
-// and batched workloads (c3 E half-step 0.833 vs 0.800 ms, c4 batch 82.4
-// vs 88.4 solves/s): the warp that takes the x-slab cells waits on their
-// psi loads while the stage it holds keeps the ring from advancing, where
-// the separate pass has every thread of the GPU in flight.
+// and batched workloads (512x512x448 E half-step 0.833 vs 0.800 ms; 256
+// grids of 32..128 cells a side 82.4 vs 88.4 solves/s): the warp that takes
+// the x-slab cells waits on their psi loads while the stage it holds keeps
+// the ring from advancing, where the separate pass has every thread of the
+// GPU in flight.
 bool use_xc() {
   static int v = -1;
   if (v < 0) {
