@@ -570,6 +570,7 @@ def run_batched(n_grids: int, batched_only: bool = False):
         b.add(P, 0, s.steps, s.mode)
     b.run()
     t_batch = time.perf_counter() - t0
+    zrun = b.zrun
     b.close()
     same = all(np.array_equal(ref[g], simFDTD("OutputVis", handles[g], np.uint32(mix[g].cells),
                                               np.int32(3))) for g in ref)
@@ -592,6 +593,7 @@ def run_batched(n_grids: int, batched_only: bool = False):
                     "one_at_a_time": None if t_one is None else round(t_one, 3),
                     "one_at_a_time_per_op": None if t_ops is None else round(t_ops, 3),
                     "setup": round(t_setup, 2)},
+        "zrun": zrun,
         "identical_results": bool(same), "members_compared": len(ref),
         "timing": "wall clock, fields resident, setup excluded; one at a time = fdtd_step_n "
                   "per grid (graph-replayed fused steps) and, separately, the per-op calls",

@@ -302,6 +302,11 @@ int fdtd_batch_progress(fdtd_batch b, fdtd_handle h, int32_t *done);
 /* Drops member h (finished or not); calls on h issued afterwards follow the
  * batch's queued work. */
 int fdtd_batch_remove(fdtd_batch b, fdtd_handle h);
+/* The z-planes per batched work item: measured once per batch (the first
+ * step call with at least 8 active members tries 8, 16 and 32 for a few of
+ * the members' real steps and keeps the fastest; FDTD_BATCH_ZRUN fixes it);
+ * 0 before that.  No reference counterpart. */
+int fdtd_batch_get_zrun(fdtd_batch b, int32_t *zrun);
 /* Waits for the batch's queued work and reports whether every pipelined
  * half-step completed (FDTD_ERR_CUDA if a bounded wait timed out; the
  * members' fields are then not valid). */

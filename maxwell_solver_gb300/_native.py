@@ -139,6 +139,7 @@ SIGNATURES = {
     "fdtd_batch_destroy": (ctypes.c_int, [U64]),
     "fdtd_batch_add": (ctypes.c_int, [U64, U64, I32, I32, I32, ctypes.POINTER(FdtdCurrent)]),
     "fdtd_batch_step": (ctypes.c_int, [U64, I32, ctypes.POINTER(I32)]),
+    "fdtd_batch_get_zrun": (ctypes.c_int, [U64, ctypes.POINTER(I32)]),
     "fdtd_batch_run": (ctypes.c_int, [U64]),
     "fdtd_batch_clear": (ctypes.c_int, [U64]),
     "fdtd_batch_progress": (ctypes.c_int, [U64, U64, ctypes.POINTER(I32)]),

@@ -50,6 +50,13 @@ class Batch:
         _check(self._lib.fdtd_batch_progress(self.handle, _handle(P), ctypes.byref(d)))
         return d.value
 
+    @property
+    def zrun(self) -> int:
+        """z-planes per batched work item (0 until the batch has measured it)."""
+        z = ctypes.c_int32(0)
+        _check(self._lib.fdtd_batch_get_zrun(self.handle, ctypes.byref(z)))
+        return z.value
+
     def close(self):
         if self.handle:
             _check(self._lib.fdtd_batch_destroy(self.handle))

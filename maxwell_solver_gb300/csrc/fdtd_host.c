@@ -2599,6 +2599,9 @@ typedef struct batch {
   /* GRAPH_CHUNK steps of the active set, captured after each rebuild */
   cudaGraphExec_t gexec;
   unsigned long long g_kernels;
+  /* z-planes per work item, measured once (batch_tune) */
+  int zrun, tuned;
+  cudaEvent_t tev[2];
 } batch;
 
 static batch *g_batches[MAX_BATCHES];
@@ -2619,6 +2622,11 @@ int fdtd_batch_create(fdtd_batch *out) {
   if (!b) return fail(FDTD_ERR_OOM, "out of host memory");
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->tev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->tev[1]);
+  b->zrun = batch_zrun();
+  /* the z-run is measured at the first large enough step unless fixed */
+  b->tuned = getenv("FDTD_BATCH_ZRUN") != NULL || !tune_enabled();
   if (e == cudaSuccess) e = pool_alloc((void **)&b->d_work, 4 * sizeof(int32_t), b->stream);
   if (e == cudaSuccess) e = pool_alloc((void **)&b->d_err, sizeof(int32_t), b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_work, 0, 4 * sizeof(int32_t), b->stream);
@@ -2690,6 +2698,8 @@ int fdtd_batch_destroy(fdtd_batch h) {
   dfree_on(b->stream, b->d_err);
   cudaStreamSynchronize(b->stream);
   cudaEventDestroy(b->ev);
+  cudaEventDestroy(b->tev[0]);
+  cudaEventDestroy(b->tev[1]);
   cudaStreamDestroy(b->stream);
   free(b->m);
   free(b);
@@ -2772,8 +2782,7 @@ static int ensure_cap(void **d, void **hbuf, int *cap, int need, size_t elem, cu
   return FDTD_OK;
 }
 
-static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk) {
-  const int zr = batch_zrun();
+static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk, int zr) {
   assert(nk <= 65536 && zr < 32768); /* kb and np share one int32 (fdtd_batch_add) */
   for (int kb = 0; kb < nk; kb += zr) {
     const int np = nk - kb < zr ? nk - kb : zr;
@@ -2790,9 +2799,9 @@ static int add_items(int32_t *tab, int n, int g, int ni, int nj, int nk) {
   return n;
 }
 
-static int count_items(int ni, int nj, int nk) {
+static int count_items(int ni, int nj, int nk, int zr) {
   return ((ni + FDTD_BTILE_X - 1) / FDTD_BTILE_X) * ((nj + FDTD_BTILE_Y - 1) / FDTD_BTILE_Y) *
-         ((nk + batch_zrun() - 1) / batch_zrun());
+         ((nk + zr - 1) / zr);
 }
 
 /* Builds and uploads the device mirrors of the active members. */
@@ -2804,8 +2813,8 @@ static int batch_rebuild(batch *b) {
     sim *s = lookup(m->h);
     if (!s) return fail(FDTD_ERR_INVALID_HANDLE, "a batch member was deleted");
     ++na;
-    nh += count_items(s->I - 1, s->J - 1, s->K - 1);
-    ne += count_items(s->I, s->J, s->K);
+    nh += count_items(s->I - 1, s->J - 1, s->K - 1, b->zrun);
+    ne += count_items(s->I, s->J, s->K, b->zrun);
   }
   int rc;
   if (na > b->dev_cap) { /* per-member mirrors share one capacity */
@@ -2891,8 +2900,8 @@ static int batch_rebuild(batch *b) {
     }
     b->h_steps[g] = m->first + m->done;
     if (s->dev.num_ant > 0) b->any_probes = 1;
-    nh = add_items(b->h_tab_h, nh, g, s->I - 1, s->J - 1, s->K - 1);
-    ne = add_items(b->h_tab_e, ne, g, s->I, s->J, s->K);
+    nh = add_items(b->h_tab_h, nh, g, s->I - 1, s->J - 1, s->K - 1, b->zrun);
+    ne = add_items(b->h_tab_e, ne, g, s->I, s->J, s->K, b->zrun);
     ++g;
   }
   b->n_act = na;
@@ -2945,6 +2954,57 @@ static int batch_step_ops(batch *b) {
   return FDTD_OK;
 }
 
+/* The batch's z-run (z-planes per work item) is measured once, on the
+ * first step call with at least BATCH_TUNE_MIN_MEMBERS active members: a
+ * few steps of the members with each candidate (the steps are real: the
+ * result does not depend on the z-run), the fastest kept.  *steps_done
+ * receives the steps taken.  The caller asks for more steps than the tuning
+ * takes, so no member finishes inside it and every rebuild keeps them all. */
+#define BATCH_TUNE_MIN_MEMBERS 8
+#define BATCH_TUNE_CANDS 3
+static int batch_tune(batch *b, int32_t *steps_done) {
+  static const int cand[BATCH_TUNE_CANDS] = {8, 16, 32};
+  float best = 1e30f;
+  int bz = b->zrun, rc;
+  for (int c = 0; c < BATCH_TUNE_CANDS; ++c) {
+    b->zrun = cand[c];
+    if (b->gexec) {
+      cudaGraphExecDestroy(b->gexec);
+      b->gexec = NULL;
+    }
+    if ((rc = batch_rebuild(b))) return rc;
+    if ((rc = batch_step_ops(b))) return rc; /* untimed: the new tables */
+    CU(cudaEventRecord(b->tev[0], b->stream));
+    for (int k = 0; k < 3; ++k)
+      if ((rc = batch_step_ops(b))) return rc;
+    CU(cudaEventRecord(b->tev[1], b->stream));
+    CU(cudaEventSynchronize(b->tev[1]));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, b->tev[0], b->tev[1]));
+    if (ms < best) {
+      best = ms;
+      bz = cand[c];
+    }
+    /* the members' progress before the next rebuild uploads their steps */
+    for (int g = 0; g < b->n_act; ++g) b->m[b->act[g]].done += 4;
+    *steps_done += 4;
+  }
+  if (bz != b->zrun) {
+    b->zrun = bz;
+    if ((rc = batch_rebuild(b))) return rc;
+  }
+  b->tuned = 1;
+  return FDTD_OK;
+}
+
+int fdtd_batch_get_zrun(fdtd_batch bh, int32_t *zrun) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  if (!zrun) return fail(FDTD_ERR_INVALID_ARG, "null output");
+  *zrun = b->tuned ? b->zrun : 0;
+  return FDTD_OK;
+}
+
 /* Advances every active member by up to max_steps steps (all by the same
  * number: the fewest remaining steps of any active member, capped by
  * max_steps).  *active_left receives the number of members still running. */
@@ -2977,8 +3037,12 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
     const bmember *m = &b->m[b->act[g]];
     if (m->count - m->done < nsteps) nsteps = m->count - m->done;
   }
-  int32_t t = 0;
-  if (nsteps >= GRAPH_CHUNK) {
+  int32_t tuned = 0; /* steps the tuning took (already counted per member) */
+  if (!b->tuned && b->n_act >= BATCH_TUNE_MIN_MEMBERS && nsteps > 4 * BATCH_TUNE_CANDS) {
+    if ((rc = batch_tune(b, &tuned))) return rc;
+  }
+  int32_t t = tuned;
+  if (nsteps - t >= GRAPH_CHUNK) {
     if (!b->gexec) {
       cudaGraph_t g;
       const unsigned long long before = fdtdk_launch_count();
@@ -2997,7 +3061,8 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
       b->g_kernels = fdtdk_launch_count() - before;
       g_captured_kernels += b->g_kernels;
     }
-    for (; nsteps - t >= GRAPH_CHUNK; t += GRAPH_CHUNK) {
+    while (nsteps - t >= GRAPH_CHUNK) {
+      t += GRAPH_CHUNK;
       CU(cudaGraphLaunch(b->gexec, b->stream));
       g_graph_kernels += b->g_kernels;
     }
@@ -3007,7 +3072,7 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
   int finished = 0;
   for (int g = 0; g < b->n_act; ++g) {
     bmember *m = &b->m[b->act[g]];
-    m->done += nsteps;
+    m->done += nsteps - tuned;
     if (m->done >= m->count) finished = 1;
   }
   if (finished) {

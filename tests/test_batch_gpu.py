@@ -1,6 +1,8 @@
 """Batched execution: heterogeneous grids advanced together by the batched
 persistent kernels end bit-identical to each grid run alone (and to the
 oracle), whatever the mix, the step counts, or when members join."""
+import os
+
 import numpy as np
 import pytest
 
@@ -124,6 +126,46 @@ def test_graph_replayed_rounds_equal_alone():
         for a, w, n in zip(got, want, FIELDS):
             np.testing.assert_array_equal(a, w, err_msg=f"{sc.name} {n}")
             np.testing.assert_array_equal(a, o.field(n), err_msg=f"{sc.name} {n} oracle")
+        simFDTD("DeleteSimulation", P)
+
+
+def test_zrun_measured_on_real_steps():
+    """A batch of 8 members or more measures its z-run on its first step
+    call of more than 12 steps: 4 real steps with each of 8, 16 and 32
+    z-planes per work item; the members' progress counts them and every
+    member still ends bit-identical to running alone."""
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.batch import Batch
+
+    if os.environ.get("FDTD_AUTOTUNE") == "0" or "FDTD_BATCH_ZRUN" in os.environ:
+        pytest.skip("the z-run is fixed in this environment")
+    picks = list(SCENARIOS) + [SCENARIOS[0], SCENARIOS[3]]
+    members = []
+    with Batch() as b:
+        for idx, sc in enumerate(picks):
+            inp = sc.inputs()
+            steps = sc.steps - 3 * idx
+            P = _ready(sc, inp)
+            b.add(P, 0, steps, sc.mode, _current(sc))
+            members.append((sc, inp, steps, P))
+        assert b.zrun == 0
+        assert b.step(12) == len(picks)  # not more than the tuning takes
+        assert b.zrun == 0
+        assert b.step(20) == len(picks)
+        assert b.zrun in (8, 16, 32)
+        for sc, inp, steps, P in members:
+            assert b.progress(P) == 32
+        b.run()
+        for sc, inp, steps, P in members:
+            assert b.progress(P) == steps
+    for sc, inp, steps, P in members:
+        got = _fields(P, sc)
+        want, want_probes = _alone(sc, inp, steps)
+        for a, w, n in zip(got, want, FIELDS):
+            np.testing.assert_array_equal(a, w, err_msg=f"{sc.name} {n}")
+        if sc.n_probes:
+            rec = simFDTD("OutputProbes", P, np.uint32(sc.steps * sc.n_probes * 6))
+            np.testing.assert_array_equal(rec, want_probes)
         simFDTD("DeleteSimulation", P)
 
 
