@@ -24,6 +24,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <sys/stat.h>
+#include <time.h>
 
 #include <cuda_runtime_api.h>
 
@@ -2602,6 +2603,9 @@ typedef struct batch {
   /* z-planes per work item, measured once (batch_tune) */
   int zrun, tuned;
   cudaEvent_t tev[2];
+  /* rebuilds and graph captures so far, and their host seconds */
+  uint64_t n_rebuild, n_capture;
+  double t_rebuild, t_capture;
 } batch;
 
 static batch *g_batches[MAX_BATCHES];
@@ -2804,8 +2808,22 @@ static int count_items(int ni, int nj, int nk, int zr) {
          ((nk + zr - 1) / zr);
 }
 
+static double mono_s(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+static int batch_rebuild_(batch *b);
 /* Builds and uploads the device mirrors of the active members. */
 static int batch_rebuild(batch *b) {
+  const double t0 = mono_s();
+  const int rc = batch_rebuild_(b);
+  b->t_rebuild += mono_s() - t0;
+  b->n_rebuild += 1;
+  return rc;
+}
+static int batch_rebuild_(batch *b) {
   int na = 0, nh = 0, ne = 0;
   for (int i = 0; i < b->n; ++i) {
     const bmember *m = &b->m[i];
@@ -3045,6 +3063,7 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
   if (nsteps - t >= GRAPH_CHUNK) {
     if (!b->gexec) {
       cudaGraph_t g;
+      const double tc0 = mono_s();
       const unsigned long long before = fdtdk_launch_count();
       CU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
       int crc = FDTD_OK;
@@ -3060,6 +3079,8 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
       }
       b->g_kernels = fdtdk_launch_count() - before;
       g_captured_kernels += b->g_kernels;
+      b->t_capture += mono_s() - tc0;
+      b->n_capture += 1;
     }
     while (nsteps - t >= GRAPH_CHUNK) {
       t += GRAPH_CHUNK;
@@ -3089,6 +3110,16 @@ int fdtd_batch_step(fdtd_batch bh, int32_t max_steps, int32_t *active_left) {
   left = 0;
   for (int i = 0; i < b->n; ++i) left += b->m[i].done < b->m[i].count;
   if (active_left) *active_left = left;
+  return FDTD_OK;
+}
+
+int fdtd_internal_batch_counts(fdtd_batch bh, uint64_t n[2], double t[2]) {
+  batch *b = blookup(bh);
+  if (!b) return fail(FDTD_ERR_INVALID_HANDLE, "invalid batch handle");
+  n[0] = b->n_rebuild;
+  n[1] = b->n_capture;
+  t[0] = b->t_rebuild;
+  t[1] = b->t_capture;
   return FDTD_OK;
 }
 

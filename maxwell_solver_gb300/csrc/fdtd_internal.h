@@ -304,6 +304,9 @@ int fdtd_internal_fail(int code, const char *msg);
  * the work queued so far (the serving loop paces itself with these). */
 int fdtd_internal_record(fdtd_handle h, cudaEvent_t ev);
 int fdtd_internal_batch_record(fdtd_batch b, cudaEvent_t ev);
+/* A batch's rebuilds and graph captures so far (n) and their host seconds
+ * (t), for the serving loop's trace. */
+int fdtd_internal_batch_counts(fdtd_batch b, uint64_t n[2], double t[2]);
 
 /* TF/SF corrections of a split half-step over the face cells (single grid,
  * and every active member of a batch whose op has tfsf_split set;

@@ -75,6 +75,11 @@ typedef struct req {
   struct req *next;
 } req;
 
+/* phases of the serving loop (trace) */
+enum { TR_SETUP, TR_SELECT, TR_SOLO, TR_BATCH, TR_PACE, TR_RETIRE, TR_N };
+static const char *const k_tr_name[TR_N] = {"set-up", "select", "solo issue", "batch issue",
+                                            "pacing wait", "retire"};
+
 typedef struct server {
   fdtd_server_config cfg;
   pthread_t thread;
@@ -110,6 +115,10 @@ typedef struct server {
   double first_submit, last_finish;
   double *lat;
   size_t n_lat, cap_lat;
+  /* server thread only: seconds and counts per phase of the loop, printed
+   * to stderr at destroy when FDTD_SERVE_TRACE is set */
+  double tr[TR_N];
+  uint64_t trn[TR_N];
 } server;
 
 static pthread_mutex_t g_srv_lock = PTHREAD_MUTEX_INITIALIZER;
@@ -273,17 +282,20 @@ static double serve_max_ratio(void) {
 
 /* Estimated seconds a request of `cells` cells takes alone for `steps`
  * steps through fdtd_step_n (a fixed cost per step of the launches, then a
- * cell rate rising from 60 G cell-steps/s at 16 M cells to 80 G at 100 M;
- * measured on GB300), and its set-up (rasterising, indexing, autotuning). */
+ * cell rate rising from 55 G cell-steps/s for small grids to 102 G at 100 M
+ * cells), and its set-up with its readout (rasterising, indexing, a cached
+ * autotune, the probe record).  Least-squares fit to the one-at-a-time
+ * queue's service times of 100 mixed requests (0.1-55 M cells, 200-4000
+ * steps) on GB300: within 6 % (standard deviation) per request, 1 % on
+ * their sum. */
 static double solo_step_s(int64_t cells) {
-  const double c = (double)cells, rate = 6.0e10 + 2.0e10 * (c < 1.0e8 ? c / 1.0e8 : 1.0);
-  return 2.0e-5 + c / rate;
+  const double c = (double)cells, rate = 5.55e10 + 4.66e10 * (c < 1.0e8 ? c / 1.0e8 : 1.0);
+  return 2.7e-5 + c / rate;
 }
-static double solo_setup_s(int64_t cells) { return 1.0e-2 + (double)cells * 1.5e-9; }
+static double solo_setup_s(int64_t cells) { return 3.0e-3 + (double)cells * 4.6e-10; }
 /* Deadlines use those estimates times FDTD_SERVE_DEADLINE_SCALE (default
- * 1; read once).  The estimates run about 12 % above the times measured in
- * the one-at-a-time queue: a smaller scale keeps the order nearer to the
- * queue's (tail nearer the queue's, less gain at the median). */
+ * 1; read once): a smaller scale keeps the order nearer to the queue's
+ * (tail nearer the queue's, less gain at the median). */
 static double deadline_scale(void) {
   static double v = 0.0;
   if (v <= 0.0) {
@@ -468,10 +480,19 @@ static void *serve_loop(void *arg) {
         S->pend[kept++] = r;
         continue;
       }
+      double t_ = now_s(S);
       int rc = setup(r);
+      S->tr[TR_SETUP] += now_s(S) - t_;
+      S->trn[TR_SETUP] += 1;
       if (!rc && S->cfg.one_at_a_time) {
+        t_ = now_s(S);
         rc = fdtd_step_n(r->h, 0, r->r.steps, r->r.tfsf_mode, NULL);
+        S->tr[TR_SOLO] += now_s(S) - t_;
+        S->trn[TR_SOLO] += 1;
+        t_ = now_s(S);
         if (!rc) rc = collect(S, r);
+        S->tr[TR_RETIRE] += now_s(S) - t_;
+        S->trn[TR_RETIRE] += 1;
         if (rc) drop_handle(S, r);
         finish(S, r, rc, NULL);
         continue;
@@ -500,7 +521,11 @@ static void *serve_loop(void *arg) {
      * alone through fdtd_step_n */
     req *solo = NULL;
     if (S->n_act > 0) {
+      double t_ = now_s(S);
       int rc = select_round(S, fill, solo_cells, &solo);
+      S->tr[TR_SELECT] += now_s(S) - t_;
+      S->trn[TR_SELECT] += 1;
+      t_ = now_s(S);
       if (!rc && solo) {
         /* a solo round lasts about 20 ms (at least `round` steps), so that
          * the loop's turn between rounds costs little next to it while a
@@ -523,6 +548,10 @@ static void *serve_loop(void *arg) {
         int32_t left = 0;
         rc = fdtd_batch_step(S->batch, round, &left);
       }
+      const int k_ = solo ? TR_SOLO : TR_BATCH;
+      S->tr[k_] += now_s(S) - t_;
+      S->trn[k_] += 1;
+      t_ = now_s(S);
       if (!rc && S->ev[0]) { /* pace: wait for the previous round */
         const int e = solo ? fdtd_internal_record(solo->h, S->ev[S->ev_i])
                            : fdtd_internal_batch_record(S->batch, S->ev[S->ev_i]);
@@ -533,8 +562,11 @@ static void *serve_loop(void *arg) {
           S->ev_used[S->ev_i] = 0;
         }
       }
+      S->tr[TR_PACE] += now_s(S) - t_;
+      S->trn[TR_PACE] += 1;
       if (rc) fail_active(S, rc);
     }
+    const double t_ret = now_s(S);
 
     /* 4. retire the finished ones (after checking the batch's pipelines
      * completed: a bounded wait that timed out invalidates the round) */
@@ -566,7 +598,9 @@ static void *serve_loop(void *arg) {
       if (rc) drop_handle(S, r);
       finish(S, r, rc, NULL);
       S->act[a] = S->act[--S->n_act];
+      S->trn[TR_RETIRE] += 1;
     }
+    S->tr[TR_RETIRE] += now_s(S) - t_ret;
     pthread_mutex_lock(&S->mu);
   }
   pthread_mutex_unlock(&S->mu);
@@ -883,6 +917,19 @@ int fdtd_server_destroy(fdtd_server h) {
   pthread_cond_broadcast(&S->cv_work);
   pthread_mutex_unlock(&S->mu);
   if (S->thread_started) pthread_join(S->thread, NULL);
+  if (getenv("FDTD_SERVE_TRACE")) {
+    fprintf(stderr, "fdtd serve trace (%s, %llu completed, %.3f s first submission to last result):\n",
+            S->cfg.one_at_a_time ? "one at a time" : "served", (unsigned long long)S->completed,
+            S->last_finish - S->first_submit);
+    for (int k = 0; k < TR_N; ++k)
+      fprintf(stderr, "  %-12s %9.3f s  %8llu\n", k_tr_name[k], S->tr[k],
+              (unsigned long long)S->trn[k]);
+    uint64_t n[2] = {0, 0};
+    double t[2] = {0, 0};
+    if (S->batch && fdtd_internal_batch_counts(S->batch, n, t) == FDTD_OK)
+      fprintf(stderr, "  batch rebuilds %llu (%.3f s), graph captures %llu (%.3f s)\n",
+              (unsigned long long)n[0], t[0], (unsigned long long)n[1], t[1]);
+  }
   release_gpu(S);
   for (size_t i = 0; i < S->tab_n; ++i) free_req(S->tab[i]);
   free(S->tab);
