@@ -11,6 +11,7 @@ from __future__ import annotations
 import ctypes
 import os
 import subprocess
+import sys
 import threading
 
 import numpy as np
@@ -85,6 +86,18 @@ def build_reference_funlib(ref_root: str | None = None) -> str | None:
     subprocess.run([os.path.join(HERE, "funlib_build.sh"), root], check=True,
                    stdout=subprocess.DEVNULL)
     return REF_FUNLIB_PATH
+
+
+def build_reference_gpu(ref_root: str | None = None) -> str | None:
+    """Builds oracle/_ref/ref_gpu.cubin and ref_gpu_nofma.cubin, the
+    reference's own kernels (src/gpu.h) for sm_103a through NVRTC, when the
+    reference sources are present; returns the directory or None."""
+    root = reference_root(ref_root)
+    if root is None or not os.path.exists(os.path.join(root, "src", "gpu.h")):
+        return None
+    subprocess.run([sys.executable, os.path.join(HERE, "ref_gpu_build.py"), root], check=True,
+                   stdout=subprocess.DEVNULL)
+    return os.path.join(HERE, "_ref")
 
 
 def _load():

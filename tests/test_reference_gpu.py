@@ -1,0 +1,154 @@
+"""The library against the reference's own CUDA kernels on the same GPU.
+
+tests/refgpu.py runs the reference's kernels (src/gpu.h, compiled for
+sm_103a by oracle/ref_gpu_build.py) with the reference's launch shapes over
+the CPU oracle's set-up.  Built without multiply-add contraction they
+evaluate every expression the way the library does, so the fields must be
+equal bit for bit; built with the reference's own flags (contraction on,
+src/Compile.m:4-6) they must agree to the parity tolerance, a relative L2
+error of at most 1e-5 per field.  The last test times both on the
+512 x 512 x 448 workload.
+"""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+from refgpu import unavailable
+from scenarios import SCENARIOS, run_mex
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+REL_L2 = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_reference_kernels():
+    why = unavailable()
+    if why:
+        pytest.skip(f"reference kernels: {why}")
+
+
+def _ours(P, n):
+    from maxwell_solver_gb300 import simFDTD
+
+    return {f: simFDTD("OutputVis", P, np.uint32(n), np.int32(i + 1))
+            for i, f in enumerate(FIELDS)}
+
+
+def _rel_l2(a, b):
+    d = np.linalg.norm(a.astype(np.float64) - b.astype(np.float64))
+    n = np.linalg.norm(b.astype(np.float64))
+    return d / n if n > 0 else d
+
+
+@pytest.mark.parametrize("sc", SCENARIOS, ids=[s.name for s in SCENARIOS])
+def test_scenarios_equal_reference_kernels(sc):
+    """Every scenario (modes 1-4, current sources, probes): bit-identical to
+    the reference's kernels without contraction, within 1e-5 with it."""
+    from maxwell_solver_gb300 import simFDTD
+    from refgpu import RefGPU
+
+    inp = sc.inputs()
+    P = run_mex(simFDTD, sc, inp)
+    got = _ours(P, int(np.prod(sc.dims)))
+    simFDTD("DeleteSimulation", P)
+    for fma in (False, True):
+        ref = RefGPU(fma=fma)
+        run_mex(ref, sc, inp)
+        for f in FIELDS:
+            r = ref.field(f)
+            if fma:
+                assert _rel_l2(got[f], r) <= REL_L2, (sc.name, f, _rel_l2(got[f], r))
+            else:
+                np.testing.assert_array_equal(got[f], r, err_msg=f"{sc.name} {f}")
+        ref.close()
+
+
+def _run_workload(name, steps, timed=0):
+    """The workload through the library and through the reference's kernels
+    (contraction off, then on, from the same set-up); returns the fields of
+    each after `steps` steps and, with timed > 0, the seconds per step of
+    the last `timed` of them."""
+    import torch
+
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.workloads import WORKLOADS, setup
+    from refgpu import RefGPU
+
+    w = WORKLOADS[name]
+    n = w.cells
+    P = setup(simFDTD, w, steps=steps)
+    warm = steps - timed
+    simFDTD("StepN", P, np.int32([0, warm, w.mode]))
+    simFDTD("Synchronize", P)
+    t0 = time.perf_counter()
+    if timed:
+        simFDTD("StepN", P, np.int32([warm, timed, w.mode]))
+        simFDTD("Synchronize", P)
+    ours_s = (time.perf_counter() - t0) / max(timed, 1)
+    ours = _ours(P, n)
+    simFDTD("DeleteSimulation", P)
+
+    ref = RefGPU(fma=False)
+    setup(ref, w, steps=steps)
+    out = {}
+    ref_s = None
+    for fma in (False, True):
+        ref.load(fma)
+        ref("ResetFieldAll")
+        for k in range(warm):
+            ref.step(k, w.mode)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for k in range(warm, steps):
+            ref.step(k, w.mode)
+        ev1.record()
+        torch.cuda.synchronize()
+        if fma and timed:
+            ref_s = ev0.elapsed_time(ev1) * 1e-3 / timed
+        out[fma] = {f: ref.field(f) for f in FIELDS}
+    ref.close()
+    return ours, out, ours_s, ref_s
+
+
+def test_c1_full_run_equals_reference_kernels():
+    """64^3, 10-cell CPML, TF/SF mode 3, 500 steps."""
+    ours, ref, _, _ = _run_workload("c1", 500)
+    for f in FIELDS:
+        np.testing.assert_array_equal(ours[f], ref[False][f], err_msg=f)
+        assert _rel_l2(ours[f], ref[True][f]) <= REL_L2, (f, _rel_l2(ours[f], ref[True][f]))
+
+
+def test_c3_equals_and_outruns_reference_kernels():
+    """512 x 512 x 448, 16-cell CPML, six layers, TF/SF mode 1: 36 steps
+    equal to the reference's kernels, and the step time of both (the last
+    32 steps; inputs far larger than L2)."""
+    from maxwell_solver_gb300.workloads import WORKLOADS
+
+    timed = 32
+    ours, ref, ours_s, ref_s = _run_workload("c3", 36, timed)
+    for f in FIELDS:
+        np.testing.assert_array_equal(ours[f], ref[False][f], err_msg=f)
+        assert _rel_l2(ours[f], ref[True][f]) <= REL_L2, (f, _rel_l2(ours[f], ref[True][f]))
+    cells = WORKLOADS["c3"].cells
+    rep = {"workload": "c3 512x512x448, 16-cell CPML, 6 layers, TF/SF mode 1",
+           "steps_timed": timed,
+           "reference_kernels_ms_per_step": round(ref_s * 1e3, 4),
+           "reference_kernels_Mcell_steps_per_s": round(cells / ref_s / 1e6, 1),
+           "library_ms_per_step": round(ours_s * 1e3, 4),
+           "library_Mcell_steps_per_s": round(cells / ours_s / 1e6, 1),
+           "speedup": round(ref_s / ours_s, 2),
+           "timing": "reference: CUDA events around its 32 steps of kernel launches "
+                     "(12 per step, the reference's launch shapes); library: wall clock "
+                     "around fdtd_step_n of 32 steps and a synchronize (probe gather included)"}
+    print(json.dumps(rep))
+    path = os.environ.get("FDTD_REF_GPU_REPORT")
+    if path:
+        with open(path, "w") as fh:
+            json.dump(rep, fh)
+    assert ours_s < ref_s
