@@ -176,3 +176,40 @@ def test_c3_equals_and_outruns_reference_kernels():
             json.dump(rep, fh)
     assert max(err.values()) <= REL_L2, err
     assert ours_s < ref_s
+
+
+def test_probe_record_samples_reference_kernel_fields():
+    """The probe record (row n: the six fields at each probe at the start of
+    step n) holds exactly the reference kernels' fields at the probe cells,
+    whose linear index is the reference's coax index: (pml + x) + (pml + y)
+    Imax + (pml + z) Imax Jmax (src/simulation.h:1047-1067; the reference
+    allocates the record but no kernel of it writes one)."""
+    import torch
+
+    from maxwell_solver_gb300 import simFDTD
+    from refgpu import RefGPU
+    from scenarios import by_name
+
+    sc = by_name("mode3_probes_y_current")
+    inp = sc.inputs()
+    P = run_mex(simFDTD, sc, inp)
+    rec = simFDTD("OutputProbes", P, np.uint32(sc.steps * sc.n_probes * 6))
+    simFDTD("DeleteSimulation", P)
+    rec = rec.reshape(sc.steps, sc.n_probes, 6)
+
+    I, J, _ = sc.dims
+    p = 10  # the scenarios keep the reference's CPML thickness
+    loc = np.asarray(inp["probes"], dtype=np.int64)
+    idx = torch.as_tensor((p + loc[:, 0]) + (p + loc[:, 1]) * I + (p + loc[:, 2]) * I * J,
+                          device="cuda")
+    ref = RefGPU(fma=False)
+    rows = [np.zeros((sc.n_probes, 6), dtype=np.float32)]  # the state before step 0
+
+    def sample(n, _P):
+        if n + 1 < sc.steps:
+            rows.append(torch.stack([ref.d[f][idx] for f in FIELDS], dim=1).cpu().numpy())
+
+    run_mex(ref, sc, inp, on_step=sample)
+    ref.close()
+    np.testing.assert_array_equal(rec, np.stack(rows))
+    assert np.abs(rec).max() > 0
