@@ -179,3 +179,35 @@ def test_batch_rejects_unready_members():
             b.add(P, 0, 10, 0)
         assert e.value.identifier == "simFDTD:InvalidState"
     simFDTD("DeleteSimulation", P)
+
+
+def test_lean_batch_of_mix_equals_alone():
+    """Grids of the batched mix (axes 32..128, 8-cell CPML, spheres, oblique
+    TF/SF: the lean batched kernels, which prefetch the next plane's psi
+    pairs) end bit-identical to each grid stepped alone, over 12 members of
+    uneven step counts (the z-run measured on the first call)."""
+    from maxwell_solver_gb300 import simFDTD
+    from maxwell_solver_gb300.batch import Batch
+    from maxwell_solver_gb300.workloads import batch_mix, setup_grid
+
+    mix = batch_mix(12)
+    counts = [40 + 5 * g for g in range(len(mix))]
+
+    def fields(P, spec):
+        return [simFDTD("OutputVis", P, np.uint32(spec.cells), np.int32(f)) for f in range(1, 7)]
+
+    want = []
+    for spec, n in zip(mix, counts):
+        P = setup_grid(simFDTD, spec)
+        simFDTD("StepN", P, np.int32([0, n, spec.mode]))
+        want.append(fields(P, spec))
+        simFDTD("DeleteSimulation", P)
+    handles = [setup_grid(simFDTD, spec) for spec in mix]
+    with Batch() as b:
+        for P, spec, n in zip(handles, mix, counts):
+            b.add(P, 0, n, spec.mode)
+        b.run()
+    for g, (P, spec) in enumerate(zip(handles, mix)):
+        for a, w, name in zip(fields(P, spec), want[g], FIELDS):
+            np.testing.assert_array_equal(a, w, err_msg=f"grid {g} {name}")
+        simFDTD("DeleteSimulation", P)
