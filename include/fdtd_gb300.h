@@ -303,9 +303,10 @@ int fdtd_batch_progress(fdtd_batch b, fdtd_handle h, int32_t *done);
  * batch's queued work. */
 int fdtd_batch_remove(fdtd_batch b, fdtd_handle h);
 /* The z-planes per batched work item: measured once per batch (the first
- * step call with at least 8 active members tries 8, 16 and 32 for a few of
- * the members' real steps and keeps the fastest; FDTD_BATCH_ZRUN fixes it);
- * 0 before that.  No reference counterpart. */
+ * step call of more than 12 steps with at least 8 active members runs 4 of
+ * the members' real steps with each of 8, 16 and 32 and keeps the fastest;
+ * FDTD_BATCH_ZRUN fixes it, FDTD_AUTOTUNE=0 keeps 16); 0 before that.  No
+ * reference counterpart. */
 int fdtd_batch_get_zrun(fdtd_batch b, int32_t *zrun);
 /* Waits for the batch's queued work and reports whether every pipelined
  * half-step completed (FDTD_ERR_CUDA if a bounded wait timed out; the
