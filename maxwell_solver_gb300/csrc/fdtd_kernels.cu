@@ -255,6 +255,21 @@ __global__ void k_faces(const fdtd_dev d, const fdtd_op op) {
                          gridDim.x * blockDim.x);
 }
 
+// Batched passes: the block's member descriptor is copied into shared
+// memory once (every thread of the block calls this, after any block-uniform
+// early return), so that the per-cell code reads it there; stores to the
+// fields (global memory) cannot alias it, so the compiler keeps the fields
+// it reads in registers instead of reloading them after every store.
+__device__ __forceinline__ const fdtd_dev &stage_desc(const fdtd_dev *src) {
+  __shared__ __align__(16) fdtd_dev sd;
+  static_assert(sizeof(fdtd_dev) % 16 == 0, "descriptor copy in 16-byte units");
+  const int4 *s4 = reinterpret_cast<const int4 *>(src);
+  int4 *d4 = reinterpret_cast<int4 *>(&sd);
+  for (int t = threadIdx.x; t < (int)(sizeof(fdtd_dev) / 16); t += blockDim.x) d4[t] = s4[t];
+  __syncthreads();
+  return sd;
+}
+
 // Batched: blockIdx.z = active member g (its op says whether it split),
 // blockIdx.y = face plane.
 template <bool HFAM>
@@ -262,7 +277,7 @@ __global__ void k_batch_faces(const fdtd_dev *devs, const fdtd_op *ops, const in
   const int g = blockIdx.z;
   const fdtd_op &op = ops[g];
   if (!op.tfsf_split) return;
-  const fdtd_dev &d = devs[g];
+  const fdtd_dev &d = stage_desc(&devs[g]);
   const int mode = op.tfsf_mode, step = steps[g] + op.step;
   const float *inc = HFAM ? inc_h_row(d, mode, step) : inc_e_row(d, mode, step);
   face_plane_cells<HFAM>(d, mode, inc, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x,
@@ -318,7 +333,7 @@ __global__ void k_e_xslab(const fdtd_dev d) {
 // Batched: blockIdx.y = active member (members without xsplit skip).
 __global__ void k_batch_e_xslab(const fdtd_dev *devs, const fdtd_op *ops) {
   if (!ops[blockIdx.y].xsplit) return;
-  e_xslab_range(devs[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x,
+  e_xslab_range(stage_desc(&devs[blockIdx.y]), blockIdx.x * blockDim.x + threadIdx.x,
                 gridDim.x * blockDim.x);
 }
 
@@ -490,8 +505,8 @@ __global__ void k_batch_faces_oblique(const fdtd_dev *devs, const fdtd_op *ops,
   const int g = blockIdx.z;
   const fdtd_op &op = ops[g];
   if (!op.tfsf_split || op.tfsf_mode != FDTD_MODE_OBLIQUE) return;
-  ob_planes<HFAM>(devs[g], blockIdx.y, steps[g] + op.step, blockIdx.x * blockDim.x + threadIdx.x,
-                  gridDim.x * blockDim.x);
+  ob_planes<HFAM>(stage_desc(&devs[g]), blockIdx.y, steps[g] + op.step,
+                  blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // --------------------------------------------------------------- probes
