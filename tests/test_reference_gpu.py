@@ -131,15 +131,78 @@ def _run_workload(name, steps, timed=0):
     return ours, out, ours_s, ref_s
 
 
+def _ref_graph_s_per_step(name, steps, timed):
+    """Device time per step of the reference's kernels with launch costs
+    taken out: the last `timed` steps captured into one CUDA graph and
+    replayed (the most favourable measure for the reference, whose own
+    loop launches its twelve kernels per step one by one)."""
+    import torch
+
+    from maxwell_solver_gb300.workloads import WORKLOADS, setup
+    from refgpu import RefGPU
+
+    w = WORKLOADS[name]
+    ref = RefGPU(fma=True)
+    setup(ref, w, steps=steps)
+    ref("ResetFieldAll")
+    for k in range(steps - timed):
+        ref.step(k, w.mode)
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    ref.stream = side.cuda_stream
+    with torch.cuda.graph(graph, stream=side):
+        for k in range(steps - timed, steps):
+            ref.step(k, w.mode)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    graph.replay()
+    ev1.record()
+    torch.cuda.synchronize()
+    sec = ev0.elapsed_time(ev1) * 1e-3 / timed
+    del graph
+    ref.close()
+    return sec
+
+
+def _report(rep):
+    """Prints the comparison; with FDTD_REF_GPU_REPORT=path also merges it
+    into that JSON file, keyed by workload."""
+    print(json.dumps(rep))
+    path = os.environ.get("FDTD_REF_GPU_REPORT")
+    if path:
+        allrep = {}
+        if os.path.exists(path):
+            with open(path) as fh:
+                allrep = json.load(fh)
+        allrep[rep["workload"].split()[0]] = rep
+        with open(path, "w") as fh:
+            json.dump(allrep, fh)
+
+
 def test_c1_full_run_equals_reference_kernels():
-    """64^3, 10-cell CPML, TF/SF mode 3, 500 steps."""
-    ours, ref, _, _ = _run_workload("c1", 500)
+    """64^3, 10-cell CPML, TF/SF mode 3, 500 steps (the last 400 timed)."""
+    from maxwell_solver_gb300.workloads import WORKLOADS
+
+    timed = 400
+    ours, ref, ours_s, _ = _run_workload("c1", 500, timed)
+    ref_s = _ref_graph_s_per_step("c1", 500, timed)
     for fam in ("E", "H"):
         assert max(np.abs(ours[fam + c]).max() for c in "xyz") > 0
     for f in FIELDS:
         np.testing.assert_array_equal(ours[f], ref[False][f], err_msg=f)
     err = _family_errors(ours, ref[True])
-    print(json.dumps({"workload": "c1", "contracted_rel_l2": err}))
+    cells = WORKLOADS["c1"].cells
+    _report({"workload": "c1 64^3, 10-cell CPML, vacuum, TF/SF mode 3", "steps": 500,
+             "steps_timed": timed,
+             "reference_kernels_ms_per_step": round(ref_s * 1e3, 4),
+             "reference_kernels_Mcell_steps_per_s": round(cells / ref_s / 1e6, 1),
+             "library_ms_per_step": round(ours_s * 1e3, 4),
+             "library_Mcell_steps_per_s": round(cells / ours_s / 1e6, 1),
+             "speedup": round(ref_s / ours_s, 2), "contracted_rel_l2": err,
+             "timing": "reference: its 400 steps (12 launches each) captured into one CUDA "
+                       "graph and replayed, CUDA events around the replay (device time only); "
+                       "library: wall clock around fdtd_step_n of 400 steps"})
     assert max(err.values()) <= REL_L2, err
 
 
@@ -169,11 +232,7 @@ def test_c3_equals_and_outruns_reference_kernels():
            "timing": "reference: CUDA events around its 32 steps of kernel launches "
                      "(12 per step, the reference's launch shapes); library: wall clock "
                      "around fdtd_step_n of 32 steps and a synchronize (probe gather included)"}
-    print(json.dumps(rep))
-    path = os.environ.get("FDTD_REF_GPU_REPORT")
-    if path:
-        with open(path, "w") as fh:
-            json.dump(rep, fh)
+    _report(rep)
     assert max(err.values()) <= REL_L2, err
     assert ours_s < ref_s
 
