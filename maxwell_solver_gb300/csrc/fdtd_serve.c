@@ -294,18 +294,19 @@ static double solo_step_s(int64_t cells) {
 }
 static double solo_setup_s(int64_t cells) { return 3.0e-3 + (double)cells * 4.6e-10; }
 /* Deadlines use those estimates times FDTD_SERVE_DEADLINE_SCALE (read
- * once; default 1.1: a request may finish up to about 10 % after its time
+ * once; default 1.05: a request may finish up to about 5 % after its time
  * in the one-at-a-time queue, and that slack is what lets the smaller
  * requests go first).  At 1.0 the order stays near the queue's: the median
  * gain is gone while the tail still lands a few % above the queue's, since
  * both run the GPU at the same speed and estimate errors make the
- * deadline order miss by about that much. */
+ * deadline order miss by about that much; at 1.1 the median drops further
+ * and the tail rises by up to a quarter under load. */
 static double deadline_scale(void) {
   static double v = 0.0;
   if (v <= 0.0) {
     const char *e = getenv("FDTD_SERVE_DEADLINE_SCALE");
     const double x = e ? atof(e) : 0.0;
-    v = x > 0.0 ? x : 1.1;
+    v = x > 0.0 ? x : 1.05;
   }
   return v;
 }
